@@ -1,0 +1,227 @@
+// SDDMM: out[e] = A.val[e] * sum_k X[i,k] * Y[j,k] for every stored entry
+// e = (i, j) of a CSR matrix A (for CSC the roles of X and Y swap: the
+// compressed coordinate indexes X).
+//
+// Work is split by stored entries, not by rows, so the power-law row
+// lengths of real graphs do not unbalance the grid: warp w owns entries
+// [w*CH, (w+1)*CH), finds its first row by a binary search of ptr and walks
+// rows forward from there.  Inside the warp, groups of L lanes each own one
+// entry at a time; a lane holds V consecutive k of X[i,:] and Y[j,:] (one
+// 16-byte load each for fp32), the group reduces the L partial dot products
+// with xor-shuffles, and one lane writes out[e].  Y rows are gathered with
+// an evict-last L2 hint; A's idx/val and the output stream with evict-first.
+//
+// FGB_FINCH_ORDER selects one thread per entry and a sequential dot over k
+// ascending, then the product with A.val[e].
+#include "fgb_internal.cuh"
+#include "semiring.cuh"
+
+namespace fgb {
+
+template <class PtrT>
+__device__ __forceinline__ int64_t row_of(const PtrT* ptr, int64_t nrows, int64_t e, int base) {
+  // largest r with ptr[r] - base <= e  (ptr is non-decreasing)
+  int64_t lo = 0, hi = nrows;  // answer in [lo, hi)
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (ld_ptr(ptr, mid) - base <= e) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <class T, int V>
+struct SVec {
+  T v[V];
+};
+
+template <class T, int V>
+__device__ __forceinline__ SVec<T, V> ldv(const T* p, uint64_t pol, bool use_pol) {
+  SVec<T, V> r;
+#pragma unroll
+  for (int q = 0; q < V; ++q) r.v[q] = __ldg(p + q);
+  return r;
+}
+template <>
+__device__ __forceinline__ SVec<float, 4> ldv<float, 4>(const float* p, uint64_t pol, bool use_pol) {
+  float4 f;
+  if (use_pol)
+    f = ld_gather_f32x4(p, pol);
+  else
+    f = __ldg(reinterpret_cast<const float4*>(p));
+  return SVec<float, 4>{{f.x, f.y, f.z, f.w}};
+}
+
+template <class T, class PtrT, int L, int V, int U>
+__global__ void __launch_bounds__(256) sddmm_csr(int64_t nrows, int64_t nnz,
+                                                 const PtrT* __restrict__ ptr,
+                                                 const int* __restrict__ idx,
+                                                 const T* __restrict__ val,
+                                                 const T* __restrict__ X, int64_t ldx,
+                                                 const T* __restrict__ Y, int64_t ldy, int64_t k,
+                                                 T* __restrict__ out, int base, int64_t chunk) {
+  constexpr int GPW = 32 / L;  // groups per warp
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (L - 1);  // lane inside group
+  const int g = lane / L;         // group inside warp
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << (g * L));
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t pol_stream = policy_evict_first();
+  const uint64_t pol_keep = policy_evict_last();
+  for (int64_t c = warp * chunk; c < nnz; c += nwarps * chunk) {
+    const int64_t cend = min(c + chunk, nnz);
+    int64_t row = row_of(ptr, nrows, c, base);
+    int64_t row_end = ld_ptr(ptr, row + 1) - base;
+    for (int64_t e0 = c + g; e0 < cend; e0 += (int64_t)GPW * U) {
+      int64_t e[U];
+      int64_t r[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        e[u] = e0 + (int64_t)u * GPW;
+        ok[u] = e[u] < cend;
+        if (ok[u]) {
+          while (e[u] >= row_end) {
+            ++row;
+            row_end = ld_ptr(ptr, row + 1) - base;
+          }
+        }
+        r[u] = row;
+      }
+      T dot[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) dot[u] = T(0);
+      int jj[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) jj[u] = ok[u] ? ld_stream_i32(idx + e[u], pol_stream) - base : 0;
+      for (int64_t k0 = (int64_t)gl * V; k0 < k; k0 += (int64_t)L * V) {
+        SVec<T, V> xv[U], yv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) {
+            xv[u] = ldv<T, V>(X + r[u] * ldx + k0, pol_keep, false);
+            yv[u] = ldv<T, V>(Y + (int64_t)jj[u] * ldy + k0, pol_keep, true);
+          }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u])
+#pragma unroll
+            for (int q = 0; q < V; ++q) dot[u] = fused(xv[u].v[q], yv[u].v[q], dot[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int m = L / 2; m >= 1; m >>= 1) dot[u] += __shfl_xor_sync(gmask, dot[u], m, L);
+        if (ok[u] && gl == 0) out[e[u]] = wmul(__ldg(val + e[u]), dot[u]);
+      }
+    }
+  }
+}
+
+// One thread per entry, sequential dot over k ascending.
+template <class T, class PtrT>
+__global__ void sddmm_csr_serial(int64_t nrows, int64_t nnz, const PtrT* __restrict__ ptr,
+                                 const int* __restrict__ idx, const T* __restrict__ val,
+                                 const T* __restrict__ X, int64_t ldx, const T* __restrict__ Y,
+                                 int64_t ldy, int64_t k, T* __restrict__ out, int base, int fm) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = row_of(ptr, nrows, e, base);
+    const int64_t j = __ldg(idx + e) - base;
+    T acc = T(0);
+    for (int64_t q = 0; q < k; ++q)
+      acc = Semi<SR_PT, T>::step(acc, X[i * ldx + q], Y[j * ldy + q], fm);
+    out[e] = wmul(val[e], acc);
+  }
+}
+
+template <class T, class PtrT>
+static int run(fgb_ctx* ctx, const fgb_sparse* A, const T* X, int64_t ldx, const T* Y,
+               int64_t ldy, int64_t k, T* out, unsigned flags, int lanes, int64_t chunk,
+               cudaStream_t s) {
+  const int64_t nf = n_fibers(A);
+  const int64_t nnz = A->nnz;
+  if (nnz == 0) return FGB_OK;
+  const PtrT* ptr = (const PtrT*)A->ptr;
+  const int* idx = (const int*)A->idx;
+  const T* val = (const T*)A->val;
+  const int base = A->index_base;
+  const int threads = 256;
+  if (flags & FGB_FINCH_ORDER) {
+    const int fm = (flags & FGB_NO_FMA) ? FM_NOFMA : FM_FMA;
+    sddmm_csr_serial<T, PtrT><<<grid_for(nnz, threads, ctx->num_sms, 8), threads, 0, s>>>(
+        nf, nnz, ptr, idx, val, X, ldx, Y, ldy, k, out, base, fm);
+    return check_launch("sddmm_csr_serial");
+  }
+  if (chunk <= 0) chunk = 256;
+  const int64_t nchunks = (nnz + chunk - 1) / chunk;
+  const int grid = grid_for(nchunks * 32, threads, ctx->num_sms, 8);
+  constexpr int VN = sizeof(T) == 4 ? 4 : 1;
+  const bool vec_ok = VN > 1 && k % VN == 0 && ldx % VN == 0 && ldy % VN == 0 &&
+                      (uintptr_t)X % 16 == 0 && (uintptr_t)Y % 16 == 0;
+  if (lanes <= 0) {
+    const int64_t need = vec_ok ? (k + VN - 1) / VN : k;
+    lanes = need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+  }
+#define FGB_SDDMM(LL, VV, UU)                                                            \
+  sddmm_csr<T, PtrT, LL, VV, UU><<<grid, threads, 0, s>>>(nf, nnz, ptr, idx, val, X, ldx, Y, \
+                                                          ldy, k, out, base, chunk)
+  if (vec_ok) {
+    switch (lanes) {
+      case 4: FGB_SDDMM(4, VN, 2); break;
+      case 8: FGB_SDDMM(8, VN, 2); break;
+      case 16: FGB_SDDMM(16, VN, 4); break;
+      default: FGB_SDDMM(32, VN, 4); break;
+    }
+  } else {
+    switch (lanes) {
+      case 4: FGB_SDDMM(4, 1, 2); break;
+      case 8: FGB_SDDMM(8, 1, 2); break;
+      case 16: FGB_SDDMM(16, 1, 4); break;
+      default: FGB_SDDMM(32, 1, 4); break;
+    }
+  }
+#undef FGB_SDDMM
+  return check_launch("sddmm_csr");
+}
+
+int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
+               int64_t ldy, int64_t k, void* out, int dtype, unsigned flags, int lanes,
+               int64_t chunk, void* stream) {
+  if (!ctx) return set_error(FGB_EINVAL, "fgb_sddmm: null ctx");
+  int rc = check_sparse(A, "fgb_sddmm: A", true);
+  if (rc) return rc;
+  if (k < 0 || ldx < k || ldy < k) return set_error(FGB_EINVAL, "fgb_sddmm: bad k/ldx/ldy");
+  if (A->val_t != dtype)
+    return set_error(FGB_EUNSUPPORTED, "fgb_sddmm: A values must have the output dtype");
+  if (A->nnz > 0 && (!X || !Y || !out)) return set_error(FGB_EINVAL, "fgb_sddmm: null operand");
+  // For CSC the compressed coordinate is j, so X and Y trade places.
+  const void* Xc = A->orient == FGB_CSR ? X : Y;
+  const void* Yc = A->orient == FGB_CSR ? Y : X;
+  const int64_t ldxc = A->orient == FGB_CSR ? ldx : ldy;
+  const int64_t ldyc = A->orient == FGB_CSR ? ldy : ldx;
+  cudaStream_t s = pick_stream(ctx, stream);
+  if (dtype == FGB_F32) {
+    if (A->ptr_t == FGB_I32)
+      return run<float, int32_t>(ctx, A, (const float*)Xc, ldxc, (const float*)Yc, ldyc, k,
+                                 (float*)out, flags, lanes, chunk, s);
+    return run<float, int64_t>(ctx, A, (const float*)Xc, ldxc, (const float*)Yc, ldyc, k,
+                               (float*)out, flags, lanes, chunk, s);
+  }
+  if (dtype == FGB_F64) {
+    if (A->ptr_t == FGB_I32)
+      return run<double, int32_t>(ctx, A, (const double*)Xc, ldxc, (const double*)Yc, ldyc, k,
+                                  (double*)out, flags, lanes, chunk, s);
+    return run<double, int64_t>(ctx, A, (const double*)Xc, ldxc, (const double*)Yc, ldyc, k,
+                                (double*)out, flags, lanes, chunk, s);
+  }
+  return set_error(FGB_EUNSUPPORTED, "fgb_sddmm: dtype %d", dtype);
+}
+
+}  // namespace fgb
+
+extern "C" int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
+                         const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
+                         unsigned flags, void* stream) {
+  return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, 0, 0, stream);
+}

@@ -1,0 +1,281 @@
+// SpMM: C[i,k] += A[i,j] * B[j,k] over a SparseList matrix A and a
+// row-major dense B (k fastest).
+//
+// CSR (pull).  A group of G lanes owns one row i and a column slab
+// [c0, c0 + G*V) of C; each lane holds V consecutive k in registers.  The
+// group walks the row's stored entries in order, G at a time: every lane
+// loads one (j, a) pair with a coalesced streaming load, then the pairs are
+// broadcast by shuffles and each lane gathers its V-wide piece of B[j, :]
+// (one 16-byte load for fp32) and updates its accumulators.  Every C[i,k] is
+// therefore one running sum over j ascending -- Finch's serial order -- and
+// the results equal Finch's CPU nest for the same contraction choice.
+//
+// When B does not fit in L2 the columns are processed as slabs (one launch
+// per slab, slab width G*V): the rows of a slab of B are gathered from L2
+// while A's idx/val stream through with evict-first hints.
+//
+// CSC (push).  A group owns column j of A (row j of B) and adds a*B[j, :]
+// into C[i, :] with atomics.
+#include "fgb_internal.cuh"
+#include "semiring.cuh"
+
+namespace fgb {
+
+template <class T, int V>
+struct VecT {
+  T v[V];
+};
+
+template <class T, int V>
+__device__ __forceinline__ VecT<T, V> gather(const T* p, uint64_t pol);
+
+template <>
+__device__ __forceinline__ VecT<float, 4> gather<float, 4>(const float* p, uint64_t pol) {
+  float4 f = ld_gather_f32x4(p, pol);
+  return VecT<float, 4>{{f.x, f.y, f.z, f.w}};
+}
+template <>
+__device__ __forceinline__ VecT<double, 2> gather<double, 2>(const double* p, uint64_t pol) {
+  double2 d;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;"
+               : "=d"(d.x), "=d"(d.y)
+               : "l"(p), "l"(pol));
+  return VecT<double, 2>{{d.x, d.y}};
+}
+template <>
+__device__ __forceinline__ VecT<float, 1> gather<float, 1>(const float* p, uint64_t) {
+  return VecT<float, 1>{{__ldg(p)}};
+}
+template <>
+__device__ __forceinline__ VecT<double, 1> gather<double, 1>(const double* p, uint64_t) {
+  return VecT<double, 1>{{__ldg(p)}};
+}
+
+template <class T, int V>
+__device__ __forceinline__ void store_out(T* p, const VecT<T, V>& a, uint64_t pol) {
+#pragma unroll
+  for (int q = 0; q < V; ++q) p[q] = a.v[q];
+}
+template <>
+__device__ __forceinline__ void store_out<float, 4>(float* p, const VecT<float, 4>& a,
+                                                     uint64_t pol) {
+  st_stream_f32x4(p, make_float4(a.v[0], a.v[1], a.v[2], a.v[3]), pol);
+}
+
+template <class T, int V>
+__device__ __forceinline__ VecT<T, V> load_out(const T* p) {
+  VecT<T, V> r;
+#pragma unroll
+  for (int q = 0; q < V; ++q) r.v[q] = p[q];
+  return r;
+}
+
+// Value of stored entry p as the accumulation type.
+template <class T, class VT>
+__device__ __forceinline__ T load_val(const VT* val, int64_t p, uint64_t pol) {
+  return to_acc<T>(__ldg(val + p));
+}
+template <>
+__device__ __forceinline__ float load_val<float, float>(const float* val, int64_t p, uint64_t pol) {
+  return ld_stream_f32(val + p, pol);
+}
+
+template <class T, int V>
+__device__ __forceinline__ void acc_step(VecT<T, V>& acc, T a, const VecT<T, V>& b, int fm) {
+#pragma unroll
+  for (int q = 0; q < V; ++q) acc.v[q] = Semi<SR_PT, T>::step(acc.v[q], a, b.v[q], fm);
+}
+
+// One launch = one column slab [c0, c0 + G*V) (clipped to nk) of every row.
+template <class T, class VT, class PtrT, int G, int V>
+__global__ void __launch_bounds__(256) spmm_csr_pull(
+    int64_t nrows, const PtrT* __restrict__ ptr, const int* __restrict__ idx,
+    const VT* __restrict__ val, const T* __restrict__ B, int64_t ldb, T* __restrict__ C,
+    int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, int fm) {
+  constexpr int BATCH = 8;
+  const int lane = threadIdx.x & (G - 1);
+  const unsigned gmask =
+      G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t col = c0 + (int64_t)lane * V;
+  const bool active_col = col < nk;  // V divides nk - c0 in the vector path
+  const uint64_t pol_stream = policy_evict_first();
+  const uint64_t pol_keep = policy_evict_last();
+  for (int64_t row = group; row < nrows; row += ngroups) {
+    const int64_t p0 = ld_ptr(ptr, row) - base;
+    const int64_t p1 = ld_ptr(ptr, row + 1) - base;
+    VecT<T, V> acc;
+    if (accumulate && active_col)
+      acc = load_out<T, V>(C + row * ldc + col);
+    else
+#pragma unroll
+      for (int q = 0; q < V; ++q) acc.v[q] = T(0);
+    for (int64_t pb = p0; pb < p1; pb += G) {
+      const int64_t pe = pb + lane;
+      int my_j = 0;
+      T my_a = T(0);
+      if (pe < p1) {
+        my_j = ld_stream_i32(idx + pe, pol_stream) - base;
+        my_a = load_val<T, VT>(val, pe, pol_stream);
+      }
+      const int cnt = (p1 - pb) < (int64_t)G ? (int)(p1 - pb) : G;
+#pragma unroll
+      for (int t0 = 0; t0 < G; t0 += BATCH) {
+        if (t0 >= cnt) break;
+        VecT<T, V> b[BATCH];
+        T a[BATCH];
+#pragma unroll
+        for (int t = 0; t < BATCH; ++t) {
+          const int src = t0 + t < G ? t0 + t : 0;
+          const int j = __shfl_sync(gmask, my_j, src, G);
+          a[t] = __shfl_sync(gmask, my_a, src, G);
+          if (t0 + t < cnt && active_col)
+            b[t] = gather<T, V>(B + (int64_t)j * ldb + col, pol_keep);
+        }
+#pragma unroll
+        for (int t = 0; t < BATCH; ++t)
+          if (t0 + t < cnt && active_col) acc_step<T, V>(acc, a[t], b[t], fm);
+      }
+    }
+    if (active_col) store_out<T, V>(C + row * ldc + col, acc, pol_stream);
+  }
+}
+
+template <class T, class VT, class PtrT>
+__global__ void __launch_bounds__(256) spmm_csc_push(int64_t ncols_a, const PtrT* __restrict__ ptr,
+                                                     const int* __restrict__ idx,
+                                                     const VT* __restrict__ val,
+                                                     const T* __restrict__ B, int64_t ldb,
+                                                     T* __restrict__ C, int64_t ldc, int64_t nk,
+                                                     int base) {
+  // one warp per column j of A; lanes stride over k
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = w; j < ncols_a; j += nw) {
+    const int64_t p0 = ld_ptr(ptr, j) - base, p1 = ld_ptr(ptr, j + 1) - base;
+    for (int64_t p = p0; p < p1; ++p) {
+      const int i = __ldg(idx + p) - base;
+      const T a = to_acc<T>(__ldg(val + p));
+      for (int64_t k = lane; k < nk; k += 32) atomicAdd(C + (int64_t)i * ldc + k, a * __ldg(B + j * ldb + k));
+    }
+  }
+}
+
+template <class T>
+__global__ void zero_rows(T* C, int64_t m, int64_t nk, int64_t ldc) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * nk;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / nk, k = e - i * nk;
+    C[i * ldc + k] = T(0);
+  }
+}
+
+template <class T, class VT, class PtrT, int G, int V>
+static int launch_pull(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                       void* C, int64_t ldc, int accumulate, int fm, cudaStream_t s) {
+  const int64_t m = A->nrows;
+  const int64_t slab = (int64_t)G * V;
+  const int threads = 256;
+  const int grid = grid_for(m * G, threads, ctx->num_sms, 8);
+  for (int64_t c0 = 0; c0 < nk; c0 += slab) {
+    spmm_csr_pull<T, VT, PtrT, G, V><<<grid, threads, 0, s>>>(
+        m, (const PtrT*)A->ptr, (const int*)A->idx, (const VT*)A->val, (const T*)B, ldb, (T*)C,
+        ldc, c0, nk, A->index_base, accumulate, fm);
+    int rc = check_launch("spmm_csr_pull");
+    if (rc) return rc;
+  }
+  return FGB_OK;
+}
+
+// Slab width in lanes: the whole of nk when it fits one warp, else the
+// widest group that keeps the gathered slab of B near L2 capacity.
+template <class T, class VT, class PtrT>
+static int dispatch_pull(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                         void* C, int64_t ldc, int accumulate, int fm, int lanes, cudaStream_t s) {
+  constexpr int VN = sizeof(T) == 4 ? 4 : 2;
+  const bool vec_ok = (nk % VN == 0) && (ldb % VN == 0) && (ldc % VN == 0) &&
+                      ((uintptr_t)B % (VN * sizeof(T)) == 0) && ((uintptr_t)C % (VN * sizeof(T)) == 0);
+  if (vec_ok) {
+    switch (lanes) {
+      case 4: return launch_pull<T, VT, PtrT, 4, VN>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+      case 8: return launch_pull<T, VT, PtrT, 8, VN>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+      case 16: return launch_pull<T, VT, PtrT, 16, VN>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+      default: return launch_pull<T, VT, PtrT, 32, VN>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+    }
+  }
+  switch (lanes) {
+    case 4: return launch_pull<T, VT, PtrT, 4, 1>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+    case 8: return launch_pull<T, VT, PtrT, 8, 1>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+    case 16: return launch_pull<T, VT, PtrT, 16, 1>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+    default: return launch_pull<T, VT, PtrT, 32, 1>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, s);
+  }
+}
+
+static int default_lanes(int64_t nk, int vn, int64_t b_bytes) {
+  // lanes needed to cover nk in one slab
+  int64_t need = (nk + vn - 1) / vn;
+  int lanes = need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+  (void)b_bytes;
+  return lanes;
+}
+
+template <class T, class VT>
+static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                     void* C, int64_t ldc, unsigned flags, int lanes, cudaStream_t s) {
+  const int accumulate = (flags & FGB_ACCUMULATE) ? 1 : 0;
+  int fm = FM_DEFAULT;
+  if (flags & FGB_NO_FMA) fm = FM_NOFMA;
+  if (flags & FGB_FMA) fm = FM_FMA;
+  if (A->orient == FGB_CSR) {
+    if (A->nrows == 0 || nk == 0) return FGB_OK;
+    if (lanes <= 0) lanes = default_lanes(nk, sizeof(T) == 4 ? 4 : 2, A->ncols * nk * (int64_t)sizeof(T));
+    if (A->ptr_t == FGB_I32)
+      return dispatch_pull<T, VT, int32_t>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, lanes, s);
+    return dispatch_pull<T, VT, int64_t>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, lanes, s);
+  }
+  if (flags & FGB_FINCH_ORDER)
+    return set_error(FGB_EUNSUPPORTED, "fgb_spmm: FGB_FINCH_ORDER needs a CSR matrix");
+  if (A->nrows == 0 || nk == 0) return FGB_OK;
+  const int threads = 256;
+  if (!accumulate) {
+    zero_rows<T><<<grid_for(A->nrows * nk, threads, ctx->num_sms, 4), threads, 0, s>>>((T*)C, A->nrows, nk, ldc);
+    int rc = check_launch("zero_rows");
+    if (rc) return rc;
+  }
+  const int grid = grid_for(A->ncols * 32, threads, ctx->num_sms, 8);
+  if (A->ptr_t == FGB_I32)
+    spmm_csc_push<T, VT, int32_t><<<grid, threads, 0, s>>>(A->ncols, (const int32_t*)A->ptr, (const int*)A->idx,
+                                                          (const VT*)A->val, (const T*)B, ldb, (T*)C, ldc, nk, A->index_base);
+  else
+    spmm_csc_push<T, VT, int64_t><<<grid, threads, 0, s>>>(A->ncols, (const int64_t*)A->ptr, (const int*)A->idx,
+                                                          (const VT*)A->val, (const T*)B, ldb, (T*)C, ldc, nk, A->index_base);
+  return check_launch("spmm_csc_push");
+}
+
+int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
+              int64_t ldc, int dtype, unsigned flags, int lanes, void* stream) {
+  if (!ctx) return set_error(FGB_EINVAL, "fgb_spmm: null ctx");
+  int rc = check_sparse(A, "fgb_spmm: A", true);
+  if (rc) return rc;
+  if (nk < 0 || ldb < nk || ldc < nk) return set_error(FGB_EINVAL, "fgb_spmm: bad nk/ldb/ldc");
+  if ((A->ncols > 0 && nk > 0 && !B) || (A->nrows > 0 && nk > 0 && !C))
+    return set_error(FGB_EINVAL, "fgb_spmm: null B or C");
+  cudaStream_t s = pick_stream(ctx, stream);
+  if (dtype == FGB_F32) {
+    if (A->val_t == FGB_F32) return run_typed<float, float>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+    if (A->val_t == FGB_BF16)
+      return run_typed<float, __nv_bfloat16>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+  } else if (dtype == FGB_F64) {
+    if (A->val_t == FGB_F64) return run_typed<double, double>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+  }
+  return set_error(FGB_EUNSUPPORTED, "fgb_spmm: no kernel for val %d / dtype %d", A->val_t, dtype);
+}
+
+}  // namespace fgb
+
+extern "C" int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                        void* C, int64_t ldc, int dtype, unsigned flags, void* stream) {
+  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, 0, stream);
+}

@@ -1,0 +1,204 @@
+// Semiring SpMV over SparseList fibers.
+//
+// CSR (pull): a group of G lanes owns one row i and folds
+//   acc = (+)_{j ascending} A[i,j] (*) x[j]
+// lane-strided over the row's stored entries, then combines the G partials
+// with xor-shuffles.  G = 1 is Finch's serial order: one running value per
+// output, updated j ascending, exactly the update
+//   y[i] = x[j] * A[i,j] + y[i]
+// of Finch's CSC nest (test/reference64/typical/typical_spmv_csc.txt:61-79),
+// so FGB_FINCH_ORDER results equal Finch's bit for bit.
+//
+// CSC (push): a group of G lanes owns one column j, reads x[j] once and
+// applies y[i] <<(+)>>= A[i,j] (*) x[j] for every stored i with an atomic
+// update.  For exact semirings (integer +, min, max, |) the atomics commute,
+// so results are exact; float sums are exact up to summation order.
+#include "fgb_internal.cuh"
+#include "semiring.cuh"
+
+namespace fgb {
+
+template <int SR, class VT, class A, class PtrT, int G, bool PATTERN>
+__global__ void __launch_bounds__(256) spmv_csr_pull(int64_t nrows, const PtrT* __restrict__ ptr,
+                                                     const int* __restrict__ idx,
+                                                     const VT* __restrict__ val,
+                                                     const A* __restrict__ x, A* __restrict__ y,
+                                                     int base, int accumulate, int fm) {
+  using S = Semi<SR, A>;
+  const int lane = threadIdx.x & (G - 1);
+  const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+  for (int64_t row = group; row < nrows; row += ngroups) {
+    const int64_t p0 = ld_ptr(ptr, row) - base;
+    const int64_t p1 = ld_ptr(ptr, row + 1) - base;
+    A acc = (G == 1 && accumulate) ? y[row] : S::identity();
+#pragma unroll 4
+    for (int64_t p = p0 + lane; p < p1; p += G) {
+      const int j = __ldg(idx + p) - base;
+      const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
+      acc = S::step(acc, a, __ldg(x + j), fm);
+    }
+    if (G > 1) {
+#pragma unroll
+      for (int m = G / 2; m >= 1; m >>= 1) acc = S::add(acc, shfl_xor(group_mask<G>(), acc, m, G));
+      if (lane == 0) y[row] = accumulate ? S::add(y[row], acc) : acc;
+    } else {
+      y[row] = acc;
+    }
+  }
+}
+
+template <int SR, class VT, class A, class PtrT, int G, bool PATTERN>
+__global__ void __launch_bounds__(256) spmv_csc_push(int64_t ncols, const PtrT* __restrict__ ptr,
+                                                     const int* __restrict__ idx,
+                                                     const VT* __restrict__ val,
+                                                     const A* __restrict__ x, A* __restrict__ y,
+                                                     int base) {
+  using S = Semi<SR, A>;
+  const int lane = threadIdx.x & (G - 1);
+  const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+  for (int64_t col = group; col < ncols; col += ngroups) {
+    const int64_t p0 = ld_ptr(ptr, col) - base;
+    const int64_t p1 = ld_ptr(ptr, col + 1) - base;
+    if (p0 >= p1) continue;
+    const A xj = __ldg(x + col);
+    for (int64_t p = p0 + lane; p < p1; p += G) {
+      const int i = __ldg(idx + p) - base;
+      const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
+      AtomicAdd<SR, A>::apply(y + i, S::mul(a, xj));
+    }
+  }
+}
+
+template <int SR, class A>
+__global__ void fill_identity(A* __restrict__ y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = Semi<SR, A>::identity();
+}
+
+static int pick_group(double avg) {
+  if (avg <= 2.0) return 1;
+  if (avg <= 8.0) return 4;
+  if (avg <= 24.0) return 8;
+  return 32;
+}
+
+template <int SR, class VT, class A, class PtrT, bool PATTERN>
+static int launch_typed(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void* y, unsigned flags,
+                        cudaStream_t s) {
+  const int base = A_->index_base;
+  const int64_t nf = n_fibers(A_);
+  const PtrT* ptr = (const PtrT*)A_->ptr;
+  const int* idx = (const int*)A_->idx;
+  const VT* val = (const VT*)A_->val;
+  const double avg = nf ? (double)A_->nnz / (double)nf : 0.0;
+  const int threads = 256;
+  if (A_->orient == FGB_CSR) {
+    const int accumulate = (flags & FGB_ACCUMULATE) ? 1 : 0;
+    int fm = FM_DEFAULT;
+    if (flags & FGB_NO_FMA) fm = FM_NOFMA;
+    if (flags & FGB_FMA) fm = FM_FMA;
+    int G = (flags & FGB_FINCH_ORDER) ? 1 : pick_group(avg);
+    int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
+    if (nf == 0) return FGB_OK;
+#define FGB_PULL(GG)                                                                    \
+  spmv_csr_pull<SR, VT, A, PtrT, GG, PATTERN><<<grid, threads, 0, s>>>(                 \
+      nf, ptr, idx, val, (const A*)x, (A*)y, base, accumulate, fm)
+    switch (G) {
+      case 1: FGB_PULL(1); break;
+      case 4: FGB_PULL(4); break;
+      case 8: FGB_PULL(8); break;
+      default: FGB_PULL(32); break;
+    }
+#undef FGB_PULL
+    return check_launch("spmv_csr_pull");
+  }
+  // CSC push
+  const int64_t m = A_->nrows;
+  if (!(flags & FGB_ACCUMULATE) && m > 0) {
+    fill_identity<SR, A><<<grid_for(m, threads, ctx->num_sms, 4), threads, 0, s>>>((A*)y, m);
+    int rc = check_launch("fill_identity");
+    if (rc) return rc;
+  }
+  if (nf == 0) return FGB_OK;
+  int G = avg <= 4.0 ? 1 : (avg <= 16.0 ? 8 : 32);
+  int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
+#define FGB_PUSH(GG)                                                                    \
+  spmv_csc_push<SR, VT, A, PtrT, GG, PATTERN><<<grid, threads, 0, s>>>(nf, ptr, idx, val, \
+                                                                      (const A*)x, (A*)y, base)
+  switch (G) {
+    case 1: FGB_PUSH(1); break;
+    case 8: FGB_PUSH(8); break;
+    default: FGB_PUSH(32); break;
+  }
+#undef FGB_PUSH
+  return check_launch("spmv_csc_push");
+}
+
+template <int SR, class VT, class A, bool PATTERN = false>
+static int launch_ptr(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void* y, unsigned flags,
+                      cudaStream_t s) {
+  if (A_->ptr_t == FGB_I32)
+    return launch_typed<SR, VT, A, int32_t, PATTERN>(ctx, A_, x, y, flags, s);
+  return launch_typed<SR, VT, A, int64_t, PATTERN>(ctx, A_, x, y, flags, s);
+}
+
+template <int SR>
+static int dispatch_numeric(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, int x_t, void* y,
+                            int y_t, unsigned flags, cudaStream_t s) {
+  const int v = A_->val_t;
+  if (x_t != y_t) return set_error(FGB_EUNSUPPORTED, "fgb_spmv: x and y dtypes differ");
+  switch (y_t) {
+    case FGB_F64:
+      if (v == FGB_F64) return launch_ptr<SR, double, double>(ctx, A_, x, y, flags, s);
+      break;
+    case FGB_F32:
+      if (v == FGB_F32) return launch_ptr<SR, float, float>(ctx, A_, x, y, flags, s);
+      if (v == FGB_BF16 && SR == SR_PT)
+        return launch_ptr<SR_PT, __nv_bfloat16, float>(ctx, A_, x, y, flags, s);
+      break;
+    case FGB_I32:
+      if (v == FGB_I32) return launch_ptr<SR, int32_t, int32_t>(ctx, A_, x, y, flags, s);
+      break;
+    case FGB_I64:
+      if (v == FGB_I64) return launch_ptr<SR, int64_t, int64_t>(ctx, A_, x, y, flags, s);
+      break;
+    default: break;
+  }
+  return set_error(FGB_EUNSUPPORTED, "fgb_spmv: no kernel for semiring %d with val %d, x/y %d", SR,
+                   v, y_t);
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* x, int x_t,
+                        void* y, int y_t, unsigned flags, void* stream) {
+  if (!ctx) return set_error(FGB_EINVAL, "fgb_spmv: null ctx");
+  int rc = check_sparse(A, "fgb_spmv: A", true);
+  if (rc) return rc;
+  const int64_t n_in = A->ncols, n_out = A->nrows;
+  if ((n_in > 0 && !x) || (n_out > 0 && !y)) return set_error(FGB_EINVAL, "fgb_spmv: null x or y");
+  if ((flags & FGB_FINCH_ORDER) && A->orient != FGB_CSR)
+    return set_error(FGB_EUNSUPPORTED,
+                     "fgb_spmv: FGB_FINCH_ORDER needs a CSR matrix (transpose once with "
+                     "fgb_transpose)");
+  cudaStream_t s = pick_stream(ctx, stream);
+  switch (semiring) {
+    case FGB_PLUS_TIMES: return dispatch_numeric<SR_PT>(ctx, A, x, x_t, y, y_t, flags, s);
+    case FGB_MIN_PLUS: return dispatch_numeric<SR_MINP>(ctx, A, x, x_t, y, y_t, flags, s);
+    case FGB_MAX_PLUS: return dispatch_numeric<SR_MAXP>(ctx, A, x, x_t, y, y_t, flags, s);
+    case FGB_OR_AND:
+      if (x_t != FGB_BOOL || y_t != FGB_BOOL)
+        return set_error(FGB_EUNSUPPORTED, "fgb_spmv: OR_AND needs Bool x and y");
+      if (A->val_t == FGB_NONE)
+        return launch_ptr<SR_OA, uint8_t, uint8_t, true>(ctx, A, x, y, flags, s);
+      if (A->val_t == FGB_BOOL)
+        return launch_ptr<SR_OA, uint8_t, uint8_t, false>(ctx, A, x, y, flags, s);
+      return set_error(FGB_EUNSUPPORTED, "fgb_spmv: OR_AND needs Bool or Pattern values");
+    default: return set_error(FGB_EINVAL, "fgb_spmv: unknown semiring %d", semiring);
+  }
+}

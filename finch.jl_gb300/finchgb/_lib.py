@@ -1,0 +1,111 @@
+"""ctypes binding of libfinchgb.so, the C ABI declared in include/finchgb.h.
+
+This is the same binding a Julia `ccall` layer makes:
+plain pointers, sizes and int status codes.  There is no CPU fallback: if
+the shared library is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from ctypes import POINTER, c_double, c_int, c_int32, c_int64, c_size_t, c_uint, c_uint64, c_void_p, c_char_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_native" / "libfinchgb.so"
+
+# fgb_status
+OK, EINVAL, ENOMEM, ETIMEOUT, ECUDA, EUNSUPPORTED, EBUSY, ECANCELLED = range(8)
+STATUS_NAMES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ETIMEOUT", 4: "ECUDA", 5: "EUNSUPPORTED",
+                6: "EBUSY", 7: "ECANCELLED"}
+# fgb_dtype
+NONE, F64, F32, BF16, I32, I64, BOOL = -1, 0, 1, 2, 3, 4, 5
+# fgb_semiring
+PLUS_TIMES, MIN_PLUS, MAX_PLUS, OR_AND = 0, 1, 2, 3
+# fgb_orient
+CSR, CSC = 0, 1
+# flags
+ACCUMULATE, FINCH_ORDER, FMA, NO_FMA = 0x1, 0x2, 0x4, 0x8
+# fgb_ewise_op
+EW_MUL, EW_ADD = 0, 1
+
+
+class FinchGBError(RuntimeError):
+    """A libfinchgb call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"[{STATUS_NAMES.get(status, status)}] {message}")
+
+
+class FgbSparse(ctypes.Structure):
+    _fields_ = [("nrows", c_int64), ("ncols", c_int64), ("nnz", c_int64), ("orient", c_int32),
+                ("index_base", c_int32), ("ptr_t", c_int32), ("idx_t", c_int32),
+                ("val_t", c_int32), ("reserved", c_int32), ("ptr", c_void_p), ("idx", c_void_p),
+                ("val", c_void_p)]
+
+
+# name -> (restype, argtypes); every symbol include/finchgb.h declares.
+SIGNATURES: dict[str, tuple] = {
+    "fgb_version": (c_int, []),
+    "fgb_last_error": (c_char_p, []),
+    "fgb_ctx_create": (c_int, [c_int, POINTER(c_void_p)]),
+    "fgb_ctx_destroy": (c_int, [c_void_p]),
+    "fgb_ctx_stream": (c_void_p, [c_void_p]),
+    "fgb_ctx_num_sms": (c_int, [c_void_p]),
+    "fgb_malloc": (c_int, [c_void_p, c_size_t, POINTER(c_void_p)]),
+    "fgb_free": (c_int, [c_void_p, c_void_p]),
+    "fgb_host_alloc": (c_int, [c_void_p, c_size_t, POINTER(c_void_p)]),
+    "fgb_host_free": (c_int, [c_void_p, c_void_p]),
+    "fgb_upload": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fgb_download": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fgb_stream_sync": (c_int, [c_void_p, c_void_p]),
+    "fgb_narrow_index": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p]),
+    "fgb_transpose": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_spmv": (c_int, [c_void_p, c_int, POINTER(FgbSparse), c_void_p, c_int, c_void_p, c_int,
+                         c_uint, c_void_p]),
+    "fgb_spmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,
+                         c_int64, c_int, c_uint, c_void_p]),
+    "fgb_sddmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
+                          c_int64, c_void_p, c_int, c_uint, c_void_p]),
+    "fgb_ewise_count": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
+                                POINTER(c_int64), c_void_p]),
+    "fgb_ewise_fill": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
+                               c_void_p, c_void_p, c_void_p]),
+    "fgb_ewise_reduce": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
+                                 c_int64, c_void_p, c_int, c_uint, c_void_p]),
+}
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+def load() -> ctypes.CDLL:
+    """Loads libfinchgb.so (built in-tree); raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise FinchGBError(ECUDA, f"libfinchgb.so not built ({LIB_PATH}); run "
+                                          "__graft_entry__.build() -- there is no CPU fallback")
+            L = ctypes.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    msg = load().fgb_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        raise FinchGBError(status, f"{what}: {last_error()}" if what else last_error())
+
+
+def call(name: str, *args) -> None:
+    """Calls an entry point and raises FinchGBError on a non-zero status."""
+    check(getattr(load(), name)(*args), name)

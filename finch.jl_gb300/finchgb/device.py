@@ -1,0 +1,233 @@
+"""Device-resident level buffers and the kernel calls behind the matcher.
+
+`DeviceSparse` is a SparseList matrix whose ptr/idx/val live in HBM -- what
+Finch's `transfer(device, lvl)` recursion (src/tensors/levels/
+sparse_list_levels.jl:64-69, element_levels.jl:46-48) produces for a GPU
+device.  Finch's 1-based Int64 idx are narrowed to int32 once, at upload,
+and keep their base; ptr stays Int64 only when nnz needs it.
+
+PyTorch supplies device memory and the current stream; every computation is
+a libfinchgb call.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+_TORCH_CODE = {torch.float64: L.F64, torch.float32: L.F32, torch.bfloat16: L.BF16,
+               torch.int32: L.I32, torch.int64: L.I64, torch.uint8: L.BOOL, torch.bool: L.BOOL}
+_NP_TO_TORCH = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+                np.dtype(np.int32): torch.int32, np.dtype(np.int64): torch.int64,
+                np.dtype(np.bool_): torch.uint8, np.dtype(np.uint8): torch.uint8}
+
+_ctxs: dict[int, ctypes.c_void_p] = {}
+
+
+def require_gpu() -> None:
+    if not torch.cuda.is_available():
+        raise L.FinchGBError(L.ECUDA, "no CUDA device: the GB300 backend has no CPU fallback")
+
+
+def context(device: int | None = None) -> ctypes.c_void_p:
+    """The libfinchgb context of `device` (created on first use)."""
+    require_gpu()
+    dev = torch.cuda.current_device() if device is None else int(device)
+    if dev not in _ctxs:
+        h = ctypes.c_void_p()
+        L.call("fgb_ctx_create", dev, ctypes.byref(h))
+        _ctxs[dev] = h
+    return _ctxs[dev]
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def dtype_code(t: torch.Tensor | None) -> int:
+    return L.NONE if t is None else _TORCH_CODE[t.dtype]
+
+
+def _dptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None or t.numel() == 0 else t.data_ptr()
+
+
+@dataclass
+class DeviceSparse:
+    """A 2-D SparseList matrix in HBM.
+
+    orient 'csr': ptr over rows, idx = columns; 'csc': ptr over columns,
+    idx = rows (Finch's Dense(SparseList(Element)))."""
+
+    nrows: int
+    ncols: int
+    ptr: torch.Tensor
+    idx: torch.Tensor
+    val: torch.Tensor | None
+    orient: str = "csr"
+    base: int = 0
+    _desc: L.FgbSparse | None = field(default=None, repr=False)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.idx.numel())
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        return (self.nrows, self.ncols)
+
+    @property
+    def dtype(self):
+        return None if self.val is None else self.val.dtype
+
+    def desc(self) -> L.FgbSparse:
+        if self._desc is None:
+            self._desc = L.FgbSparse(
+                self.nrows, self.ncols, self.nnz, L.CSR if self.orient == "csr" else L.CSC,
+                self.base, dtype_code(self.ptr), dtype_code(self.idx), dtype_code(self.val),
+                0, _dptr(self.ptr), _dptr(self.idx), _dptr(self.val))
+        return self._desc
+
+    def nbytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in (self.ptr, self.idx, self.val)
+                   if t is not None)
+
+    @classmethod
+    def from_host(cls, nrows: int, ncols: int, ptr, idx, val, orient: str = "csc", base: int = 1,
+                  device: int | None = None, val_dtype: torch.dtype | None = None,
+                  pinned: bool = False) -> "DeviceSparse":
+        """Uploads Finch level buffers (ptr/idx Int64 with `base`) to HBM."""
+        ctx = context(device)
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        ptr = np.ascontiguousarray(ptr, dtype=np.int64)
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        nnz = idx.size
+        s = stream_ptr()
+        d_idx = torch.empty(nnz, dtype=torch.int32, device=dev)
+        if nnz:
+            tmp = torch.from_numpy(idx).to(dev, non_blocking=pinned)
+            L.call("fgb_narrow_index", ctx, tmp.data_ptr(), d_idx.data_ptr(), nnz, 0, s)
+        if nnz + base < 2**31 - 1:
+            d_ptr = torch.empty(ptr.size, dtype=torch.int32, device=dev)
+            tmp = torch.from_numpy(ptr).to(dev)
+            L.call("fgb_narrow_index", ctx, tmp.data_ptr(), d_ptr.data_ptr(), ptr.size, 0, s)
+        else:
+            d_ptr = torch.from_numpy(ptr).to(dev)
+        d_val = None
+        if val is not None:
+            v = torch.as_tensor(np.ascontiguousarray(val))
+            if v.dtype == torch.bool:
+                v = v.to(torch.uint8)
+            if val_dtype is not None:
+                v = v.to(val_dtype)
+            d_val = v.to(dev)
+        return cls(nrows, ncols, d_ptr, d_idx, d_val, orient, base)
+
+    def transposed_storage(self) -> "DeviceSparse":
+        """Same logical matrix, the other orientation (stable device transpose)."""
+        ctx = context(self.ptr.device.index)
+        nout = self.nrows if self.orient == "csc" else self.ncols
+        dev = self.ptr.device
+        out_ptr = torch.empty(nout + 1, dtype=torch.int64, device=dev)
+        out_idx = torch.empty(self.nnz, dtype=torch.int32, device=dev)
+        out_val = None if self.val is None else torch.empty_like(self.val)
+        d = self.desc()
+        L.call("fgb_transpose", ctx, ctypes.byref(d), out_ptr.data_ptr(), _dptr(out_idx),
+               _dptr(out_val), stream_ptr())
+        if self.nnz < 2**31 - 1:
+            p32 = torch.empty(nout + 1, dtype=torch.int32, device=dev)
+            L.call("fgb_narrow_index", ctx, out_ptr.data_ptr(), p32.data_ptr(), nout + 1, 0,
+                   stream_ptr())
+            out_ptr = p32
+        return DeviceSparse(self.nrows, self.ncols, out_ptr, out_idx, out_val,
+                            "csr" if self.orient == "csc" else "csc", 0)
+
+    def T(self) -> "DeviceSparse":
+        """The transpose A^T as a view: same buffers, other orientation."""
+        return DeviceSparse(self.ncols, self.nrows, self.ptr, self.idx, self.val,
+                            "csr" if self.orient == "csc" else "csc", self.base)
+
+    def to_host(self):
+        """(ptr, idx, val) as numpy in Finch's 1-based Int64 layout."""
+        torch.cuda.current_stream().synchronize()
+        ptr = self.ptr.cpu().numpy().astype(np.int64) - self.base + 1
+        idx = self.idx.cpu().numpy().astype(np.int64) - self.base + 1
+        val = None if self.val is None else self.val.cpu()
+        if val is not None and val.dtype == torch.bfloat16:
+            val = val.float()
+        return ptr, idx, (None if val is None else val.numpy())
+
+
+# ---------------------------------------------------------------- kernel calls
+
+def _ctx_for(t: torch.Tensor):
+    return context(t.device.index)
+
+
+def spmv(A: DeviceSparse, x: torch.Tensor, y: torch.Tensor | None = None,
+         semiring: int = L.PLUS_TIMES, flags: int = 0) -> torch.Tensor:
+    """y <<add>>= A (*) x over `semiring` (y is created and initialised if None)."""
+    if y is None:
+        y = torch.empty(A.nrows, dtype=x.dtype, device=x.device)
+        flags &= ~L.ACCUMULATE
+    d = A.desc()
+    L.call("fgb_spmv", _ctx_for(x), semiring, ctypes.byref(d), _dptr(x), dtype_code(x), _dptr(y),
+           dtype_code(y), flags, stream_ptr())
+    return y
+
+
+def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
+    """C (+)= A @ B for row-major B (n x nk)."""
+    nk = B.shape[1]
+    if C is None:
+        C = torch.empty((A.nrows, nk), dtype=B.dtype, device=B.device)
+        flags &= ~L.ACCUMULATE
+    d = A.desc()
+    L.call("fgb_spmm", _ctx_for(B), ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
+           C.stride(0), dtype_code(B), flags, stream_ptr())
+    return C
+
+
+def sddmm(A: DeviceSparse, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
+          flags: int = 0) -> torch.Tensor:
+    """out[e] = A.val[e] * <X[i,:], Y[j,:]> over A's stored entries."""
+    if out is None:
+        out = torch.empty(A.nnz, dtype=X.dtype, device=X.device)
+    d = A.desc()
+    L.call("fgb_sddmm", _ctx_for(X), ctypes.byref(d), _dptr(X), X.stride(0), _dptr(Y), Y.stride(0),
+           X.shape[1], _dptr(out), dtype_code(X), flags, stream_ptr())
+    return out
+
+
+def ewise(op: int, A: DeviceSparse, B: DeviceSparse) -> DeviceSparse:
+    """C = A .* B (op EW_MUL) or A .+ B (EW_ADD) of two same-shape matrices."""
+    ctx = _ctx_for(A.idx)
+    nf = A.nrows if A.orient == "csr" else A.ncols
+    out_ptr = torch.empty(nf + 1, dtype=torch.int64, device=A.idx.device)
+    nnz = ctypes.c_int64()
+    da, db = A.desc(), B.desc()
+    L.call("fgb_ewise_count", ctx, op, ctypes.byref(da), ctypes.byref(db), out_ptr.data_ptr(),
+           ctypes.byref(nnz), stream_ptr())
+    out_idx = torch.empty(nnz.value, dtype=torch.int32, device=A.idx.device)
+    out_val = torch.empty(nnz.value, dtype=A.val.dtype, device=A.idx.device)
+    L.call("fgb_ewise_fill", ctx, op, ctypes.byref(da), ctypes.byref(db), out_ptr.data_ptr(),
+           _dptr(out_idx), _dptr(out_val), stream_ptr())
+    return DeviceSparse(A.nrows, A.ncols, out_ptr, out_idx, out_val, A.orient, 0)
+
+
+def ewise_reduce(dims: int, A: DeviceSparse, B: DeviceSparse | None = None,
+                 B_dense: torch.Tensor | None = None, y: torch.Tensor | None = None) -> torch.Tensor:
+    """sum(A .* B; dims) (dims 0 = all, 1 = over rows, 2 = over columns)."""
+    length = 1 if dims == 0 else (A.nrows if dims == 2 else A.ncols)
+    if y is None:
+        y = torch.empty(length, dtype=A.val.dtype, device=A.idx.device)
+    da = A.desc()
+    db = None if B is None else ctypes.byref(B.desc())
+    L.call("fgb_ewise_reduce", _ctx_for(A.idx), dims, ctypes.byref(da), db, _dptr(B_dense),
+           0 if B_dense is None else B_dense.stride(0), _dptr(y), dtype_code(A.val), 0,
+           stream_ptr())
+    return y

@@ -1,0 +1,226 @@
+/*
+ * finchgb.h -- C ABI of the GB300 (sm_103a) execution backend for the sparse
+ * loop nests Finch.jl lowers to SpMV, SpMM, SDDMM, semiring SpMV and fused
+ * elementwise+reduce.
+ *
+ * Every entry point is plain C: opaque handles, raw pointers and sizes, an int
+ * status return.  Nothing aborts; the message for the last failure on the
+ * calling thread is returned by fgb_last_error().
+ *
+ * Level buffers follow Finch's SparseList layout
+ * (src/tensors/levels/sparse_list_levels.jl:37-53): for each parent position p
+ * the stored coordinates are idx[ptr[p]-base .. ptr[p+1]-base) and the values
+ * sit at the same positions of the child Element level
+ * (src/tensors/levels/element_levels.jl:20-34).  Finch's own buffers are
+ * 1-based Int64 (index_base = 1, ptr[1] == 1); 0-based PlusOneVector buffers
+ * (src/util/vectors.jl:3-37) are index_base = 0.  Compute kernels read 32-bit
+ * idx; fgb_narrow_index() converts Finch's Int64 idx once, at upload.
+ *
+ * Orientation: FGB_CSC is Finch's Dense(SparseList(Element)) of an m x n
+ * matrix A[i,j] (outer level j, ptr has n+1 entries, idx holds rows i).
+ * FGB_CSR is swizzle(Tensor(CSC of A^T), 2, 1)
+ * (src/tensors/combinators/swizzle.jl:55-58): ptr has m+1 entries and idx
+ * holds columns j.
+ *
+ * Dense operands are row-major with a leading dimension (the last index is
+ * fastest), which is how Finch stores swizzle(Tensor(Dense(Dense(Element))) of
+ * B^T, 2, 1).
+ *
+ * Pointers passed to compute entry points are DEVICE pointers (from
+ * fgb_malloc, cudaMalloc or another allocator on the same device).  All work
+ * is issued on `stream` (a cudaStream_t; NULL = the context's own stream) and
+ * is asynchronous unless stated otherwise.
+ */
+#ifndef FINCHGB_H
+#define FINCHGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FGB_API __attribute__((visibility("default")))
+#else
+#define FGB_API
+#endif
+
+#define FGB_VERSION_MAJOR 0
+#define FGB_VERSION_MINOR 1
+
+/* Status codes.  The Finch side maps EINVAL to DimensionMismatch /
+ * FinchProtocolError, like the checks in Finch's generated code
+ * (test/reference64/typical/typical_spmv_csc.txt:42). */
+typedef enum {
+  FGB_OK = 0,
+  FGB_EINVAL = 1,       /* bad shape, format, dtype or argument */
+  FGB_ENOMEM = 2,       /* allocation failed or admission refused */
+  FGB_ETIMEOUT = 3,     /* a bounded wait ran out */
+  FGB_ECUDA = 4,        /* a CUDA runtime call failed */
+  FGB_EUNSUPPORTED = 5, /* no kernel for this (semiring, dtype, format) */
+  FGB_EBUSY = 6,        /* resource in use / queue full */
+  FGB_ECANCELLED = 7    /* request cancelled before it ran */
+} fgb_status;
+
+typedef enum {
+  FGB_NONE = -1, /* no values: Pattern level (every stored entry is true) */
+  FGB_F64 = 0,
+  FGB_F32 = 1,
+  FGB_BF16 = 2,
+  FGB_I32 = 3,
+  FGB_I64 = 4,
+  FGB_BOOL = 5 /* one byte, 0 or 1 */
+} fgb_dtype;
+
+/* Semirings of y[i] <<add>>= mul(A[i,j], x[j]).  Identities follow Finch's
+ * algebra traits (src/symbolic/symbolic.jl:95-104); arithmetic follows Julia
+ * Base: integers wrap; float min/max are the @fastmath forms Finch runs under
+ * (src/execute.jl:116-120): the new operand wins only when strictly smaller
+ * (larger). */
+typedef enum {
+  FGB_PLUS_TIMES = 0, /* y[i] += A[i,j] * x[j]            */
+  FGB_MIN_PLUS = 1,   /* y[i] <<min>>= A[i,j] + x[j]      */
+  FGB_MAX_PLUS = 2,   /* y[i] <<max>>= A[i,j] + x[j]      */
+  FGB_OR_AND = 3      /* y[i] |= A[i,j] & x[j]  (Bool)    */
+} fgb_semiring;
+
+typedef enum { FGB_CSR = 0, FGB_CSC = 1 } fgb_orient;
+
+/* Flags for compute calls. */
+#define FGB_ACCUMULATE 0x1u /* y/C keep their contents (no `y .= init`)      */
+#define FGB_FINCH_ORDER 0x2u /* float sums in Finch's serial order:          \
+                                one running sum per output, j ascending       */
+#define FGB_FMA 0x4u         /* with FINCH_ORDER: fused a*b+c                */
+#define FGB_NO_FMA 0x8u      /* with FINCH_ORDER: rounded product, then add  */
+
+/* A sparse matrix as Finch level buffers (a plain struct; all pointers are
+ * device pointers for compute calls). */
+typedef struct fgb_sparse {
+  int64_t nrows;      /* logical m */
+  int64_t ncols;      /* logical n */
+  int64_t nnz;        /* stored entries */
+  int32_t orient;     /* fgb_orient */
+  int32_t index_base; /* 0 or 1 (Finch: 1) */
+  int32_t ptr_t;      /* FGB_I32 or FGB_I64 */
+  int32_t idx_t;      /* FGB_I32 (compute) or FGB_I64 (input to narrowing) */
+  int32_t val_t;      /* fgb_dtype, FGB_NONE for a Pattern level */
+  int32_t reserved;
+  const void* ptr; /* compressed-dimension + 1 entries */
+  const void* idx; /* nnz entries */
+  const void* val; /* nnz entries, or NULL for Pattern */
+} fgb_sparse;
+
+typedef struct fgb_ctx fgb_ctx;
+
+/* ---- context, errors, memory ------------------------------------------ */
+
+/* Version as MAJOR*1000 + MINOR. */
+FGB_API int fgb_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+FGB_API const char* fgb_last_error(void);
+
+/* Create a context on `device`: records SM count, creates a stream.
+ * Replaces the CPU device of src/architecture.jl (AbstractDevice/CPU,
+ * architecture.jl:1-60) as the place Finch runs the matched nests. */
+FGB_API int fgb_ctx_create(int device, fgb_ctx** out);
+FGB_API int fgb_ctx_destroy(fgb_ctx* ctx);
+/* The context's stream (a cudaStream_t). */
+FGB_API void* fgb_ctx_stream(fgb_ctx* ctx);
+FGB_API int fgb_ctx_num_sms(fgb_ctx* ctx);
+
+/* Device buffers: the storage behind device-resident level buffers (what
+ * Finch's transfer(device, lvl) recursion, sparse_list_levels.jl:64-69,
+ * element_levels.jl:46-48, would place in HBM). */
+FGB_API int fgb_malloc(fgb_ctx* ctx, size_t bytes, void** out);
+FGB_API int fgb_free(fgb_ctx* ctx, void* p);
+/* Pinned host buffers for copies that overlap compute. */
+FGB_API int fgb_host_alloc(fgb_ctx* ctx, size_t bytes, void** out);
+FGB_API int fgb_host_free(fgb_ctx* ctx, void* p);
+/* Stream-ordered copies (one cudaMemcpyAsync each). */
+FGB_API int fgb_upload(fgb_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes, void* stream);
+FGB_API int fgb_download(fgb_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes, void* stream);
+FGB_API int fgb_stream_sync(fgb_ctx* ctx, void* stream);
+
+/* ---- level-buffer conversion ------------------------------------------ */
+
+/* dst[i] = (int32)(src[i] - delta) for i < n; fails with EINVAL (after the
+ * stream finishes) if any value does not fit in int32.  Narrows Finch's Int64
+ * ptr/idx buffers (sparse_list_levels.jl:44-49) to the 32-bit form the
+ * kernels read.  Synchronous. */
+FGB_API int fgb_narrow_index(fgb_ctx* ctx, const int64_t* src, int32_t* dst, int64_t n, int64_t delta,
+                     void* stream);
+
+/* Stable transpose of the compressed orientation: CSC <-> CSR of the same
+ * logical matrix, with coordinates ascending inside every fiber.  `out`
+ * receives ptr (int64, nout+1) / idx (int32, nnz) / val (nnz, same dtype)
+ * in caller-allocated device buffers, 0-based.  Replaces Finch's
+ * CSC -> CSR copy through dropfills!/copyto! (src/interface/copy.jl:77-113).
+ * Synchronous. */
+FGB_API int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr, int32_t* out_idx,
+                  void* out_val, void* stream);
+
+/* ---- compute ------------------------------------------------------------ */
+
+/* Semiring SpMV: y[i] <<add>>= mul(A[i,j], x[j]) for A m x n.
+ * Replaces the nest `y .= init; for j=_, i=_; y[i] <<op>>= A[i,j] (*) x[j]`
+ * (test/reference64/typical/typical_spmv_csc.txt:18-81) and its CSR form.
+ * val_t/x_t/y_t combinations:
+ *   PLUS_TIMES, MIN_PLUS, MAX_PLUS: F64/F64/F64, F32/F32/F32, BF16/F32/F32
+ *                                   (PLUS_TIMES only), I32/I32/I32, I64/I64/I64
+ *   OR_AND: BOOL or NONE (Pattern) / BOOL / BOOL
+ * CSR runs as a pull (one running value per row); CSC runs as a push with
+ * atomic updates of y (order-independent for exact semirings).  With
+ * FGB_FINCH_ORDER on a CSR matrix every y[i] is one sequential sum over j
+ * ascending, which equals Finch's serial CSC nest bit for bit. */
+FGB_API int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* x, int x_t, void* y,
+             int y_t, unsigned flags, void* stream);
+
+/* SpMM: C[i,k] += A[i,j] * B[j,k], k < nk.  B row-major (ldb), C row-major
+ * (ldc).  F32 (A F32 or BF16 values, B/C F32) or F64.  Replaces
+ * `@einsum C[i,k] += A[i,j]*B[j,k]` = tensordot(A,B,(2,1))
+ * (src/interface/lazy.jl:215-257,387-404). */
+FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
+             int64_t ldc, int dtype, unsigned flags, void* stream);
+
+/* SDDMM: out[e] = A.val[e] * sum_k X[i,k] * Y[j,k] for every stored (i,j)
+ * of A (out shares A's pattern).  X is m x k, Y is n x k, both row-major.
+ * F32 or F64.  Replaces compute(lazy(A) .* (lazy(X) * lazy(Y^T)))
+ * (src/interface/lazy.jl:323-331, benchmark/benchmarks.jl:141-168). */
+FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
+              int64_t ldy, int64_t k, void* out_val, int dtype, unsigned flags, void* stream);
+
+/* Elementwise ops of two same-shape CSR/CSC matrices (same orientation). */
+typedef enum {
+  FGB_EW_MUL = 0, /* C = A .* B   (stored where both are stored) */
+  FGB_EW_ADD = 1  /* C = A .+ B   (stored where either is stored) */
+} fgb_ewise_op;
+
+/* Pass 1 of a sparse elementwise op: out_ptr (int64, nfibers+1, 0-based)
+ * gets the output pattern's fiber offsets and *out_nnz the total.
+ * Synchronous (the caller sizes idx/val from *out_nnz).  Follows Finch's
+ * two-finger merge of two SparseList fibers
+ * (test/reference64/typical/typical_merge_twofinger.txt). */
+FGB_API int fgb_ewise_count(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_sparse* B,
+                    int64_t* out_ptr, int64_t* out_nnz, void* stream);
+/* Pass 2: fill idx (int32, 0-based) and val of the output. */
+FGB_API int fgb_ewise_fill(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_sparse* B,
+                   const int64_t* out_ptr, int32_t* out_idx, void* out_val, void* stream);
+
+/* Fused elementwise multiply + reduction:
+ *   dims = 2:  y[i] = sum_j A[i,j] * B[i,j]      (length m)
+ *   dims = 1:  y[j] = sum_i A[i,j] * B[i,j]      (length n)
+ *   dims = 0:  y[0] = sum_ij A[i,j] * B[i,j]     (all dims)
+ * B is a sparse matrix of the same shape/orientation (B_dense == NULL) or a
+ * dense row-major m x n matrix (B == NULL, ld = ldb).  F32 or F64.
+ * Replaces compute(sum(lazy(A) .* lazy(B); dims)) (src/interface/lazy.jl). */
+FGB_API int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_sparse* B,
+                     const void* B_dense, int64_t ldb, void* y, int dtype, unsigned flags,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FINCHGB_H */

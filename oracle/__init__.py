@@ -1,0 +1,173 @@
+"""TEST INFRASTRUCTURE ONLY -- the oracle.
+
+ctypes wrapper around finch_oracle.c, a CPU restatement of the loop nests
+Finch.jl v1.2.12 generates for SpMV (CSC serial and CSR row-parallel), SpMM,
+SDDMM, two-finger elementwise merges and elementwise+reduce.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may use it, and only
+as the checker.  The GPU library never calls it.
+
+Sparse operands are passed in Finch's own layout: 1-based Int64 ptr/idx of a
+SparseList level and the Element values (numpy arrays).  bf16 values are
+passed as their uint16 bit patterns with ``vt=T_BF16``.
+
+Parity of this restatement is pinned by tests/test_oracle_golden.py against
+the numeric results printed in Finch's test fixtures.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "finch_oracle.c"
+BUILD_DIR = HERE / "_build"
+LIB_PATH = BUILD_DIR / "liboracle.so"
+
+SR_PT, SR_MINP, SR_MAXP, SR_OA = 0, 1, 2, 3
+T_NONE, T_F64, T_F32, T_BF16, T_I32, T_I64, T_BOOL = -1, 0, 1, 2, 3, 4, 5
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compiles finch_oracle.c with gcc (OpenMP, no FP contraction)."""
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < SRC.stat().st_mtime:
+        tmp = LIB_PATH.with_suffix(".so.tmp")
+        cmd = [os.environ.get("CC", "gcc"), "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC",
+               "-shared", "-std=c11", str(SRC), "-o", str(tmp), "-lm"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(str(LIB_PATH))
+            i64, i32, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p
+            L.orc_spmv_csc.argtypes = [i32, i32, i32, i64, i64, vp, vp, vp, vp, vp, i32, i32]
+            L.orc_spmv_csr.argtypes = [i32, i32, i32, i64, i64, vp, vp, vp, vp, vp, i32, i32, i32]
+            L.orc_spmm_csr.argtypes = [i32, i32, i64, i64, i64, vp, vp, vp, vp, i64, vp, i64, i32,
+                                       i32, i32]
+            L.orc_sddmm_csr.argtypes = [i32, i64, i64, vp, vp, vp, vp, i64, vp, i64, vp, i32, i32,
+                                        i32]
+            L.orc_ewise.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+            L.orc_ewise_reduce.argtypes = [i32, i32, i64, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp]
+            L.orc_max_threads.argtypes = []
+            _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def dtype_code(a: np.ndarray | None, bf16: bool = False) -> int:
+    if a is None:
+        return T_NONE
+    if bf16:
+        return T_BF16
+    return {np.dtype(np.float64): T_F64, np.dtype(np.float32): T_F32, np.dtype(np.int32): T_I32,
+            np.dtype(np.int64): T_I64, np.dtype(np.bool_): T_BOOL,
+            np.dtype(np.uint8): T_BOOL}[a.dtype]
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def spmv_csc(sr, m, n, ptr, idx, val, x, y=None, init=True, fma=True, bf16=False):
+    """Finch's serial CSC nest y[i] <<(+)>>= A[i,j] (*) x[j] (1-based buffers)."""
+    x = np.ascontiguousarray(x)
+    at = dtype_code(x)
+    if y is None:
+        y = np.zeros(m, dtype=x.dtype)
+    val = None if val is None else np.ascontiguousarray(val)
+    lib().orc_spmv_csc(sr, dtype_code(val, bf16), at, m, n, _p(_i64(ptr)), _p(_i64(idx)), _p(val),
+                       _p(x), _p(y), int(init), int(fma))
+    return y
+
+
+def spmv_csr(sr, m, n, ptr, idx, val, x, y=None, init=True, fma=True, bf16=False, nthreads=1):
+    """Finch's row-pull nest (static thread split) over a CSR matrix."""
+    x = np.ascontiguousarray(x)
+    at = dtype_code(x)
+    if y is None:
+        y = np.zeros(m, dtype=x.dtype)
+    val = None if val is None else np.ascontiguousarray(val)
+    lib().orc_spmv_csr(sr, dtype_code(val, bf16), at, m, n, _p(_i64(ptr)), _p(_i64(idx)), _p(val),
+                       _p(x), _p(y), int(init), int(fma), int(nthreads))
+    return y
+
+
+def spmm_csr(m, n, ptr, idx, val, B, C=None, init=True, fma=True, bf16=False, nthreads=1):
+    """C[i,k] += A[i,j] * B[j,k] for CSR A and row-major B."""
+    B = np.ascontiguousarray(B)
+    nk = B.shape[1]
+    if C is None:
+        C = np.zeros((m, nk), dtype=B.dtype)
+    at = dtype_code(B)
+    val = np.ascontiguousarray(val)
+    lib().orc_spmm_csr(dtype_code(val, bf16), at, m, n, nk, _p(_i64(ptr)), _p(_i64(idx)), _p(val),
+                       _p(B), B.shape[1], _p(C), C.shape[1], int(init), int(fma), int(nthreads))
+    return C
+
+
+def sddmm_csr(m, ptr, idx, val, X, Y, fma=True, acc64=False, nthreads=1):
+    """out[q] = A(q) * sum_k X[i,k] Y[j,k] over the stored entries of CSR A."""
+    X = np.ascontiguousarray(X)
+    Y = np.ascontiguousarray(Y)
+    val = np.ascontiguousarray(val)
+    at = dtype_code(X)
+    out = np.zeros(len(val), dtype=np.float64 if (acc64 or at == T_F64) else X.dtype)
+    lib().orc_sddmm_csr(at, m, X.shape[1], _p(_i64(ptr)), _p(_i64(idx)), _p(val), _p(X),
+                        X.shape[1], _p(Y), Y.shape[1], _p(out), int(fma), int(acc64),
+                        int(nthreads))
+    return out
+
+
+def ewise(op, nf, pa, ia, va, pb, ib, vb):
+    """Two-finger merge of two same-shape SparseList matrices (op 0 = *, 1 = +).
+
+    Returns (ptr, idx, val) in Finch's 1-based layout."""
+    va = np.ascontiguousarray(va)
+    vb = np.ascontiguousarray(vb)
+    pa, ia, pb, ib = _i64(pa), _i64(ia), _i64(pb), _i64(ib)
+    out_ptr = np.zeros(nf + 1, dtype=np.int64)
+    L = lib()
+    L.orc_ewise(op, dtype_code(va), nf, _p(pa), _p(ia), _p(va), _p(pb), _p(ib), _p(vb),
+                _p(out_ptr), None, None)
+    nnz = int(out_ptr[-1] - 1)
+    out_idx = np.zeros(nnz, dtype=np.int64)
+    out_val = np.zeros(nnz, dtype=va.dtype)
+    L.orc_ewise(op, dtype_code(va), nf, _p(pa), _p(ia), _p(va), _p(pb), _p(ib), _p(vb),
+                _p(out_ptr), _p(out_idx), _p(out_val))
+    return out_ptr, out_idx, out_val
+
+
+def ewise_reduce(dims, m, n, pa, ia, va, pb=None, ib=None, vb=None, Bd=None):
+    """sum(A .* B; dims) in double (B sparse CSR or dense row-major Bd)."""
+    va = np.ascontiguousarray(va)
+    length = 1 if dims == 0 else (m if dims == 2 else n)
+    y = np.zeros(length, dtype=np.float64)
+    if Bd is not None:
+        Bd = np.ascontiguousarray(Bd, dtype=va.dtype)
+    lib().orc_ewise_reduce(dims, dtype_code(va), m, n, _p(_i64(pa)), _p(_i64(ia)), _p(va),
+                           None if pb is None else _p(_i64(pb)),
+                           None if ib is None else _p(_i64(ib)),
+                           None if vb is None else _p(np.ascontiguousarray(vb)),
+                           _p(Bd), 0 if Bd is None else Bd.shape[1], _p(y))
+    return y

@@ -1,0 +1,185 @@
+"""GPU parity of SpMM, SDDMM, elementwise merges and elementwise+reduce
+(through the C ABI) against the oracle."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from finchgb import _lib as L
+from finchgb import device as dev
+from finchgb.workloads import SparseBuffers, csr_from_dense, fsprand, zipf_csr
+from helpers import assert_close, bf16_bits, to_dev, to_host, upload
+
+pytestmark = pytest.mark.gpu
+KATS = json.loads((Path(__file__).parent / "golden" / "finch_kats.json").read_text())["kats"]
+
+
+def csr_rand(rng, m, n, p, dtype):
+    D = np.where(rng.random((m, n)) < p, rng.standard_normal((m, n)), 0.0)
+    r = csr_from_dense(D)
+    r.val = r.val.astype(dtype)
+    return r
+
+
+def spmm_scale(r: SparseBuffers, B):
+    return oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, np.abs(r.val).astype(np.float64),
+                           np.abs(B).astype(np.float64))
+
+
+def test_kat_einsum_matmul(gpu_lib):
+    k = KATS["einsum_matmul"]
+    r = csr_from_dense(np.array(k["A"]))
+    A = upload(r)
+    C = to_host(dev.spmm(A, to_dev(np.array(k["B"]))))
+    assert C.tolist() == k["C"]
+
+
+@pytest.mark.parametrize("dtype,bf16", [(np.float32, False), (np.float64, False), (np.float32, True)])
+@pytest.mark.parametrize("nk", [128, 32, 64, 20, 3, 200])
+def test_spmm_csr_bit_exact(gpu_lib, dtype, bf16, nk):
+    """Every C[i,k] is one running sum over j ascending, like Finch's nest:
+    the result equals the oracle's fused nest bit for bit."""
+    rng = np.random.default_rng(nk)
+    r = csr_rand(rng, 257, 300, 0.05, dtype)
+    B = rng.standard_normal((300, nk)).astype(dtype)
+    A = upload(r, as_bf16=bf16)
+    C = to_host(dev.spmm(A, to_dev(B)))
+    val = bf16_bits(r.val) if bf16 else r.val
+    want = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, val, B, bf16=bf16)
+    assert np.array_equal(C, want)
+    C2 = to_host(dev.spmm(A, to_dev(B), flags=L.FINCH_ORDER | L.NO_FMA))
+    want2 = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, val, B, fma=False, bf16=bf16)
+    assert np.array_equal(C2, want2)
+
+
+def test_spmm_accumulate_and_strides(gpu_lib):
+    rng = np.random.default_rng(1)
+    r = csr_rand(rng, 100, 80, 0.1, np.float32)
+    Bfull = rng.standard_normal((80, 160)).astype(np.float32)
+    A = upload(r)
+    Bd = to_dev(Bfull)[:, :128]  # ldb = 160
+    C0 = rng.standard_normal((100, 136)).astype(np.float32)
+    Cd = to_dev(C0)
+    dev.spmm(A, Bd, Cd[:, :128], flags=L.ACCUMULATE)
+    want = oracle.spmm_csr(100, 80, r.ptr, r.idx, r.val, np.ascontiguousarray(Bfull[:, :128]),
+                           C=np.ascontiguousarray(C0[:, :128]), init=False)
+    got = to_host(Cd)
+    assert np.array_equal(got[:, :128], want)
+    assert np.array_equal(got[:, 128:], C0[:, 128:])  # untouched beyond nk
+
+
+def test_spmm_csc_push(gpu_lib):
+    rng = np.random.default_rng(2)
+    D = np.where(rng.random((120, 90)) < 0.08, rng.standard_normal((120, 90)), 0.0)
+    from finchgb.workloads import csc_from_dense
+
+    b = csc_from_dense(D)
+    b.val = b.val.astype(np.float32)
+    B = rng.standard_normal((90, 48)).astype(np.float32)
+    C = to_host(dev.spmm(upload(b), to_dev(B)))
+    r = csr_from_dense(D)
+    r.val = r.val.astype(np.float32)
+    want = oracle.spmm_csr(120, 90, r.ptr, r.idx, r.val, B)
+    assert_close(C, want, spmm_scale(r, B), np.float32)
+
+
+def test_spmm_zipf_rows(gpu_lib):
+    rng = np.random.default_rng(4)
+    r = zipf_csr(rng, 20000, 20000, mean=16, cap=50_000)
+    B = rng.standard_normal((20000, 128)).astype(np.float32)
+    C = to_host(dev.spmm(upload(r), to_dev(B)))
+    want = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, r.val, B, nthreads=oracle.max_threads())
+    assert np.array_equal(C, want)
+
+
+@pytest.mark.parametrize("k", [64, 16, 7, 100])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sddmm(gpu_lib, k, dtype):
+    rng = np.random.default_rng(k)
+    r = zipf_csr(rng, 3000, 2500, mean=12, cap=2000, dtype=dtype)
+    X = rng.standard_normal((3000, k)).astype(dtype)
+    Y = rng.standard_normal((2500, k)).astype(dtype)
+    A = upload(r)
+    out = to_host(dev.sddmm(A, to_dev(X), to_dev(Y)))
+    want = oracle.sddmm_csr(r.nrows, r.ptr, r.idx, r.val, X, Y, acc64=True)
+    scale = np.abs(r.val.astype(np.float64)) * oracle.sddmm_csr(
+        r.nrows, r.ptr, r.idx, np.ones(r.nnz), np.abs(X).astype(np.float64),
+        np.abs(Y).astype(np.float64))
+    assert_close(out, want, scale, dtype)
+    # Finch order: sequential dot, then the product with A -- bit-exact
+    out2 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), flags=L.FINCH_ORDER))
+    assert np.array_equal(out2, oracle.sddmm_csr(r.nrows, r.ptr, r.idx, r.val, X, Y))
+
+
+def test_sddmm_csc_swaps_roles(gpu_lib):
+    rng = np.random.default_rng(9)
+    D = np.where(rng.random((60, 50)) < 0.1, rng.standard_normal((60, 50)), 0.0)
+    from finchgb.workloads import csc_from_dense
+
+    b = csc_from_dense(D)
+    X = rng.standard_normal((60, 32))
+    Y = rng.standard_normal((50, 32))
+    out = to_host(dev.sddmm(upload(b), to_dev(X), to_dev(Y)))
+    f = np.repeat(np.arange(50), np.diff(b.ptr))
+    want = b.val * np.einsum("ek,ek->e", X[b.idx - 1], Y[f])
+    np.testing.assert_allclose(out, want, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64])
+@pytest.mark.parametrize("op", [L.EW_MUL, L.EW_ADD])
+def test_ewise_merge(gpu_lib, dtype, op):
+    rng = np.random.default_rng(op * 10 + np.dtype(dtype).itemsize)
+    m, n = 400, 350
+    ra = csr_rand(rng, m, n, 0.05, np.float64)
+    rb = csr_rand(rng, m, n, 0.05, np.float64)
+    ra.val = (ra.val * 100).astype(dtype)
+    rb.val = (rb.val * 100).astype(dtype)
+    C = dev.ewise(op, upload(ra), upload(rb))
+    ptr, idx, val = C.to_host()
+    wp, wi, wv = oracle.ewise(op, m, ra.ptr, ra.idx, ra.val, rb.ptr, rb.idx, rb.val)
+    assert np.array_equal(ptr, wp) and np.array_equal(idx, wi) and np.array_equal(val, wv)
+
+
+def test_ewise_kat_twofinger(gpu_lib):
+    k = KATS["merge_twofinger_add"]
+    x, y, z = k["x"], k["y"], k["z"]
+    def vec(d):  # a SparseList vector as a 1 x n CSR matrix
+        return SparseBuffers(1, d["n"], np.array(d["ptr"], np.int64), np.array(d["idx"], np.int64),
+                             np.array(d["val"]), "csr")
+    C = dev.ewise(L.EW_ADD, upload(vec(x)), upload(vec(y)))
+    ptr, idx, val = C.to_host()
+    assert ptr.tolist() == z["ptr"] and idx.tolist() == z["idx"] and val.tolist() == z["val"]
+
+
+@pytest.mark.parametrize("dims", [0, 1, 2])
+@pytest.mark.parametrize("sparse_b", [True, False])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_ewise_reduce(gpu_lib, dims, sparse_b, dtype):
+    rng = np.random.default_rng(dims + 3 * sparse_b)
+    m, n = 500, 300
+    ra = csr_rand(rng, m, n, 0.06, dtype)
+    A = upload(ra)
+    if sparse_b:
+        rb = csr_rand(rng, m, n, 0.3, dtype)
+        y = to_host(dev.ewise_reduce(dims, A, B=upload(rb)))
+        want = oracle.ewise_reduce(dims, m, n, ra.ptr, ra.idx, ra.val, rb.ptr, rb.idx, rb.val)
+        scale = oracle.ewise_reduce(dims, m, n, ra.ptr, ra.idx, np.abs(ra.val), rb.ptr, rb.idx,
+                                    np.abs(rb.val))
+    else:
+        Bd = rng.standard_normal((m, n)).astype(dtype)
+        y = to_host(dev.ewise_reduce(dims, A, B_dense=to_dev(Bd)))
+        want = oracle.ewise_reduce(dims, m, n, ra.ptr, ra.idx, ra.val, Bd=Bd)
+        scale = oracle.ewise_reduce(dims, m, n, ra.ptr, ra.idx, np.abs(ra.val), Bd=np.abs(Bd))
+    assert_close(y, want, scale, dtype)
+
+
+def test_kat_reduce(gpu_lib):
+    k = KATS["reduce"]
+    A = upload(csr_from_dense(np.array(k["A"])))
+    ones = to_dev(np.ones((4, 3)))
+    np.testing.assert_allclose(to_host(dev.ewise_reduce(1, A, B_dense=ones)), k["dims1"], rtol=1e-15)
+    np.testing.assert_allclose(to_host(dev.ewise_reduce(2, A, B_dense=ones)), k["dims2"], rtol=1e-15)
+    np.testing.assert_allclose(to_host(dev.ewise_reduce(0, A, B_dense=ones)), [k["all"]], rtol=1e-15)

@@ -1,0 +1,205 @@
+"""GPU parity of semiring SpMV (fgb_spmv through the C ABI) against the
+oracle: bit-exact for integer, Bool and min/max semirings and for float sums
+in Finch's serial order; within RTOL * sum|terms| otherwise."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from finchgb import _lib as L
+from finchgb import device as dev
+from finchgb.workloads import SparseBuffers, csc_from_dense, fsprand, random_graph
+from helpers import abs_terms, assert_close, oracle_spmv, to_dev, to_host, upload
+
+pytestmark = pytest.mark.gpu
+KATS = json.loads((Path(__file__).parent / "golden" / "finch_kats.json").read_text())["kats"]
+
+
+def csr_of(b: SparseBuffers) -> SparseBuffers:
+    """The same logical matrix stored by rows (host-side, for oracle inputs)."""
+    from finchgb.workloads import csr_from_dense
+
+    if b.val is None:
+        D = b.todense() != 0
+        r = csr_from_dense(D.astype(np.float64))
+        return SparseBuffers(r.nrows, r.ncols, r.ptr, r.idx, None, "csr")
+    D = b.todense()
+    r = csr_from_dense(D)
+    r.val = r.val.astype(b.val.dtype)
+    return r
+
+
+def test_kat_spmv_csc(gpu_lib):
+    k = KATS["spmv_csc"]
+    b = csc_from_dense(np.array(k["A"]))
+    A = upload(b)
+    x = to_dev(np.array(k["x"]))
+    # CSC push (atomics)
+    y = to_host(dev.spmv(A, x))
+    np.testing.assert_allclose(y, k["y"], rtol=1e-15)
+    # Finch order: transpose once on the device, then one running sum per row
+    At = A.transposed_storage()
+    for flags in (L.FINCH_ORDER, L.FINCH_ORDER | L.NO_FMA):
+        y = to_host(dev.spmv(At, x, flags=flags))
+        assert y.tolist() == k["y"]
+
+
+def test_kat_transposed_int(gpu_lib):
+    k = KATS["spmv_transposed_int"]
+    b = csc_from_dense(np.array(k["A"], dtype=np.int64))
+    A = upload(b)
+    x = to_dev(np.array(k["x"], dtype=np.int64))
+    y = to_host(dev.spmv(A.T(), x))  # A^T x: CSC buffers read as CSR of A^T
+    assert y.tolist() == [int(v) for v in k["y"]]
+
+
+FLOAT_CASES = [(np.float64, False), (np.float32, False), (np.float32, True)]
+
+
+@pytest.mark.parametrize("dtype,bf16", FLOAT_CASES)
+@pytest.mark.parametrize("orient", ["csc", "csr"])
+@pytest.mark.parametrize("shape,p", [((300, 200), 0.05), ((64, 1000), 0.3), ((1000, 1000), 0.001)])
+def test_plus_times_float(gpu_lib, dtype, bf16, orient, shape, p):
+    rng = np.random.default_rng([shape[0], shape[1], int(p * 1e6), orient == "csr"])
+    b = fsprand(rng, shape[0], shape[1], p, dtype=np.float64)
+    b.val = (b.val * 2 - 1).astype(dtype)
+    if orient == "csr":
+        b = csr_of(b)
+    x = (rng.random(shape[1]) * 2 - 1).astype(dtype)
+    A = upload(b, as_bf16=bf16)
+    y = to_host(dev.spmv(A, to_dev(x)))
+    want = oracle_spmv(0, b, x, bf16=bf16)
+    assert_close(y, want, abs_terms(b, x), dtype)
+    if orient == "csr":
+        # Finch order is bit-exact with the oracle's fused / unfused nests
+        for flags, fma in ((L.FINCH_ORDER, True), (L.FINCH_ORDER | L.NO_FMA, False)):
+            y = to_host(dev.spmv(A, to_dev(x), flags=flags))
+            assert np.array_equal(y, oracle_spmv(0, b, x, fma=fma, bf16=bf16))
+
+
+@pytest.mark.parametrize("sr", [L.PLUS_TIMES, L.MIN_PLUS, L.MAX_PLUS])
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.float64, np.float32])
+@pytest.mark.parametrize("orient", ["csc", "csr"])
+def test_exact_semirings(gpu_lib, sr, dtype, orient):
+    if sr == L.PLUS_TIMES and np.dtype(dtype).kind == "f":
+        pytest.skip("float sums are covered by the tolerance tests")
+    rng = np.random.default_rng(7 + sr)
+    b = fsprand(rng, 500, 400, 0.02, dtype=np.float64)
+    if np.dtype(dtype).kind == "i":
+        info = np.iinfo(dtype)
+        # full-range values so that + and * wrap
+        b.val = rng.integers(info.min // 2, info.max // 2, size=b.nnz, dtype=dtype)
+        x = rng.integers(info.min // 2, info.max // 2, size=400, dtype=dtype)
+    else:
+        b.val = rng.integers(-1000, 1000, size=b.nnz).astype(dtype)
+        x = rng.integers(-1000, 1000, size=400).astype(dtype)
+    if orient == "csr":
+        b = csr_of(b)
+    A = upload(b)
+    y = to_host(dev.spmv(A, to_dev(x), semiring=sr))
+    want = oracle_spmv(sr, b, x)
+    assert np.array_equal(y, want)
+
+
+@pytest.mark.parametrize("orient", ["csc", "csr"])
+@pytest.mark.parametrize("pattern", [True, False])
+def test_or_and(gpu_lib, orient, pattern):
+    rng = np.random.default_rng(11)
+    b = random_graph(rng, 3000, 6.0, pattern=True)
+    if not pattern:
+        b.val = rng.random(b.nnz) < 0.7
+    if orient == "csr":
+        b = csr_of(b)
+    x = rng.random(3000) < 0.1
+    A = upload(b)
+    y = to_host(dev.spmv(A, to_dev(x.astype(np.uint8)), semiring=L.OR_AND))
+    want = oracle_spmv(oracle.SR_OA, b, x.astype(np.uint8))
+    assert np.array_equal(y, want)
+
+
+def test_minplus_bellman_ford_rounds(gpu_lib):
+    """20 relaxation rounds y .= inf; y[i] <<min>>= A[i,j] + x[j]; x = min(x, y)."""
+    rng = np.random.default_rng(3)
+    n = 20000
+    b = random_graph(rng, n, 8.0)
+    sentinel = np.int32(2**30)
+    x = np.full(n, sentinel, dtype=np.int32)
+    x[0] = 0
+    A = upload(b)
+    xd = to_dev(x)
+    xh = x.copy()
+    for _ in range(20):
+        yd = dev.spmv(A, xd, semiring=L.MIN_PLUS)
+        xd = torch.minimum(xd, yd)
+        yh = oracle.spmv_csc(oracle.SR_MINP, n, n, b.ptr, b.idx, b.val, xh)
+        xh = np.minimum(xh, yh)
+    assert np.array_equal(to_host(xd), xh)
+    assert (xh < sentinel).sum() > n // 2  # the search actually reached most nodes
+
+
+@pytest.mark.parametrize("ptr_i64", [False, True])
+def test_edge_cases(gpu_lib, ptr_i64):
+    # empty matrix, empty fibers, a long fiber, 1x1
+    cases = []
+    cases.append(SparseBuffers(5, 4, np.ones(5, np.int64), np.zeros(0, np.int64),
+                               np.zeros(0), "csc"))
+    D = np.zeros((50, 3000))
+    D[7, :] = np.arange(3000) % 7 - 3.0  # one row with 2571 stored entries
+    D[9, 5] = 2.0
+    cases.append(csc_from_dense(D))
+    cases.append(csr_of(csc_from_dense(D)))
+    cases.append(csc_from_dense(np.array([[2.5]])))
+    for b in cases:
+        x = np.linspace(-1, 1, b.ncols)
+        A = upload(b)
+        if ptr_i64:
+            A.ptr = A.ptr.to(torch.int64)
+            A._desc = None
+        y = to_host(dev.spmv(A, to_dev(x)))
+        want = oracle_spmv(0, b, x)
+        assert_close(y, want, abs_terms(b, x), np.float64)
+
+
+@pytest.mark.parametrize("name", ["west0132", "lpi_itest6", "lp_blend", "Trec4"])
+def test_matrixmarket_fixtures(gpu_lib, name):
+    z = np.load(Path(__file__).parent / "golden" / f"mtx_{name}.npz")
+    m, n = (int(v) for v in z["shape"])
+    from finchgb.workloads import coo_to_csr
+
+    r = coo_to_csr(m, n, z["i"], z["j"], z["v"])
+    x = np.cos(np.arange(n))
+    A = upload(r)
+    y = to_host(dev.spmv(A, to_dev(x), flags=L.FINCH_ORDER))
+    assert np.array_equal(y, oracle_spmv(0, r, x))
+    At = A.transposed_storage()  # CSC of the same matrix
+    y2 = to_host(dev.spmv(At, to_dev(x)))
+    assert_close(y2, oracle_spmv(0, r, x), abs_terms(r, x), np.float64)
+
+
+def test_transpose_roundtrip(gpu_lib):
+    rng = np.random.default_rng(5)
+    b = fsprand(rng, 700, 300, 0.03)
+    A = upload(b)
+    At = A.transposed_storage()
+    ptr, idx, val = At.to_host()
+    r = csr_of(b)
+    assert np.array_equal(ptr, r.ptr) and np.array_equal(idx, r.idx)
+    assert np.array_equal(val, r.val)
+    back = At.transposed_storage()
+    p2, i2, v2 = back.to_host()
+    assert np.array_equal(p2, b.ptr) and np.array_equal(i2, b.idx) and np.array_equal(v2, b.val)
+
+
+def test_errors_are_status_codes(gpu_lib):
+    b = csc_from_dense(np.eye(3))
+    A = upload(b)
+    x = to_dev(np.ones(3, dtype=np.float32))  # dtype mismatch with f64 values
+    with pytest.raises(L.FinchGBError) as e:
+        dev.spmv(A, x)
+    assert e.value.status == L.EUNSUPPORTED
+    with pytest.raises(L.FinchGBError) as e:
+        dev.spmv(A, to_dev(np.ones(3)), flags=L.FINCH_ORDER)  # CSC + Finch order
+    assert e.value.status == L.EUNSUPPORTED
