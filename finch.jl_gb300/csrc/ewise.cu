@@ -128,7 +128,7 @@ __global__ void reduce_fiber_dense(int64_t nf, Fiber<PA> a, const T* __restrict_
     T acc = T(0);
     for (int64_t p = a.lo(f) + lane; p < a.hi(f); p += G) {
       const int64_t c = a.at(p);
-      const T d = csr ? __ldg(D + f * ld + c) : __ldg(D + c * ld + f);
+      const T d = !D ? T(1) : csr ? __ldg(D + f * ld + c) : __ldg(D + c * ld + f);
       acc = fused(va[p], d, acc);
     }
 #pragma unroll
@@ -162,7 +162,7 @@ __global__ void reduce_scatter_dense(int64_t nf, Fiber<PA> a, const T* __restric
   for (int64_t f = w; f < nf; f += nw)
     for (int64_t p = a.lo(f) + lane; p < a.hi(f); p += 32) {
       const int64_t c = a.at(p);
-      const T d = csr ? __ldg(D + f * ld + c) : __ldg(D + c * ld + f);
+      const T d = !D ? T(1) : csr ? __ldg(D + f * ld + c) : __ldg(D + c * ld + f);
       atomicAdd(y + c, wmul(va[p], d));
     }
 }
@@ -300,8 +300,7 @@ int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_spar
   if (dims < 0 || dims > 2) return set_error(FGB_EINVAL, "fgb_ewise_reduce: dims must be 0, 1 or 2");
   int rc = B ? check_pair(A, B, "fgb_ewise_reduce") : check_sparse(A, "fgb_ewise_reduce: A", true);
   if (rc) return rc;
-  if (!B && !B_dense) return set_error(FGB_EINVAL, "fgb_ewise_reduce: need B or B_dense");
-  if (!B && ldb < A->ncols) return set_error(FGB_EINVAL, "fgb_ewise_reduce: ldb < ncols");
+  if (!B && B_dense && ldb < A->ncols) return set_error(FGB_EINVAL, "fgb_ewise_reduce: ldb < ncols");
   if (A->val_t != dtype) return set_error(FGB_EUNSUPPORTED, "fgb_ewise_reduce: A dtype != dtype");
   if (dtype != FGB_F32 && dtype != FGB_F64)
     return set_error(FGB_EUNSUPPORTED, "fgb_ewise_reduce: dtype %d", dtype);

@@ -24,8 +24,11 @@ namespace fgb {
 int set_error(int code, const char* fmt, ...);
 void clear_error();
 
-inline cudaStream_t pick_stream(fgb_ctx* ctx, void* s) {
-  return s ? static_cast<cudaStream_t>(s) : ctx->stream;
+// NULL is CUDA's legacy default stream (the convention of every CUDA
+// library), so calls order with other work issued on it; the context's own
+// stream is used only when a caller passes it explicitly.
+inline cudaStream_t pick_stream(fgb_ctx*, void* s) {
+  return s ? static_cast<cudaStream_t>(s) : cudaStreamLegacy;
 }
 
 // Returns FGB_ECUDA with a message if the last launch failed.

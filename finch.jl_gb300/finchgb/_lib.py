@@ -73,7 +73,16 @@ SIGNATURES: dict[str, tuple] = {
                                c_void_p, c_void_p, c_void_p]),
     "fgb_ewise_reduce": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
                                  c_int64, c_void_p, c_int, c_uint, c_void_p]),
+    "fgb_dense_dot": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_dense_axpby": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_int, c_void_p]),
+    "fgb_dense_map": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
+                              c_void_p]),
+    "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
+
+# fgb_map_op
+MAP_ADD, MAP_SUB, MAP_MUL, MAP_DIV, MAP_MIN, MAP_MAX = range(6)
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

@@ -219,6 +219,44 @@ def ewise(op: int, A: DeviceSparse, B: DeviceSparse) -> DeviceSparse:
     return DeviceSparse(A.nrows, A.ncols, out_ptr, out_idx, out_val, A.orient, 0)
 
 
+def dot(x: torch.Tensor, y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """0-d device scalar sum_i x[i] y[i] (deterministic)."""
+    if out is None:
+        out = torch.empty((), dtype=x.dtype, device=x.device)
+    L.call("fgb_dense_dot", _ctx_for(x), dtype_code(x), x.numel(), _dptr(x), _dptr(y),
+           out.data_ptr(), stream_ptr())
+    return out
+
+
+def axpby(alpha: torch.Tensor | None, x: torch.Tensor, beta: torch.Tensor | None,
+          y: torch.Tensor | None, out: torch.Tensor | None = None, signs: int = 0) -> torch.Tensor:
+    """out = (+/-)alpha*x + (+/-)beta*y with device-scalar alpha/beta (None = 1)."""
+    if out is None:
+        out = torch.empty_like(x)
+    L.call("fgb_dense_axpby", _ctx_for(x), dtype_code(x), x.numel(),
+           None if alpha is None else alpha.data_ptr(), _dptr(x),
+           None if beta is None else beta.data_ptr(), _dptr(y), _dptr(out), signs, stream_ptr())
+    return out
+
+
+def dense_map(op: int, x: torch.Tensor, y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """out = op.(x, y) for op in MAP_ADD/SUB/MUL/MIN/MAX."""
+    if out is None:
+        out = torch.empty_like(x)
+    L.call("fgb_dense_map", _ctx_for(x), op, dtype_code(x), x.numel(), _dptr(x), _dptr(y),
+           _dptr(out), stream_ptr())
+    return out
+
+
+def scalar_op(op: int, a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """0-d device scalar op(a, b)."""
+    if out is None:
+        out = torch.empty((), dtype=a.dtype, device=a.device)
+    L.call("fgb_scalar_op", _ctx_for(a), op, dtype_code(a), a.data_ptr(), b.data_ptr(),
+           out.data_ptr(), stream_ptr())
+    return out
+
+
 def ewise_reduce(dims: int, A: DeviceSparse, B: DeviceSparse | None = None,
                  B_dense: torch.Tensor | None = None, y: torch.Tensor | None = None) -> torch.Tensor:
     """sum(A .* B; dims) (dims 0 = all, 1 = over rows, 2 = over columns)."""

@@ -28,7 +28,7 @@
  *
  * Pointers passed to compute entry points are DEVICE pointers (from
  * fgb_malloc, cudaMalloc or another allocator on the same device).  All work
- * is issued on `stream` (a cudaStream_t; NULL = the context's own stream) and
+ * is issued on `stream` (a cudaStream_t; NULL = CUDA's default stream) and
  * is asynchronous unless stated otherwise.
  */
 #ifndef FINCHGB_H
@@ -213,12 +213,45 @@ FGB_API int fgb_ewise_fill(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_
  *   dims = 2:  y[i] = sum_j A[i,j] * B[i,j]      (length m)
  *   dims = 1:  y[j] = sum_i A[i,j] * B[i,j]      (length n)
  *   dims = 0:  y[0] = sum_ij A[i,j] * B[i,j]     (all dims)
- * B is a sparse matrix of the same shape/orientation (B_dense == NULL) or a
- * dense row-major m x n matrix (B == NULL, ld = ldb).  F32 or F64.
+ * B is a sparse matrix of the same shape/orientation (B_dense == NULL), a
+ * dense row-major m x n matrix (B == NULL, ld = ldb), or absent (both NULL:
+ * B = 1, i.e. reduce(+, A; dims), test/reference64/interface/
+ * reduce_default.txt).  F32 or F64.
  * Replaces compute(sum(lazy(A) .* lazy(B); dims)) (src/interface/lazy.jl). */
 FGB_API int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_sparse* B,
                      const void* B_dense, int64_t ldb, void* y, int dtype, unsigned flags,
                      void* stream);
+
+/* ---- dense Element levels and 0-d Scalars ------------------------------ */
+
+typedef enum {
+  FGB_MAP_ADD = 0,
+  FGB_MAP_SUB = 1,
+  FGB_MAP_MUL = 2,
+  FGB_MAP_DIV = 3, /* fgb_scalar_op only */
+  FGB_MAP_MIN = 4,
+  FGB_MAP_MAX = 5
+} fgb_map_op;
+
+/* out[0] = sum_i x[i] * y[i] (deterministic: fixed block partials folded in
+ * index order).  F32 or F64; out is a device scalar.  Replaces
+ * `@einsum s[] += x[i]*y[i]` into a Scalar (src/tensors/scalars.jl:22-93). */
+FGB_API int fgb_dense_dot(fgb_ctx* ctx, int dtype, int64_t n, const void* x, const void* y,
+                          void* out, void* stream);
+
+/* out[i] = a*x[i] + b*y[i], a and b read from device scalars (NULL = 1;
+ * signs bit 0 negates a, bit 1 negates b; y NULL = 0).  F32 or F64. */
+FGB_API int fgb_dense_axpby(fgb_ctx* ctx, int dtype, int64_t n, const void* alpha, const void* x,
+                            const void* beta, const void* y, void* out, int signs, void* stream);
+
+/* out[i] = op(x[i], y[i]) for op in ADD/SUB/MUL/MIN/MAX, the pointwise
+ * `x = op.(x, y)` maps of Finch programs.  F64, F32, I32 (wrapping), I64. */
+FGB_API int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void* x,
+                          const void* y, void* out, void* stream);
+
+/* out[0] = op(a[0], b[0]) on device scalars (ADD/SUB/MUL/DIV/MIN/MAX). */
+FGB_API int fgb_scalar_op(fgb_ctx* ctx, int op, int dtype, const void* a, const void* b,
+                          void* out, void* stream);
 
 #ifdef __cplusplus
 }
