@@ -9,10 +9,14 @@ divided by time, in GB/s, and that figure against the measured HBM peak.
 
 Arms:
   default            the CUDA path; `value` = device-resident inputs,
-                     `e2e` = host buffers through the public API (pinned H2D
-                     of A and B, SpMM, D2H of C inside the timed region).
+                     `e2e` = host buffers through the C ABI (pinned H2D of
+                     A and B with fgb_upload, fgb_spmm_ex, D2H of C with
+                     fgb_download, all inside the timed region).
   --impl reference   Finch's CPU nest (the oracle's C restatement, all host
-                     threads) on a bounded row sample of the same workload.
+                     threads) over the same matrix.
+
+The schedule (lanes per row group = column slab, merge-path item length) is
+picked by a short autotune on the same inputs before the timed region.
 
 Multi-GPU (torchrun): replicas -- every rank runs the same workload on its
 own GPU, no data-path collective; value = all ranks' bytes / max time.
@@ -20,12 +24,12 @@ own GPU, no data-path collective; value = all ranks' bytes / max time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 from pathlib import Path
 
@@ -35,11 +39,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "finch.jl_gb300"))
 sys.path.insert(0, str(ROOT))
 
-M = N_COLS = 1_000_000
 NNZ_MEAN = 16.0
 NK = 128
 SEED = 20261203
-WORKLOAD = "spmm_csr_zipf1.5_1Mx1M_nnz16M_k128_fp32"
+
+
+def workload_name(rows: int) -> str:
+    return f"spmm_csr_zipf1.5_{rows // 1000}Kx{rows // 1000}K_nnz{int(rows * NNZ_MEAN) // 1000}K_k{NK}_fp32"
 
 
 def algorithmic_bytes(nrows: int, nnz: int, nk: int, ncols_b: int, ptr_bytes: int = 4) -> int:
@@ -47,12 +53,12 @@ def algorithmic_bytes(nrows: int, nnz: int, nk: int, ncols_b: int, ptr_bytes: in
     return ptr_bytes * (nrows + 1) + 8 * nnz + 4 * ncols_b * nk + 4 * nrows * nk
 
 
-def make_inputs():
+def make_inputs(rows: int):
     from finchgb.workloads import zipf_csr
 
     rng = np.random.default_rng(SEED)
-    A = zipf_csr(rng, M, N_COLS, mean=NNZ_MEAN, a=1.5, cap=50_000, dtype=np.float32)
-    B = rng.standard_normal((N_COLS, NK), dtype=np.float32)
+    A = zipf_csr(rng, rows, rows, mean=NNZ_MEAN, a=1.5, cap=50_000, dtype=np.float32)
+    B = rng.standard_normal((rows, NK), dtype=np.float32)
     return A, B
 
 
@@ -63,15 +69,15 @@ def load_peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def load_traffic() -> int | None:
-    """Per-launch DRAM bytes of the SpMM kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "spmm_csr_pull_zipf1M_k128.md"
+def load_traffic() -> tuple[int | None, str | None]:
+    """Per-step DRAM bytes of the SpMM kernels from the committed ncu summary."""
+    p = ROOT / "profiles" / "spmm_merge_zipf1M_k128.md"
     if not p.exists():
-        return None
+        return None, None
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
-            return int(float(line.split(":", 1)[1].strip()))
-    return None
+        if line.startswith("traffic_bytes_per_step:"):
+            return int(float(line.split(":", 1)[1].strip())), str(p.relative_to(ROOT))
+    return None, None
 
 
 class ClockSampler:
@@ -84,6 +90,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -97,7 +104,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.out = ""
         if self.proc:
             self.proc.terminate()
             try:
@@ -120,33 +126,38 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for _, _, r in rows for k, v in enumerate(r) if v == "Active"})
-        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons, "samples": len(rows)}
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def cpu_reference_run(A, B, rows: int, threads: int) -> tuple[float, float]:
-    """Finch's row-parallel CPU nest over the first `rows` rows of A.
-
-    Returns (seconds for the sample, seconds scaled to the whole matrix by
-    the fraction of stored entries the sample holds)."""
+def cpu_reference_pass(A, B, threads: int) -> float:
+    """One pass of Finch's row-parallel CPU SpMM nest over the whole matrix."""
     import oracle
 
-    p = A.ptr[: rows + 1]
-    nnz = int(p[-1] - 1)
-    idx = A.idx[:nnz]
-    val = A.val[:nnz]
-    C = np.empty((rows, NK), dtype=np.float32)
+    C = np.empty((A.nrows, NK), dtype=np.float32)
     t0 = time.perf_counter()
-    oracle.spmm_csr(rows, A.ncols, p, idx, val, B, C=C, nthreads=threads)
-    dt = time.perf_counter() - t0
-    return dt, dt * (A.nnz / max(nnz, 1))
+    oracle.spmm_csr(A.nrows, A.ncols, A.ptr, A.idx, A.val, B, C=C, nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(A, B, nbytes: int, min_seconds: float = 10.0, max_passes: int = 30) -> dict:
+    import oracle
+
+    threads = oracle.max_threads()
+    cpu_reference_pass(A, B, threads)  # warm caches and page in
+    times = []
+    while sum(times) < min_seconds and len(times) < max_passes:
+        times.append(cpu_reference_pass(A, B, threads))
+    t = statistics.median(times)
+    return {"value": round(nbytes / t / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"whole matrix, {len(times)} passes ({sum(times):.1f} s) of Finch's "
+                      f"row-parallel SpMM nest (oracle C restatement, static split), median "
+                      f"{1e3 * t:.1f} ms"}
 
 
 def run_reference(args):
@@ -155,34 +166,52 @@ def run_reference(args):
         return
     import oracle
 
-    A, B = make_inputs()
+    A, B = make_inputs(args.rows)
     threads = oracle.max_threads()
-    rows = 100_000  # bounded sample: ~10% of the rows
+    nbytes = algorithmic_bytes(A.nrows, A.nnz, NK, A.ncols)
     for _ in range(max(args.warmup, 0)):
-        cpu_reference_run(A, B, rows // 10, threads)
-    nbytes = algorithmic_bytes(M, A.nnz, NK, N_COLS)
-    times, full = [], []
-    for _ in range(args.steps):
-        dt, dt_full = cpu_reference_run(A, B, rows, threads)
-        times.append(dt)
-        full.append(dt_full)
-    total = sum(full)
+        cpu_reference_pass(A, B, threads)
+    times = [cpu_reference_pass(A, B, threads) for _ in range(args.steps)]
+    total = sum(times)
     value = nbytes * args.steps / total / 1e9
     line = {"impl": "reference", "metric": "spmm_gbps_algorithmic", "value": round(value, 3),
             "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
-            "sample_ms_per_step": round(1e3 * sum(times) / args.steps, 3),
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "sample": f"first {rows} of {M} rows",
-                       "parallelism": f"cpu{threads}"},
+            "config": {"workload": workload_name(args.rows), "parallelism": f"cpu{threads}"},
             "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                              "kind": "port",
-                             "sample": f"Finch's row-parallel SpMM nest (oracle C restatement, "
-                                       f"static split) over rows 1..{rows} of A; time scaled "
-                                       f"to the whole matrix by stored entries"},
+                             "sample": "whole matrix per step: Finch's row-parallel SpMM nest "
+                                       "(oracle C restatement, static split)"},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def autotune(A, B, C, reps: int = 3, verbose: bool = False):
+    """Times each (lanes, path) schedule on the real inputs; returns the best
+    and the table (ms per SpMM)."""
+    import torch
+
+    from finchgb import device as dev
+
+    table = {}
+    for lanes in (2, 4, 8, 16, 32):
+        for path in (128, 256, 512, 1024):
+            dev.spmm(A, B, C, lanes=lanes, path=path)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                dev.spmm(A, B, C, lanes=lanes, path=path)
+            e1.record()
+            torch.cuda.synchronize()
+            table[(lanes, path)] = e0.elapsed_time(e1) / reps
+            if verbose:
+                print(f"  lanes={lanes:2d} path={path:5d}: {table[(lanes, path)]:.3f} ms",
+                      file=sys.stderr)
+    best = min(table, key=table.get)
+    return best, table
 
 
 def run_gpu(args):
@@ -200,24 +229,29 @@ def run_gpu(args):
     from finchgb import device as dev
 
     build.build()
-    A_h, B_h = make_inputs()
-    nbytes = algorithmic_bytes(M, A_h.nnz, NK, N_COLS)
+    A_h, B_h = make_inputs(args.rows)
+    M = A_h.nrows
+    nbytes = algorithmic_bytes(M, A_h.nnz, NK, A_h.ncols)
 
     # ---- value: device-resident inputs
     A = dev.DeviceSparse.from_host(A_h.nrows, A_h.ncols, A_h.ptr, A_h.idx, A_h.val, orient="csr")
     B = torch.from_numpy(B_h).to(device)
     C = torch.empty((M, NK), dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream()
+    (lanes, path), table = autotune(A, B, C, verbose=args.sweep)
+    slabs = -(-NK // (4 * lanes))
+    launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
 
     def step():
-        dev.spmm(A, B, C)
+        dev.spmm(A, B, C, lanes=lanes, path=path)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(max(args.warmup, 3)):
+    warmup = max(args.warmup, 3)
+    for _ in range(warmup):
         step()
     barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -234,91 +268,96 @@ def run_gpu(args):
         t_end.record(stream)
         barrier()
     total_ms = t_start.elapsed_time(t_end)
-    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    step_ms = [a.elapsed_time(b) for a, b in ev]
     if world > 1:
         t = torch.tensor([total_ms], device=device)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = nbytes * args.steps * world / (total_ms / 1e3) / 1e9
 
-    # ---- e2e: host buffers -> public API -> host result
-    ptr32 = torch.from_numpy(A_h.ptr.astype(np.int32)).pin_memory()
-    idx32 = torch.from_numpy(A_h.idx.astype(np.int32)).pin_memory()
-    val_h = torch.from_numpy(A_h.val).pin_memory()
-    B_pin = torch.from_numpy(B_h).pin_memory()
-    C_pin = torch.empty((M, NK), dtype=torch.float32).pin_memory()
-    d_ptr = torch.empty_like(ptr32, device=device)
-    d_idx = torch.empty_like(idx32, device=device)
-    d_val = torch.empty_like(val_h, device=device)
-    d_B = torch.empty_like(B_pin, device=device)
-    d_C = torch.empty((M, NK), dtype=torch.float32, device=device)
-    A_e = dev.DeviceSparse(M, N_COLS, d_ptr, d_idx, d_val, "csr", 1)
-    h2d = sum(t.numel() * t.element_size() for t in (ptr32, idx32, val_h, B_pin))
-    d2h = C_pin.numel() * C_pin.element_size()
+    line = {"metric": "spmm_gbps_algorithmic", "value": round(value, 1), "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": warmup,
+            "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": workload_name(args.rows), "nnz": int(A_h.nnz), "k": NK,
+                       "algorithmic_bytes_per_step": nbytes,
+                       "schedule": {"lanes": lanes, "column_slab": 4 * lanes,
+                                    "merge_path_item": path,
+                                    "autotune_ms": {f"{k[0]}x{k[1]}": round(v, 4)
+                                                    for k, v in table.items()}},
+                       "l2": "inputs larger than L2 (1.16 GB per step vs 129 MB)",
+                       "parallelism": f"replicas{world}"},
+            "gpu_launches": args.steps * launches_per_step}
 
-    def e2e_step():
-        d_ptr.copy_(ptr32, non_blocking=True)
-        d_idx.copy_(idx32, non_blocking=True)
-        d_val.copy_(val_h, non_blocking=True)
-        d_B.copy_(B_pin, non_blocking=True)
-        dev.spmm(A_e, d_B, d_C)
-        C_pin.copy_(d_C, non_blocking=True)
+    # ---- e2e: host buffers through the C ABI -> host result
+    if not args.no_e2e:
+        ctx = dev.context()
+        lib = L.load()
+        ptr32 = torch.from_numpy(A_h.ptr.astype(np.int32)).pin_memory()
+        idx32 = torch.from_numpy(A_h.idx.astype(np.int32)).pin_memory()
+        val_h = torch.from_numpy(A_h.val).pin_memory()
+        B_pin = torch.from_numpy(B_h).pin_memory()
+        C_pin = torch.empty((M, NK), dtype=torch.float32).pin_memory()
+        d_ptr = torch.empty(ptr32.shape, dtype=torch.int32, device=device)
+        d_idx = torch.empty(idx32.shape, dtype=torch.int32, device=device)
+        d_val = torch.empty(val_h.shape, dtype=torch.float32, device=device)
+        d_B = torch.empty(B_pin.shape, dtype=torch.float32, device=device)
+        d_C = torch.empty((M, NK), dtype=torch.float32, device=device)
+        A_e = dev.DeviceSparse(M, A_h.ncols, d_ptr, d_idx, d_val, "csr", 1)
+        desc = A_e.desc()
+        tune = L.FgbSpmmTuning(lanes, 0, path)
+        h2d_pairs = [(d_ptr, ptr32), (d_idx, idx32), (d_val, val_h), (d_B, B_pin)]
+        h2d = sum(h.numel() * h.element_size() for _, h in h2d_pairs)
+        d2h = C_pin.numel() * C_pin.element_size()
 
-    for _ in range(3):
-        e2e_step()
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2e_steps = max(3, args.steps // 4)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        e2e_step()
-    e1.record(stream)
-    barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = nbytes * e2e_steps * world / (e2e_ms / 1e3) / 1e9
-    ok = np.allclose(C_pin[:1000].numpy(), C[:1000].cpu().numpy(), rtol=0, atol=0)
+        def e2e_step():
+            s = dev.stream_ptr()
+            for d, h in h2d_pairs:
+                L.check(lib.fgb_upload(ctx, d.data_ptr(), h.data_ptr(), h.numel() * h.element_size(), s))
+            L.check(lib.fgb_spmm_ex(ctx, ctypes.byref(desc), d_B.data_ptr(), NK, NK, d_C.data_ptr(),
+                                    NK, L.F32, 0, ctypes.byref(tune), s))
+            L.check(lib.fgb_download(ctx, C_pin.data_ptr(), d_C.data_ptr(), d2h, s))
 
-    # ---- roofline of the dominant kernel (one SpMM launch per step)
+        for _ in range(3):
+            e2e_step()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e2e_steps = max(3, args.steps // 4)
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        e2e_ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=device)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        ok = bool(np.array_equal(C_pin[:2000].numpy(), C[:2000].cpu().numpy()))
+        line["e2e"] = {"value": round(nbytes * e2e_steps * world / (e2e_ms / 1e3) / 1e9, 1),
+                       "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "steps": e2e_steps, "ms_per_step": round(e2e_ms / e2e_steps, 3),
+                       "result_matches_device_run": ok}
+        line["gpu_launches"] += (e2e_steps) * launches_per_step
+
+    # ---- roofline of the SpMM (plan + per-slab merge kernels + fix-up)
     peak, peak_kind = load_peaks()
-    avg_kernel_ms = sum(kernel_ms) / len(kernel_ms)
-    achieved = nbytes / (avg_kernel_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": load_traffic(), "kernel": "spmm_csr_pull<float,float,int,32,4>",
-                "algorithmic_bytes_per_launch": nbytes}
-
-    cpu_base = None
+    avg_ms = sum(step_ms) / len(step_ms)
+    achieved = nbytes / (avg_ms / 1e3) / 1e9
+    traffic, traffic_src = load_traffic()
+    line["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(achieved / peak, 4),
+                        "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                        "traffic": traffic, "traffic_source": traffic_src,
+                        "kernel": f"spmm_merge_k x{slabs} slabs + merge_plan_k + spmm_fixup_k",
+                        "algorithmic_bytes_per_launch": nbytes,
+                        "avg_launch_ms": round(avg_ms, 4)}
+    line["cpu_baseline"] = None
     if rank == 0 and not args.skip_cpu_baseline:
-        import oracle
-
-        threads = oracle.max_threads()
-        rows = 60_000
-        dt, dt_full = cpu_reference_run(A_h, B_h, rows, threads)
-        cpu_base = {"value": round(nbytes / dt_full / 1e9, 3), "unit": "GB/s", "cores": threads,
-                    "kind": "port",
-                    "sample": f"Finch's row-parallel SpMM nest (oracle C restatement) over rows "
-                              f"1..{rows} of A, {threads} threads, {dt:.2f} s; time scaled to "
-                              f"the whole matrix by stored entries"}
-
+        line["cpu_baseline"] = cpu_baseline(A_h, B_h, nbytes)
+    line["clocks"] = clk.summary()
     if rank == 0:
-        line = {"metric": "spmm_gbps_algorithmic", "value": round(value, 1), "unit": "GB/s",
-                "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-                "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded PCG64)",
-                "config": {"workload": WORKLOAD, "nnz": int(A_h.nnz), "k": NK,
-                           "algorithmic_bytes_per_step": nbytes,
-                           "l2": "inputs larger than L2 (1.16 GB per step vs 129 MB)",
-                           "parallelism": f"replicas{world}"},
-                "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h, "steps": e2e_steps,
-                        "ms_per_step": round(e2e_ms / e2e_steps, 3), "result_matches": bool(ok)},
-                "roofline": roofline, "cpu_baseline": cpu_base,
-                "gpu_launches": args.steps, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -330,7 +369,11 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rows", type=int, default=1_000_000,
+                    help="rows = columns of A (16 stored entries per row on average)")
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sweep", action="store_true", help="print the autotune table to stderr")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

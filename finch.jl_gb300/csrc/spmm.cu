@@ -18,73 +18,9 @@
 // into C[i, :] with atomics.
 #include "fgb_internal.cuh"
 #include "semiring.cuh"
+#include "spmm_common.cuh"
 
 namespace fgb {
-
-template <class T, int V>
-struct VecT {
-  T v[V];
-};
-
-template <class T, int V>
-__device__ __forceinline__ VecT<T, V> gather(const T* p, uint64_t pol);
-
-template <>
-__device__ __forceinline__ VecT<float, 4> gather<float, 4>(const float* p, uint64_t pol) {
-  float4 f = ld_gather_f32x4(p, pol);
-  return VecT<float, 4>{{f.x, f.y, f.z, f.w}};
-}
-template <>
-__device__ __forceinline__ VecT<double, 2> gather<double, 2>(const double* p, uint64_t pol) {
-  double2 d;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;"
-               : "=d"(d.x), "=d"(d.y)
-               : "l"(p), "l"(pol));
-  return VecT<double, 2>{{d.x, d.y}};
-}
-template <>
-__device__ __forceinline__ VecT<float, 1> gather<float, 1>(const float* p, uint64_t) {
-  return VecT<float, 1>{{__ldg(p)}};
-}
-template <>
-__device__ __forceinline__ VecT<double, 1> gather<double, 1>(const double* p, uint64_t) {
-  return VecT<double, 1>{{__ldg(p)}};
-}
-
-template <class T, int V>
-__device__ __forceinline__ void store_out(T* p, const VecT<T, V>& a, uint64_t pol) {
-#pragma unroll
-  for (int q = 0; q < V; ++q) p[q] = a.v[q];
-}
-template <>
-__device__ __forceinline__ void store_out<float, 4>(float* p, const VecT<float, 4>& a,
-                                                     uint64_t pol) {
-  st_stream_f32x4(p, make_float4(a.v[0], a.v[1], a.v[2], a.v[3]), pol);
-}
-
-template <class T, int V>
-__device__ __forceinline__ VecT<T, V> load_out(const T* p) {
-  VecT<T, V> r;
-#pragma unroll
-  for (int q = 0; q < V; ++q) r.v[q] = p[q];
-  return r;
-}
-
-// Value of stored entry p as the accumulation type.
-template <class T, class VT>
-__device__ __forceinline__ T load_val(const VT* val, int64_t p, uint64_t pol) {
-  return to_acc<T>(__ldg(val + p));
-}
-template <>
-__device__ __forceinline__ float load_val<float, float>(const float* val, int64_t p, uint64_t pol) {
-  return ld_stream_f32(val + p, pol);
-}
-
-template <class T, int V>
-__device__ __forceinline__ void acc_step(VecT<T, V>& acc, T a, const VecT<T, V>& b, int fm) {
-#pragma unroll
-  for (int q = 0; q < V; ++q) acc.v[q] = Semi<SR_PT, T>::step(acc.v[q], a, b.v[q], fm);
-}
 
 // One launch = one column slab [c0, c0 + G*V) (clipped to nk) of every row.
 template <class T, class VT, class PtrT, int G, int V>
@@ -221,15 +157,43 @@ static int default_lanes(int64_t nk, int vn, int64_t b_bytes) {
   return lanes;
 }
 
+// Default merge-path tuning: the column slab keeps the gathered slab of B
+// within about half of L2 (one slab when B already fits), items of 256
+// path steps.
+static void default_merge_tuning(const fgb_sparse* A, int64_t nk, size_t esz, int* lanes,
+                                 int64_t* path) {
+  const int vn = esz == 4 ? 4 : 2;
+  const double b_bytes = (double)A->ncols * (double)nk * (double)esz;
+  const double budget = 64.0 * 1024 * 1024;
+  int64_t slab = nk;
+  while (slab > vn * 4 && (double)A->ncols * slab * esz > budget) slab /= 2;
+  (void)b_bytes;
+  int64_t need = (slab + vn - 1) / vn;
+  int l = 4;
+  while (l < need && l < 32) l *= 2;
+  if (*lanes <= 0) *lanes = l;
+  if (*path <= 0) *path = 256;
+}
+
 template <class T, class VT>
 static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
-                     void* C, int64_t ldc, unsigned flags, int lanes, cudaStream_t s) {
+                     void* C, int64_t ldc, unsigned flags, int lanes, int64_t path,
+                     cudaStream_t s) {
   const int accumulate = (flags & FGB_ACCUMULATE) ? 1 : 0;
   int fm = FM_DEFAULT;
   if (flags & FGB_NO_FMA) fm = FM_NOFMA;
   if (flags & FGB_FMA) fm = FM_FMA;
   if (A->orient == FGB_CSR) {
     if (A->nrows == 0 || nk == 0) return FGB_OK;
+    constexpr int VN = sizeof(T) == 4 ? 4 : 2;
+    const bool vec_ok = (nk % VN == 0) && (ldb % VN == 0) && (ldc % VN == 0) &&
+                        ((uintptr_t)B % (VN * sizeof(T)) == 0) &&
+                        ((uintptr_t)C % (VN * sizeof(T)) == 0);
+    if (!(flags & FGB_FINCH_ORDER) && vec_ok) {
+      default_merge_tuning(A, nk, sizeof(T), &lanes, &path);
+      return spmm_merge(ctx, A, B, ldb, nk, C, ldc, sizeof(T) == 8 ? FGB_F64 : FGB_F32,
+                        accumulate, lanes, path, nullptr, 0, s);
+    }
     if (lanes <= 0) lanes = default_lanes(nk, sizeof(T) == 4 ? 4 : 2, A->ncols * nk * (int64_t)sizeof(T));
     if (A->ptr_t == FGB_I32)
       return dispatch_pull<T, VT, int32_t>(ctx, A, B, ldb, nk, C, ldc, accumulate, fm, lanes, s);
@@ -255,7 +219,7 @@ static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
 }
 
 int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
-              int64_t ldc, int dtype, unsigned flags, int lanes, void* stream) {
+              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream) {
   if (!ctx) return set_error(FGB_EINVAL, "fgb_spmm: null ctx");
   int rc = check_sparse(A, "fgb_spmm: A", true);
   if (rc) return rc;
@@ -264,11 +228,11 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
     return set_error(FGB_EINVAL, "fgb_spmm: null B or C");
   cudaStream_t s = pick_stream(ctx, stream);
   if (dtype == FGB_F32) {
-    if (A->val_t == FGB_F32) return run_typed<float, float>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+    if (A->val_t == FGB_F32) return run_typed<float, float>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
     if (A->val_t == FGB_BF16)
-      return run_typed<float, __nv_bfloat16>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+      return run_typed<float, __nv_bfloat16>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
   } else if (dtype == FGB_F64) {
-    if (A->val_t == FGB_F64) return run_typed<double, double>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, s);
+    if (A->val_t == FGB_F64) return run_typed<double, double>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
   }
   return set_error(FGB_EUNSUPPORTED, "fgb_spmm: no kernel for val %d / dtype %d", A->val_t, dtype);
 }
@@ -277,5 +241,16 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
 
 extern "C" int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
                         void* C, int64_t ldc, int dtype, unsigned flags, void* stream) {
-  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, 0, stream);
+  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, 0, 0, stream);
+}
+
+extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb,
+                           int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags,
+                           const fgb_spmm_tuning* tune, void* stream) {
+  int lanes = tune ? tune->lanes : 0;
+  int64_t path = tune ? tune->path : 0;
+  if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
+  if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");
+  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, lanes, path, stream);
 }

@@ -1,0 +1,81 @@
+// Vector helpers shared by the SpMM kernels: V consecutive k of a row of B
+// or C per lane, gathered with an L2 cache policy.
+#pragma once
+
+#include "fgb_internal.cuh"
+#include "semiring.cuh"
+
+namespace fgb {
+
+// Merge-path SpMM (spmm_merge.cu).
+size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
+int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
+               int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
+               size_t scratch_bytes, cudaStream_t s);
+
+template <class T, int V>
+struct VecT {
+  T v[V];
+};
+
+template <class T, int V>
+__device__ __forceinline__ VecT<T, V> gather(const T* p, uint64_t pol);
+
+template <>
+__device__ __forceinline__ VecT<float, 4> gather<float, 4>(const float* p, uint64_t pol) {
+  float4 f = ld_gather_f32x4(p, pol);
+  return VecT<float, 4>{{f.x, f.y, f.z, f.w}};
+}
+template <>
+__device__ __forceinline__ VecT<double, 2> gather<double, 2>(const double* p, uint64_t pol) {
+  double2 d;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;"
+               : "=d"(d.x), "=d"(d.y)
+               : "l"(p), "l"(pol));
+  return VecT<double, 2>{{d.x, d.y}};
+}
+template <>
+__device__ __forceinline__ VecT<float, 1> gather<float, 1>(const float* p, uint64_t) {
+  return VecT<float, 1>{{__ldg(p)}};
+}
+template <>
+__device__ __forceinline__ VecT<double, 1> gather<double, 1>(const double* p, uint64_t) {
+  return VecT<double, 1>{{__ldg(p)}};
+}
+
+template <class T, int V>
+__device__ __forceinline__ void store_out(T* p, const VecT<T, V>& a, uint64_t pol) {
+#pragma unroll
+  for (int q = 0; q < V; ++q) p[q] = a.v[q];
+}
+template <>
+__device__ __forceinline__ void store_out<float, 4>(float* p, const VecT<float, 4>& a,
+                                                     uint64_t pol) {
+  st_stream_f32x4(p, make_float4(a.v[0], a.v[1], a.v[2], a.v[3]), pol);
+}
+
+template <class T, int V>
+__device__ __forceinline__ VecT<T, V> load_out(const T* p) {
+  VecT<T, V> r;
+#pragma unroll
+  for (int q = 0; q < V; ++q) r.v[q] = p[q];
+  return r;
+}
+
+// Value of stored entry p as the accumulation type.
+template <class T, class VT>
+__device__ __forceinline__ T load_val(const VT* val, int64_t p, uint64_t pol) {
+  return to_acc<T>(__ldg(val + p));
+}
+template <>
+__device__ __forceinline__ float load_val<float, float>(const float* val, int64_t p, uint64_t pol) {
+  return ld_stream_f32(val + p, pol);
+}
+
+template <class T, int V>
+__device__ __forceinline__ void acc_step(VecT<T, V>& acc, T a, const VecT<T, V>& b, int fm) {
+#pragma unroll
+  for (int q = 0; q < V; ++q) acc.v[q] = Semi<SR_PT, T>::step(acc.v[q], a, b.v[q], fm);
+}
+
+}  // namespace fgb

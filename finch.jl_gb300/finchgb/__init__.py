@@ -1,6 +1,12 @@
 """finchgb -- GB300 (sm_103a) execution backend for Finch.jl's sparse loop nests.
 
-Layers:
+Finch-facing API (mirrors Finch.jl names):
+  levels     Dense, SparseList, SparseCOO, Element, Pattern
+  tensors    Tensor, swizzle, csr, fsprand, transfer, gpu
+  front ends einsum (@einsum), lazy/compute, finch (@finch programs),
+             tensordot, reduce, permutedims, broadcast, minimum, maximum
+  scheduler  GB300Scheduler, set_scheduler, with_scheduler, Scalar
+Lower layers:
   _lib       ctypes binding of libfinchgb.so (the C ABI of include/finchgb.h)
   device     device-resident level buffers + the kernel calls
   workloads  seeded synthetic inputs in Finch's level layout
@@ -8,6 +14,17 @@ Layers:
 from . import _lib
 from ._lib import FinchGBError
 from .device import DeviceSparse, context, ewise, ewise_reduce, sddmm, spmm, spmv
+from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, reduce, tensordot
+from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, default_scheduler,
+                        einsum, finch, get_scheduler, set_scheduler, with_scheduler)
+from .tensors import (GPU, Dense, Element, Pattern, SparseCOO, SparseList, SwizzleArray, Tensor,
+                      csr, fsprand, gpu, swizzle, transfer)
 
-__all__ = ["FinchGBError", "DeviceSparse", "context", "spmv", "spmm", "sddmm", "ewise",
-           "ewise_reduce", "_lib"]
+__all__ = [
+    "FinchGBError", "FinchGBUnsupported", "DeviceSparse", "context", "spmv", "spmm", "sddmm",
+    "ewise", "ewise_reduce", "LazyTensor", "lazy", "compute", "einsum", "finch", "tensordot",
+    "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",
+    "default_scheduler", "get_scheduler", "set_scheduler", "with_scheduler", "GPU", "Dense",
+    "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsprand",
+    "gpu", "swizzle", "transfer", "_lib",
+]

@@ -37,6 +37,10 @@ class FinchGBError(RuntimeError):
         super().__init__(f"[{STATUS_NAMES.get(status, status)}] {message}")
 
 
+class FgbSpmmTuning(ctypes.Structure):
+    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64)]
+
+
 class FgbSparse(ctypes.Structure):
     _fields_ = [("nrows", c_int64), ("ncols", c_int64), ("nnz", c_int64), ("orient", c_int32),
                 ("index_base", c_int32), ("ptr_t", c_int32), ("idx_t", c_int32),
@@ -65,6 +69,8 @@ SIGNATURES: dict[str, tuple] = {
                          c_uint, c_void_p]),
     "fgb_spmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,
                          c_int64, c_int, c_uint, c_void_p]),
+    "fgb_spmm_ex": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,
+                            c_int64, c_int, c_uint, POINTER(FgbSpmmTuning), c_void_p]),
     "fgb_sddmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
                           c_int64, c_void_p, c_int, c_uint, c_void_p]),
     "fgb_ewise_count": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,

@@ -180,15 +180,17 @@ def spmv(A: DeviceSparse, x: torch.Tensor, y: torch.Tensor | None = None,
     return y
 
 
-def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
-    """C (+)= A @ B for row-major B (n x nk)."""
+def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0,
+         lanes: int = 0, path: int = 0) -> torch.Tensor:
+    """C (+)= A @ B for row-major B (n x nk); lanes/path override the schedule."""
     nk = B.shape[1]
     if C is None:
         C = torch.empty((A.nrows, nk), dtype=B.dtype, device=B.device)
         flags &= ~L.ACCUMULATE
     d = A.desc()
-    L.call("fgb_spmm", _ctx_for(B), ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
-           C.stride(0), dtype_code(B), flags, stream_ptr())
+    tune = L.FgbSpmmTuning(lanes, 0, path)
+    L.call("fgb_spmm_ex", _ctx_for(B), ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
+           C.stride(0), dtype_code(B), flags, ctypes.byref(tune), stream_ptr())
     return C
 
 

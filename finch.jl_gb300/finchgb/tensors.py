@@ -1,0 +1,383 @@
+"""Finch's tensor construction API over level formats, host and device.
+
+Mirrors the constructors of Finch.jl's levels and Tensor wrapper:
+
+    Tensor(Dense(SparseList(Element(0.0))), A)      # CSC (Finch's CSCFormat)
+    Tensor(Dense(SparseList(Pattern())), A)         # Boolean pattern
+    Tensor(Dense(Element(0.0)), x)                  # dense vector
+    Tensor(Dense(Dense(Element(0.0))), B)           # dense matrix
+    Tensor(SparseCOO(2, Element(0.0)), A)           # COO
+    swizzle(Tensor(Dense(SparseList(Element(0.0))), A.T), 2, 1)  # CSR of A
+
+(src/tensors/levels/{dense,sparse_list,sparse_coo,element,pattern}_levels.jl,
+src/tensors/tensors.jl:10-69, src/tensors/combinators/swizzle.jl:1-58,
+src/Finch.jl:188-258).  Host buffers use Finch's layout (1-based Int64
+ptr/idx).  `transfer(gpu(), t)` moves the level buffers into HBM once
+(narrowing idx to int32); tensors then stay resident across calls.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .workloads import SparseBuffers, coo_to_csr, csc_from_dense
+
+
+# ---------------------------------------------------------------- levels
+
+
+@dataclass(frozen=True)
+class Element:
+    """Leaf level holding values; `fill_value` is the implicit value."""
+
+    fill_value: object = 0.0
+    dtype: object = None
+
+    def eltype(self):
+        if self.dtype is not None:
+            return np.dtype(self.dtype)
+        return np.asarray(self.fill_value).dtype
+
+
+@dataclass(frozen=True)
+class Pattern:
+    """Leaf level of a Boolean structure: stored entries are true, fill false."""
+
+    fill_value: bool = False
+
+    def eltype(self):
+        return np.dtype(np.bool_)
+
+
+@dataclass(frozen=True)
+class SparseList:
+    """Compressed fiber level (ptr/idx)."""
+
+    lvl: object
+    index_type: object = np.int64
+
+    def eltype(self):
+        return self.lvl.eltype()
+
+    @property
+    def fill_value(self):
+        return self.lvl.fill_value
+
+
+@dataclass(frozen=True)
+class Dense:
+    """Dense fiber level."""
+
+    lvl: object
+
+    def eltype(self):
+        return self.lvl.eltype()
+
+    @property
+    def fill_value(self):
+        return self.lvl.fill_value
+
+
+@dataclass(frozen=True)
+class SparseCOO:
+    """N-d coordinate list level."""
+
+    ndim: int
+    lvl: object
+
+    def eltype(self):
+        return self.lvl.eltype()
+
+    @property
+    def fill_value(self):
+        return self.lvl.fill_value
+
+
+def _kind(fmt) -> str:
+    if isinstance(fmt, Dense) and isinstance(fmt.lvl, (Element, Pattern)):
+        return "dense1"
+    if isinstance(fmt, Dense) and isinstance(fmt.lvl, Dense):
+        return "dense2"
+    if isinstance(fmt, Dense) and isinstance(fmt.lvl, SparseList):
+        return "csc"
+    if isinstance(fmt, SparseList) and isinstance(fmt.lvl, (Element, Pattern)):
+        return "sparse1"
+    if isinstance(fmt, SparseCOO) and fmt.ndim == 2:
+        return "coo"
+    raise NotImplementedError(f"level format {fmt} is outside the GB300 backend's formats")
+
+
+# ---------------------------------------------------------------- tensors
+
+
+class Tensor:
+    """A Finch tensor: a level format plus its buffers (host or device).
+
+    Storage by kind:
+      dense1/dense2   `data` (numpy, logical shape) / `ddata` (torch, row-major)
+      csc             `buf` (SparseBuffers, orient csc) / `dsparse` (DeviceSparse)
+      sparse1         a 1 x n CSR in `buf` / `dsparse`
+      coo             COO triplets (converted to CSC on transfer)
+    """
+
+    def __init__(self, fmt, arr=None, shape=None, _buf=None):
+        self.fmt = fmt
+        self.kind = _kind(fmt)
+        self.fill_value = fmt.fill_value
+        self.dtype = fmt.eltype()
+        self.data = None
+        self.buf: SparseBuffers | None = _buf
+        self.ddata = None
+        self.dsparse = None
+        self.coo = None
+        if _buf is not None:
+            self.shape = (_buf.nrows, _buf.ncols) if self.kind != "sparse1" else (_buf.ncols,)
+            return
+        if arr is None:
+            if shape is None:
+                raise ValueError("Tensor needs an array or a shape")
+            arr = np.full(shape, self.fill_value, dtype=self.dtype)
+        if isinstance(arr, Tensor):
+            arr = arr.todense()
+        arr = _as_array(arr, self.dtype)
+        self.shape = tuple(arr.shape)
+        fill = np.asarray(self.fill_value, dtype=self.dtype)
+        if self.kind == "dense1":
+            assert arr.ndim == 1, "Dense(Element) holds a vector"
+            self.data = np.ascontiguousarray(arr)
+        elif self.kind == "dense2":
+            assert arr.ndim == 2
+            self.data = np.ascontiguousarray(arr)
+        elif self.kind == "csc":
+            assert arr.ndim == 2
+            b = csc_from_dense(np.where(arr != fill, arr, 0) if arr.dtype != np.bool_ else arr)
+            if isinstance(fmt.lvl.lvl, Pattern):
+                b.val = None
+            else:
+                b.val = b.val.astype(self.dtype)
+            self.buf = b
+        elif self.kind == "sparse1":
+            assert arr.ndim == 1
+            nz = np.flatnonzero(arr != fill)
+            self.buf = SparseBuffers(1, arr.size, np.array([1, nz.size + 1], np.int64),
+                                     nz.astype(np.int64) + 1,
+                                     None if isinstance(fmt.lvl, Pattern) else arr[nz].astype(self.dtype),
+                                     "csr")
+        elif self.kind == "coo":
+            I, J = np.nonzero(arr != fill)
+            order = np.lexsort((I, J))  # Finch sorts by reverse coordinates (column-major)
+            self.coo = (I[order] + 1, J[order] + 1, arr[I[order], J[order]])
+
+    # -- constructors from level buffers (zero-copy on the host)
+    @classmethod
+    def from_buffers(cls, fmt, buf: SparseBuffers) -> "Tensor":
+        return cls(fmt, _buf=buf)
+
+    @property
+    def ndim(self) -> int:
+        return len(self.shape)
+
+    @property
+    def on_device(self) -> bool:
+        return self.ddata is not None or self.dsparse is not None
+
+    def is_sparse(self) -> bool:
+        return self.kind in ("csc", "sparse1", "coo")
+
+    def todense(self) -> np.ndarray:
+        if self.kind in ("dense1", "dense2"):
+            if self.data is None:
+                self.data = self.ddata.cpu().numpy()
+            return self.data
+        if self.kind == "coo":
+            out = np.full(self.shape, self.fill_value, dtype=self.dtype)
+            I, J, V = self.coo
+            out[I - 1, J - 1] = V
+            return out
+        buf = self.host_buffers()
+        D = buf.todense()
+        if buf.val is None:
+            D = D != 0
+        out = np.full(buf.todense().shape, self.fill_value, dtype=self.dtype)
+        mask = _stored_mask(buf)
+        out[mask] = D[mask]
+        return out.reshape(self.shape)
+
+    def host_buffers(self) -> SparseBuffers:
+        if self.buf is None and self.dsparse is not None:
+            ptr, idx, val = self.dsparse.to_host()
+            d = self.dsparse
+            self.buf = SparseBuffers(d.nrows, d.ncols, ptr, idx, val, d.orient)
+        return self.buf
+
+    def countstored(self) -> int:
+        if self.kind in ("dense1", "dense2"):
+            return int(np.prod(self.shape))
+        if self.kind == "coo":
+            return len(self.coo[0])
+        return self.dsparse.nnz if self.dsparse is not None else self.buf.nnz
+
+    def __repr__(self):
+        where = "HBM" if self.on_device else "host"
+        return f"Tensor({self.fmt}, shape={self.shape}, {where})"
+
+    def __eq__(self, other):  # value-wise, like src/interface/compare.jl
+        a = self.todense()
+        b = other.todense() if isinstance(other, (Tensor, SwizzleArray)) else np.asarray(other)
+        return a.shape == b.shape and bool(np.all(a == b))
+
+    __hash__ = None
+
+
+def _stored_mask(buf: SparseBuffers) -> np.ndarray:
+    mask = np.zeros((buf.nrows, buf.ncols), dtype=bool)
+    f = np.repeat(np.arange(buf.nfibers), np.diff(buf.ptr))
+    if buf.orient == "csc":
+        mask[buf.idx - 1, f] = True
+    else:
+        mask[f, buf.idx - 1] = True
+    return mask
+
+
+def _as_array(arr, dtype) -> np.ndarray:
+    try:
+        import scipy.sparse as sp
+
+        if sp.issparse(arr):
+            arr = arr.toarray()
+    except ImportError:
+        pass
+    return np.asarray(arr).astype(dtype, copy=False)
+
+
+class SwizzleArray:
+    """A permuted view of a tensor (src/tensors/combinators/swizzle.jl).
+
+    swizzle(Tensor(Dense(SparseList(...)), A^T), 2, 1) is Finch's CSR of A."""
+
+    def __init__(self, body: Tensor, dims: tuple[int, ...]):
+        self.body = body
+        self.dims = tuple(dims)
+        self.shape = tuple(body.shape[d - 1] for d in self.dims)
+        self.dtype = body.dtype
+        self.fill_value = body.fill_value
+
+    @property
+    def ndim(self):
+        return len(self.shape)
+
+    @property
+    def kind(self):
+        return self.body.kind
+
+    def is_sparse(self):
+        return self.body.is_sparse()
+
+    def todense(self):
+        return np.transpose(self.body.todense(), [d - 1 for d in self.dims])
+
+    def __eq__(self, other):
+        b = other.todense() if hasattr(other, "todense") else np.asarray(other)
+        return bool(np.all(self.todense() == b))
+
+    __hash__ = None
+
+    def __repr__(self):
+        return f"swizzle({self.body!r}, {', '.join(map(str, self.dims))})"
+
+
+def swizzle(t, *dims) -> SwizzleArray:
+    if isinstance(t, SwizzleArray):
+        return SwizzleArray(t.body, tuple(t.dims[d - 1] for d in dims))
+    return SwizzleArray(t, dims)
+
+
+def csr(A, fill_value=0.0, dtype=None) -> SwizzleArray:
+    """Finch's CSR of a matrix: swizzle(Tensor(Dense(SparseList(Element)), A^T), 2, 1)."""
+    A = np.asarray(A) if not hasattr(A, "toarray") else A.toarray()
+    el = Element(fill_value, dtype or A.dtype)
+    return swizzle(Tensor(Dense(SparseList(el)), A.T), 2, 1)
+
+
+def fsprand(rng, m: int, n: int, p: float, dtype=np.float64) -> Tensor:
+    """Finch's fsprand + Tensor(Dense(SparseList(Element(0))), ...)."""
+    from .workloads import fsprand as _fsprand
+
+    b = _fsprand(rng, m, n, p, dtype=dtype)
+    return Tensor.from_buffers(Dense(SparseList(Element(np.zeros((), dtype)[()], dtype))), b)
+
+
+# ---------------------------------------------------------------- devices
+
+
+@dataclass(frozen=True)
+class GPU:
+    """The CUDA device target (Finch's AbstractDevice, src/architecture.jl)."""
+
+    index: int = 0
+
+
+def gpu(index: int = 0) -> GPU:
+    return GPU(index)
+
+
+def transfer(device, t):
+    """Moves a tensor's level buffers into HBM (Finch's transfer(device, tns)).
+
+    Sparse levels are narrowed to int32 idx once; dense levels are copied
+    row-major.  Returns the same tensor object, now resident."""
+    import torch
+
+    from . import device as dev
+
+    if isinstance(t, SwizzleArray):
+        transfer(device, t.body)
+        return t
+    if t.on_device:
+        return t
+    idx = device.index if isinstance(device, GPU) else int(device)
+    if t.kind in ("dense1", "dense2"):
+        src = np.ascontiguousarray(t.data)
+        tt = torch.from_numpy(src if src.dtype != np.bool_ else src.astype(np.uint8))
+        t.ddata = tt.to(torch.device("cuda", idx))
+        return t
+    if t.kind == "coo":
+        I, J, V = t.coo
+        b = coo_to_csr(t.shape[1], t.shape[0], J, I, V)  # CSR of A^T == CSC of A
+        t.buf = SparseBuffers(t.shape[0], t.shape[1], b.ptr, b.idx, b.val, "csc")
+        t.kind = "csc"
+    b = t.buf
+    val = b.val
+    t.dsparse = dev.DeviceSparse.from_host(b.nrows, b.ncols, b.ptr, b.idx, val, orient=b.orient,
+                                           base=1, device=idx)
+    return t
+
+
+def dense_from_device(x, fill_value=0.0) -> Tensor:
+    """Wraps a device array (torch) as a Dense tensor resident in HBM."""
+    dt = np.dtype(str(x.dtype).replace("torch.", "").replace("uint8", "bool"))
+    fmt = Dense(Element(fill_value, dt)) if x.dim() == 1 else Dense(Dense(Element(fill_value, dt)))
+    t = Tensor.__new__(Tensor)
+    t.fmt, t.kind = fmt, ("dense1" if x.dim() == 1 else "dense2")
+    t.fill_value, t.dtype = fill_value, dt
+    t.data, t.buf, t.ddata, t.dsparse, t.coo = None, None, x, None, None
+    t.shape = tuple(x.shape)
+    return t
+
+
+def sparse_from_device(d, fill_value=0.0) -> Tensor:
+    """Wraps a DeviceSparse as a resident tensor (CSC kind, or swizzled CSR)."""
+    import torch
+
+    dt = np.float64 if d.val is None else np.dtype(str(d.val.dtype).replace("torch.", "").replace("bfloat16", "float32"))
+    lvl = Pattern() if d.val is None else Element(fill_value, dt)
+    fmt = Dense(SparseList(lvl))
+    t = Tensor.__new__(Tensor)
+    t.fmt, t.kind, t.fill_value, t.dtype = fmt, "csc", fill_value, np.dtype(dt)
+    t.data, t.buf, t.ddata, t.coo = None, None, None, None
+    if d.orient == "csc":
+        t.dsparse, t.shape = d, (d.nrows, d.ncols)
+        return t
+    t.dsparse, t.shape = d.T(), (d.ncols, d.nrows)  # CSR of A == CSC of A^T
+    return swizzle(t, 2, 1)

@@ -178,12 +178,34 @@ FGB_API int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr, i
 FGB_API int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* x, int x_t, void* y,
              int y_t, unsigned flags, void* stream);
 
-/* SpMM: C[i,k] += A[i,j] * B[j,k], k < nk.  B row-major (ldb), C row-major
- * (ldc).  F32 (A F32 or BF16 values, B/C F32) or F64.  Replaces
- * `@einsum C[i,k] += A[i,j]*B[j,k]` = tensordot(A,B,(2,1))
- * (src/interface/lazy.jl:215-257,387-404). */
+/* SpMM: C[i,k] = (C[i,k] +) sum_j A[i,j] * B[j,k], k < nk.  B row-major
+ * (ldb), C row-major (ldc).  F32 (A F32 or BF16 values, B/C F32) or F64.
+ * Replaces `@einsum C[i,k] += A[i,j]*B[j,k]` = tensordot(A,B,(2,1))
+ * (src/interface/lazy.jl:215-257,387-404).  CSR runs load-balanced
+ * (merge-path items, deterministic carry fix-up); with FGB_FINCH_ORDER (or
+ * an unaligned nk/ldb/ldc) each row is one running sum per column, j
+ * ascending, bit-identical to Finch's nest.  CSC runs as a push with
+ * atomics. */
 FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
              int64_t ldc, int dtype, unsigned flags, void* stream);
+
+/* Schedule knobs of the load-balanced CSR SpMM (the autotuner's search
+ * space).  CSR SpMM walks merge-path items of `path` steps (rows + stored
+ * entries) with groups of `lanes` lanes, each lane holding 4 (fp32) or 2
+ * (fp64) consecutive columns; columns are processed in slabs of
+ * lanes * vector-width, one launch per slab, so the gathered slab of B stays
+ * L2-resident.  Zero fields take the defaults. */
+typedef struct fgb_spmm_tuning {
+  int32_t lanes;    /* 2, 4, 8, 16 or 32 */
+  int32_t reserved; /* 0 */
+  int64_t path;     /* merge-path item length */
+} fgb_spmm_tuning;
+
+/* fgb_spmm with an explicit schedule (NULL = defaults).  The result does not
+ * depend on the schedule beyond float summation order. */
+FGB_API int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                        void* C, int64_t ldc, int dtype, unsigned flags,
+                        const fgb_spmm_tuning* tune, void* stream);
 
 /* SDDMM: out[e] = A.val[e] * sum_k X[i,k] * Y[j,k] for every stored (i,j)
  * of A (out shares A's pattern).  X is m x k, Y is n x k, both row-major.
