@@ -238,7 +238,11 @@ def run_gpu(args):
     B = torch.from_numpy(B_h).to(device)
     C = torch.empty((M, NK), dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream()
-    (lanes, path), table = autotune(A, B, C, verbose=args.sweep)
+    if args.schedule:
+        lanes, path = (int(v) for v in args.schedule.split(","))
+        table = {}
+    else:
+        (lanes, path), table = autotune(A, B, C, verbose=args.sweep)
     slabs = -(-NK // (4 * lanes))
     launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
 
@@ -374,6 +378,7 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--sweep", action="store_true", help="print the autotune table to stderr")
+    ap.add_argument("--schedule", default="", help="fixed LANES,PATH instead of the autotune")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
