@@ -3,25 +3,33 @@
 // Merge-path partitioning: the walk over a CSR matrix is the merge of two
 // sorted lists -- the row ends (ptr) and the stored-entry positions -- of
 // total length nrows + nnz.  Cutting that path into equal items gives every
-// group of lanes the same amount of work whether it lands on one long row or
-// on many empty ones.  A small plan kernel finds each item's start (row,
-// entry) by binary search along its diagonal.
+// warp the same amount of work whether it lands on one long row or on many
+// empty ones.  A small plan kernel finds each item's start (row, entry) by
+// binary search along its diagonal.
 //
-// Each item is walked by a group of G lanes holding a V-wide piece of a
-// column slab [c0, c0 + G*V) of C.  Rows that end inside the item are
-// stored directly (their first portion may belong to earlier items); the
-// partial sum of the row still open at the item's end goes to a carry slot.
-// A fix-up kernel then adds every run of carries of the same row to that row
-// in item order, so results are deterministic run to run.
+// One warp walks one item at a time over a column slab [c0, c0 + 4L) of C
+// (fp32; 2L for fp64): the warp splits into P = 32/L sub-groups of L lanes,
+// every sub-group takes a different stored entry of the current row, and
+// each lane gathers its 16-byte piece of that entry's row of B.  Control
+// flow is uniform across the warp.  At a row end the P partial sums are
+// combined with xor-shuffles and L lanes store the row's slab of C.  Row ends
+// are read 32 at a time into a register window, so walking empty rows costs
+// no dependent loads.  Rows that end inside the item are stored directly
+// (their first portion may belong to earlier items); the partial sum of the
+// row still open at the item's end goes to a carry slot, and a fix-up kernel
+// adds every run of carries of one row to that row in item order -- results
+// are deterministic run to run.
 //
-// Stored entries are read in chunks of G*E with coalesced evict-first loads,
-// broadcast by shuffles, and up to BATCH gathers of B are kept in flight per
-// lane.  One launch per slab keeps the gathered slab of B L2-resident.
+// Stored entries are read 32*E at a time with coalesced evict-first loads and
+// broadcast by shuffles; up to BATCH gathers of B are in flight per lane.  The
+// grid is persistent: occupancy-many blocks per SM, items handed out by warp.
 #include "spmm_common.cuh"
 
 namespace fgb {
 
 constexpr int MP_BATCH = 8;
+constexpr int MP_THREADS = 256;
+constexpr int MP_MIN_BLOCKS = 3;  // <= 85 registers per thread: 24 warps per SM
 
 template <class PtrT>
 __global__ void merge_plan_k(int64_t nrows, int64_t nnz, const PtrT* __restrict__ ptr, int base,
@@ -43,38 +51,59 @@ __global__ void merge_plan_k(int64_t nrows, int64_t nnz, const PtrT* __restrict_
   }
 }
 
-template <class T, class VT, class PtrT, int G, int V>
-__global__ void __launch_bounds__(256) spmm_merge_k(
+// Sums the P sub-group partials (lanes congruent mod L) into every lane.
+template <class T, int V, int L>
+__device__ __forceinline__ void reduce_subgroups(VecT<T, V>& acc) {
+#pragma unroll
+  for (int m = L; m < 32; m <<= 1)
+#pragma unroll
+    for (int q = 0; q < V; ++q) acc.v[q] += __shfl_xor_sync(0xffffffffu, acc.v[q], m);
+}
+
+template <class T, class VT, class PtrT, int L, int V>
+__global__ void __launch_bounds__(MP_THREADS, MP_MIN_BLOCKS) spmm_merge_k(
     int64_t nrows, const PtrT* __restrict__ ptr, const int* __restrict__ idx,
     const VT* __restrict__ val, const T* __restrict__ B, int64_t ldb, T* __restrict__ C,
     int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, int64_t n_items,
     const int64_t* __restrict__ plan_row, const int64_t* __restrict__ plan_k,
     int64_t* __restrict__ carry_row, T* __restrict__ carry) {
-  constexpr int E = G >= MP_BATCH ? 1 : MP_BATCH / G;  // entries per lane per chunk
-  constexpr int CH = G * E;
-  const int lane = threadIdx.x & (G - 1);
-  const unsigned gmask = group_mask<G>();
-  const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
-  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
-  const int64_t col = c0 + (int64_t)lane * V;
+  constexpr int P = 32 / L;                          // entries in flight per warp step
+  constexpr int E = (MP_BATCH + L - 1) / L;          // so every sub-group gets >= BATCH
+  constexpr int CH = 32 * E;                         // entries per chunk
+  constexpr int PER_SUB = CH / P;                    // entries per sub-group per chunk
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / L, sl = lane % L;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t col = c0 + (int64_t)sl * V;
   const bool active_col = col < nk;
+  const T* Bc = B + col;
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
 
-  for (int64_t w = group; w < n_items; w += ngroups) {
+  for (int64_t w = warp; w < n_items; w += nwarps) {
     int64_t r = plan_row[w], k = plan_k[w];
     const int64_t r1 = plan_row[w + 1], k1 = plan_k[w + 1];
+    // row-end window: lane l holds the end of row rw + l
+    int64_t rw = r;
+    int64_t re = rw + lane < nrows ? ld_ptr(ptr, rw + 1 + lane) - base : INT64_MAX;
     VecT<T, V> acc;
 #pragma unroll
     for (int q = 0; q < V; ++q) acc.v[q] = T(0);
+    bool touched = false;
     while (true) {
-      const int64_t e = r < r1 ? ld_ptr(ptr, r + 1) - base : k1;
+      if (r - rw >= 32) {
+        rw = r;
+        re = rw + lane < nrows ? ld_ptr(ptr, rw + 1 + lane) - base : INT64_MAX;
+      }
+      const int64_t e = r < r1 ? __shfl_sync(0xffffffffu, re, (int)(r - rw)) : k1;
+      touched |= k < e;
       for (int64_t kb = k; kb < e; kb += CH) {
         int jj[E];
         T aa[E];
 #pragma unroll
         for (int q = 0; q < E; ++q) {
-          const int64_t p = kb + lane + q * G;
+          const int64_t p = kb + lane + 32 * q;
           jj[q] = 0;
           aa[q] = T(0);
           if (p < e) {
@@ -84,25 +113,34 @@ __global__ void __launch_bounds__(256) spmm_merge_k(
         }
         const int cnt = (e - kb) < (int64_t)CH ? (int)(e - kb) : CH;
 #pragma unroll
-        for (int t0 = 0; t0 < CH; t0 += MP_BATCH) {
-          if (t0 >= cnt) break;
+        for (int t0 = 0; t0 < PER_SUB; t0 += MP_BATCH) {
+          if (t0 * P >= cnt) break;
           VecT<T, V> b[MP_BATCH];
-          T a[MP_BATCH];
+          // issue the batch's gathers first, then consume them
 #pragma unroll
           for (int t = 0; t < MP_BATCH; ++t) {
-            const int tt = t0 + t < CH ? t0 + t : 0;
-            const int j = __shfl_sync(gmask, jj[tt / G], tt % G, G);
-            a[t] = __shfl_sync(gmask, aa[tt / G], tt % G, G);
-            if (t0 + t < cnt && active_col) b[t] = gather<T, V>(B + (int64_t)j * ldb + col, pol_keep);
+            const int tt = t0 + t;                 // step inside the chunk
+            const int q = (tt * P) / 32;           // compile-time register slot
+            const int src = (tt * P) % 32 + sub;   // lane that loaded the entry
+            const int j = __shfl_sync(0xffffffffu, jj[q < E ? q : 0], src);
+            if (tt < PER_SUB && tt * P + sub < cnt && active_col)
+              b[t] = gather<T, V>(Bc + (int64_t)j * ldb, pol_keep);
           }
 #pragma unroll
-          for (int t = 0; t < MP_BATCH; ++t)
-            if (t0 + t < cnt && active_col) acc_step<T, V>(acc, a[t], b[t], FM_DEFAULT);
+          for (int t = 0; t < MP_BATCH; ++t) {
+            const int tt = t0 + t;
+            const int q = (tt * P) / 32;
+            const int src = (tt * P) % 32 + sub;
+            const T a = __shfl_sync(0xffffffffu, aa[q < E ? q : 0], src);
+            if (tt < PER_SUB && tt * P + sub < cnt && active_col)
+              acc_step<T, V>(acc, a, b[t], FM_DEFAULT);
+          }
         }
       }
       k = e;
       if (r >= r1) break;
-      if (active_col) {
+      if (touched) reduce_subgroups<T, V, L>(acc);
+      if (sub == 0 && active_col) {
         T* dst = C + r * ldc + col;
         if (accumulate) {
           const VecT<T, V> old = load_out<T, V>(dst);
@@ -113,11 +151,13 @@ __global__ void __launch_bounds__(256) spmm_merge_k(
       }
 #pragma unroll
       for (int q = 0; q < V; ++q) acc.v[q] = T(0);
+      touched = false;
       ++r;
     }
     // the row left open at the item's end (if any) carries its partial sum
+    if (touched) reduce_subgroups<T, V, L>(acc);
     if (lane == 0 && c0 == 0) carry_row[w] = r1 < nrows ? r1 : -1;
-    if (active_col) {
+    if (sub == 0 && active_col) {
       T* cdst = carry + w * nk + col;
 #pragma unroll
       for (int q = 0; q < V; ++q) cdst[q] = acc.v[q];
@@ -148,7 +188,7 @@ size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t e
          align256(esz * n_items * nk);
 }
 
-template <class T, class VT, class PtrT, int G>
+template <class T, class VT, class PtrT, int L>
 static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                         T* C, int64_t ldc, int accumulate, int64_t path, char* scratch,
                         cudaStream_t s) {
@@ -164,10 +204,19 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
       nrows, nnz, ptr, A->index_base, path, n_items, plan_row, plan_k);
   int rc = check_launch("merge_plan_k");
   if (rc) return rc;
-  const int threads = 256;
-  const int grid = grid_for(n_items * G, threads, ctx->num_sms, 16);
-  for (int64_t c0 = 0; c0 < nk; c0 += (int64_t)G * V) {
-    spmm_merge_k<T, VT, PtrT, G, V><<<grid, threads, 0, s>>>(
+  static thread_local int occ_cache[2][6] = {};
+  int& occ = occ_cache[sizeof(T) == 8][L == 1 ? 0 : L == 2 ? 1 : L == 4 ? 2 : L == 8 ? 3 : L == 16 ? 4 : 5];
+  if (occ == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmm_merge_k<T, VT, PtrT, L, V>, MP_THREADS, 0);
+    if (occ <= 0) occ = 1;
+  }
+  const int64_t warps_needed = n_items;
+  int64_t grid = (int64_t)ctx->num_sms * occ;
+  const int64_t grid_need = (warps_needed * 32 + MP_THREADS - 1) / MP_THREADS;
+  if (grid > grid_need) grid = grid_need;
+  if (grid < 1) grid = 1;
+  for (int64_t c0 = 0; c0 < nk; c0 += (int64_t)L * V) {
+    spmm_merge_k<T, VT, PtrT, L, V><<<(int)grid, MP_THREADS, 0, s>>>(
         nrows, ptr, (const int*)A->idx, (const VT*)A->val, B, ldb, C, ldc, c0, nk, A->index_base,
         accumulate, n_items, plan_row, plan_k, carry_row, carry);
     rc = check_launch("spmm_merge_k");
