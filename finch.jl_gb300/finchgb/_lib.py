@@ -41,6 +41,17 @@ class FgbSpmmTuning(ctypes.Structure):
     _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64)]
 
 
+class FgbCgOptions(ctypes.Structure):
+    _fields_ = [("rtol", c_double), ("max_iter", c_int64), ("chunk", c_int32),
+                ("precision", c_int32), ("replace_every", c_int64)]
+
+
+class FgbCgResult(ctypes.Structure):
+    _fields_ = [("iterations", c_int64), ("replacements", c_int64),
+                ("true_rel_residual", c_double), ("seconds", c_double), ("converged", c_int32),
+                ("reserved", c_int32)]
+
+
 class FgbSparse(ctypes.Structure):
     _fields_ = [("nrows", c_int64), ("ncols", c_int64), ("nnz", c_int64), ("orient", c_int32),
                 ("index_base", c_int32), ("ptr_t", c_int32), ("idx_t", c_int32),
@@ -85,6 +96,8 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_dense_map": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_cg_solve": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p, c_void_p,
+                             POINTER(FgbCgOptions), POINTER(FgbCgResult), c_void_p]),
 }
 
 # fgb_map_op

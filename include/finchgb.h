@@ -275,6 +275,37 @@ FGB_API int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void
 FGB_API int fgb_scalar_op(fgb_ctx* ctx, int op, int dtype, const void* a, const void* b,
                           void* out, void* stream);
 
+/* ---- conjugate gradients ------------------------------------------------ */
+
+typedef struct fgb_cg_options {
+  double rtol;           /* stop when ||b - A x|| <= rtol * ||b|| (true residual) */
+  int64_t max_iter;      /* iteration cap (rounded up to whole chunks) */
+  int32_t chunk;         /* iterations per captured CUDA graph (even) */
+  int32_t precision;     /* value type of the iteration SpMV: FGB_F64, FGB_F32 or FGB_BF16 */
+  int64_t replace_every; /* FP64 residual replacement period in iterations (0 = only at the end) */
+} fgb_cg_options;
+
+typedef struct fgb_cg_result {
+  int64_t iterations;       /* iterations run */
+  int64_t replacements;     /* FP64 residual replacements done */
+  double true_rel_residual; /* ||b - A x|| / ||b|| at exit, FP64 */
+  double seconds;           /* wall time of the solve */
+  int32_t converged;
+  int32_t reserved;
+} fgb_cg_result;
+
+/* Solves A x = b for SPD CSR A; x holds the initial guess and receives the
+ * solution (device FP64 vectors).  A64 carries FP64 values (residual
+ * replacement and the FP64 mode); Alow (same pattern) carries the FP32 or
+ * BF16 values of the iteration SpMV (NULL when precision is FGB_F64).  The
+ * loop is the Finch program `@einsum q[i] += A[i,j]*p[j]`,
+ * `@einsum s[] += p[i]*q[i]` and the vector updates, with dot products and
+ * updates in FP64 and FP64 reliable updates of the residual.
+ * Synchronous with respect to `stream`. */
+FGB_API int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_sparse* Alow,
+                         const double* b, double* x, const fgb_cg_options* opt,
+                         fgb_cg_result* res, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
