@@ -367,6 +367,237 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------- the other configurations
+
+def _timed_ms(fn, reps: int = 20, warm: int = 3) -> float:
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _graph_ms(fn, reps: int = 200) -> float:
+    """Device time per call with `reps` calls captured in one CUDA graph (the
+    launch-latency-free figure for microsecond kernels)."""
+    import torch
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fn()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            for _ in range(reps):
+                fn()
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _cpu_time(fn, min_seconds: float = 2.0, max_reps: int = 1000) -> float:
+    fn()
+    t, n = 0.0, 0
+    while t < min_seconds and n < max_reps:
+        t0 = time.perf_counter()
+        fn()
+        t += time.perf_counter() - t0
+        n += 1
+    return t / n
+
+
+def _roof(nbytes: int, ms: float) -> dict:
+    peak, kind = load_peaks()
+    ach = nbytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "peak_kind": kind, "algorithmic_bytes": nbytes,
+            "ms": round(ms, 5)}
+
+
+def suite_spmv_fp64() -> list[dict]:
+    """y[i] += A[i,j]*x[j], A 10,000^2 CSC (fsprand 0.001), FP64 throughout."""
+    import torch
+
+    import oracle
+    from finchgb import _lib as L
+    from finchgb import device as dev
+    from finchgb.workloads import fsprand
+
+    rng = np.random.default_rng(SEED + 1)
+    n = 10_000
+    A = fsprand(rng, n, n, 0.001)
+    x = rng.random(n)
+    Ad = dev.DeviceSparse.from_host(n, n, A.ptr, A.idx, A.val, orient="csc")
+    Ar = Ad.transposed_storage()
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    nbytes = 12 * A.nnz + 4 * (n + 1) + 16 * n
+    out = []
+    threads = oracle.max_threads()
+    t_serial = _cpu_time(lambda: oracle.spmv_csc(0, n, n, A.ptr, A.idx, A.val, x))
+    for name, fn in (("csc_push_atomic", lambda: dev.spmv(Ad, xd, y)),
+                     ("csr_pull_finch_order", lambda: dev.spmv(Ar, xd, y, flags=L.FINCH_ORDER)),
+                     ("csr_pull", lambda: dev.spmv(Ar, xd, y))):
+        ms_launch = _timed_ms(fn, reps=200)
+        ms_graph = _graph_ms(fn)
+        out.append({"suite": "spmv_fp64_10k", "variant": name, "metric": "spmv_latency_us",
+                    "value": round(ms_graph * 1e3, 3), "unit": "us", "higher_is_better": False,
+                    "per_call_launch_us": round(ms_launch * 1e3, 3), "dtype": "f64",
+                    "config": {"workload": "fsprand 10000x10000 p=0.001 CSC, x U[0,1)",
+                               "nnz": int(A.nnz)},
+                    "roofline": _roof(nbytes, ms_graph),
+                    "cpu_baseline": {"value": round(t_serial * 1e6, 3), "unit": "us", "cores": 1,
+                                     "kind": "port",
+                                     "sample": "whole matrix, Finch's serial CSC nest (oracle)"}})
+    return out
+
+
+def suite_sddmm() -> list[dict]:
+    """out[e] = A[i,j] * <X[i,:], Y[j,:]>, A the 1M^2 power-law CSR, k = 64, FP32."""
+    import torch
+
+    import oracle
+    from finchgb import device as dev
+    from finchgb.workloads import zipf_csr
+
+    rng = np.random.default_rng(SEED)
+    m = 1_000_000
+    A = zipf_csr(rng, m, m, mean=NNZ_MEAN, a=1.5, cap=50_000, dtype=np.float32)
+    X = rng.standard_normal((m, 64), dtype=np.float32)
+    Y = rng.standard_normal((m, 64), dtype=np.float32)
+    Ad = dev.DeviceSparse.from_host(m, m, A.ptr, A.idx, A.val, orient="csr")
+    Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+    outd = torch.empty(A.nnz, dtype=torch.float32, device="cuda")
+    nbytes = 4 * (m + 1) + 8 * A.nnz + 2 * 4 * m * 64 + 4 * A.nnz
+    ms = _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd), reps=10)
+    rows = 100_000
+    p = A.ptr[: rows + 1]
+    nnz_s = int(p[-1] - 1)
+    threads = oracle.max_threads()
+    t = _cpu_time(lambda: oracle.sddmm_csr(rows, p, A.idx[:nnz_s], A.val[:nnz_s], X[:rows], Y,
+                                           nthreads=threads), min_seconds=3.0)
+    t_full = t * A.nnz / max(nnz_s, 1)
+    return [{"suite": "sddmm_1M_k64", "metric": "sddmm_gbps_algorithmic",
+             "value": round(nbytes / (ms / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "f32",
+             "ms_per_call": round(ms, 4),
+             "config": {"workload": "zipf1.5 1Mx1M nnz 16M CSR, X/Y 1Mx64 N(0,1)"},
+             "roofline": _roof(nbytes, ms),
+             "cpu_baseline": {"value": round(nbytes / t_full / 1e9, 3), "unit": "GB/s",
+                              "cores": threads, "kind": "port",
+                              "sample": f"rows 1..{rows}, time scaled by stored entries"}}]
+
+
+def suite_semiring() -> list[dict]:
+    """Bellman-Ford min-plus (Int32) and or-and reachability on a 4M-node graph."""
+    import torch
+
+    import oracle
+    from finchgb import _lib as L
+    from finchgb import device as dev
+    from finchgb.workloads import random_graph
+
+    rng = np.random.default_rng(SEED + 3)
+    n = 4_000_000
+    g = random_graph(rng, n, 8.0)
+    Ad = dev.DeviceSparse.from_host(n, n, g.ptr, g.idx, g.val, orient="csc")
+    Ap = dev.DeviceSparse(n, n, Ad.ptr, Ad.idx, None, "csc", Ad.base)
+    sentinel = 2**30
+    x0 = torch.full((n,), sentinel, dtype=torch.int32, device="cuda")
+    x0[0] = 0
+
+    def rounds(nr=20):
+        x = x0.clone()
+        y = torch.empty_like(x)
+        for _ in range(nr):
+            dev.spmv(Ad, x, y, semiring=L.MIN_PLUS)
+            dev.dense_map(L.MAP_MIN, x, y, x)
+        return x
+
+    ms20 = _timed_ms(lambda: rounds(20), reps=3, warm=1)
+    per_round_bytes = 8 * g.nnz + 4 * (n + 1) + 3 * 4 * n + 2 * 4 * n
+    f0 = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    f0[0] = 1
+    yb = torch.empty_like(f0)
+    ms_or = _timed_ms(lambda: dev.spmv(Ap, f0, yb, semiring=L.OR_AND), reps=20)
+    or_bytes = 4 * g.nnz + 4 * (n + 1) + 2 * n
+    threads = oracle.max_threads()
+    xh = np.full(n, sentinel, dtype=np.int32)
+    xh[0] = 0
+    t_round = _cpu_time(lambda: oracle.spmv_csc(oracle.SR_MINP, n, n, g.ptr, g.idx, g.val, xh),
+                        min_seconds=3.0, max_reps=5)
+    return [{"suite": "bellman_ford_minplus_4M", "metric": "minplus_round_gbps",
+             "value": round(20 * per_round_bytes / (ms20 / 1e3) / 1e9, 1), "unit": "GB/s",
+             "dtype": "i32", "ms_per_20_rounds": round(ms20, 3),
+             "config": {"workload": "4M nodes, Poisson(8) out-degree, Int32 weights U{1..1000}",
+                        "nnz": int(g.nnz)},
+             "roofline": _roof(20 * per_round_bytes, ms20),
+             "cpu_baseline": {"value": round(per_round_bytes / t_round / 1e9, 3), "unit": "GB/s",
+                              "cores": 1, "kind": "port",
+                              "sample": "one round: Finch's serial CSC min-plus nest (oracle)"}},
+            {"suite": "reachability_or_and_4M", "metric": "or_and_spmv_gbps",
+             "value": round(or_bytes / (ms_or / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "bool",
+             "ms_per_call": round(ms_or, 4), "config": {"workload": "same graph, Pattern level"},
+             "roofline": _roof(or_bytes, ms_or)}]
+
+
+def suite_cg() -> list[dict]:
+    """CG on the 2048^2 5-point Poisson matrix: FP64, FP32 and BF16 SpMV."""
+    import torch
+
+    from finchgb import cg
+    from finchgb import device as dev
+    from finchgb.workloads import poisson2d
+
+    A = poisson2d(2048)
+    rng = np.random.default_rng(SEED + 4)
+    b = rng.uniform(-1, 1, A.nrows)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    out = []
+    for prec in ("f64", "f32", "bf16"):
+        x, res = cg.cg_solve(Ad, bd, precision=prec, rtol=1e-10, max_iter=60_000, chunk=64,
+                             replace_every=1024)
+        torch.cuda.synchronize()
+        vb = {"f64": 8, "f32": 4, "bf16": 2}[prec]
+        # SpMV: ptr, idx, values, p, q; updates: x rw, r rw, p, q; p update: r, p rw
+        per_it = A.nnz * (4 + vb) + 4 * (A.nrows + 1) + 8 * A.nrows * 11
+        out.append({"suite": "cg_poisson2048", "variant": prec, "metric": "cg_seconds",
+                    "value": round(res.seconds, 4), "unit": "s", "higher_is_better": False,
+                    "iterations": res.iterations, "replacements": res.replacements,
+                    "true_rel_residual": res.true_rel_residual, "converged": res.converged,
+                    "ms_per_iteration": round(1e3 * res.seconds / max(res.iterations, 1), 4),
+                    "roofline": _roof(per_it, 1e3 * res.seconds / max(res.iterations, 1))})
+    return out
+
+
+def run_suite(args):
+    from finchgb import build
+
+    build.build()
+    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm):
+        if args.suite_only and fn.__name__ not in args.suite_only.split(","):
+            continue
+        try:
+            for line in fn():
+                print(json.dumps(line), flush=True)
+        except Exception as e:  # report and continue with the next configuration
+            print(json.dumps({"suite": fn.__name__, "error": repr(e)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -379,8 +610,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--sweep", action="store_true", help="print the autotune table to stderr")
     ap.add_argument("--schedule", default="", help="fixed LANES,PATH instead of the autotune")
+    ap.add_argument("--suite", action="store_true",
+                    help="measure the other configurations (one JSON line each) instead")
+    ap.add_argument("--suite-only", default="", help="comma-separated suite function names")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.suite:
+        run_suite(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
