@@ -7,6 +7,10 @@
 
 namespace fgb {
 
+// fgb_spmm's dispatcher (spmm.cu); lanes/path 0 = defaults.
+int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
+              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream);
+
 // Merge-path SpMM (spmm_merge.cu).
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,

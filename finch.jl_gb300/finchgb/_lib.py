@@ -82,6 +82,8 @@ SIGNATURES: dict[str, tuple] = {
                          c_int64, c_int, c_uint, c_void_p]),
     "fgb_spmm_ex": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,
                             c_int64, c_int, c_uint, POINTER(FgbSpmmTuning), c_void_p]),
+    "fgb_spmm_noalloc": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64,
+                                 c_void_p, c_int64, c_int, c_uint, c_void_p]),
     "fgb_sddmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
                           c_int64, c_void_p, c_int, c_uint, c_void_p]),
     "fgb_ewise_count": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,

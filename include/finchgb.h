@@ -207,6 +207,27 @@ FGB_API int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_
                         void* C, int64_t ldc, int dtype, unsigned flags,
                         const fgb_spmm_tuning* tune, void* stream);
 
+/* Size of the fixed device scratch array behind fgb_spmm_noalloc (16 MiB). */
+#define FGB_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* fgb_spmm without any memory allocation.  No counterpart in the reference:
+ * Finch's CPU kernels allocate nothing on a device, so this exists only for
+ * callers of the GPU library that must not allocate device memory -- e.g. a
+ * host whose device memory belongs to another pool (CUDA.jl), or a serving
+ * loop that cannot afford an allocator call in its latency budget.  Same
+ * arguments and results as fgb_spmm; the scratch of the load-balanced
+ * schedule comes from one fixed array of FGB_NOALLOC_SCRATCH_BYTES per
+ * device, held from first use until the process exits.  The schedule
+ * lengthens its merge-path items until its scratch fits; a matrix whose
+ * scratch exceeds the array even at the longest items (2^24 steps) is
+ * rejected with FGB_EINVAL before any device work.  The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress) with that device
+ * current, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+FGB_API int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb,
+                             int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags,
+                             void* stream);
+
 /* SDDMM: out[e] = A.val[e] * sum_k X[i,k] * Y[j,k] for every stored (i,j)
  * of A (out shares A's pattern).  X is m x k, Y is n x k, both row-major.
  * F32 or F64.  Replaces compute(lazy(A) .* (lazy(X) * lazy(Y^T)))
