@@ -10,8 +10,9 @@
 // products and the updates are FP64.  Accuracy is won back by reliable
 // updates: every `replace_every` iterations, and whenever the recursive
 // residual reaches the tolerance, the true residual r = b - A x is recomputed
-// with the FP64 matrix, replaces the recursive one, and the solve stops only
-// when that true residual is below rtol * ||b||.
+// with the FP64 matrix, replaces the recursive one (the search direction
+// restarts from it), and the solve stops only when that true residual is
+// below rtol * ||b||.
 //
 // One iteration is three kernels -- SpMV fused with the p.q partials; the
 // x/r update (every block folds the p.q partials itself) fused with the r.r
@@ -96,7 +97,8 @@ __global__ void __launch_bounds__(CG_THREADS) cg_update_xr(
     const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
   __shared__ double sh[33];
   const double pq = fold_parts(part_pq, nparts, sh);
-  const double alpha = rr[slot] / pq;
+  // a vanished curvature (p.q == 0) only happens once r is exactly zero
+  const double alpha = pq != 0.0 ? rr[slot] / pq : 0.0;
   double acc = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_update_p(
     int slot_out, double* __restrict__ hist, int64_t it) {
   __shared__ double sh[33];
   const double rr_new = fold_parts(part_rr, nparts, sh);
-  const double beta = rr_new / rr[slot_in];
+  const double beta = rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     p[i] = __fma_rn(beta, p[i], r[i]);
@@ -307,10 +309,13 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
       const bool broken = !(hist[chunk - 1] == hist[chunk - 1]);  // NaN: breakdown
       if (broken) { rc = set_error(FGB_EINVAL, "fgb_cg_solve: breakdown (NaN residual) after %lld iterations", (long long)it); break; }
       if (small || (replace_every && since_replace >= replace_every)) {
-        // reliable update: r = b - A x in FP64, rr[0] = r.r (slot 0 starts the next chunk)
+        // reliable update: r = b - A x in FP64, rr[0] = r.r (slot 0 starts the
+        // next chunk), and the direction restarts from the true residual, so
+        // the drift the low-precision products left in p is dropped as well.
         if (i32) launch_residual<int32_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
         else launch_residual<int64_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
         cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
+        cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p);
         double rr_true = 0;
         if ((e = cudaMemcpyAsync(&rr_true, bufs.rr, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess) { fail(FGB_ECUDA, "replacement sync", e); break; }
