@@ -10,9 +10,9 @@
 // products and the updates are FP64.  Accuracy is won back by reliable
 // updates: every `replace_every` iterations, and whenever the recursive
 // residual reaches the tolerance, the true residual r = b - A x is recomputed
-// with the FP64 matrix, replaces the recursive one (the search direction
-// restarts from it), and the solve stops only when that true residual is
-// below rtol * ||b||.
+// with the FP64 matrix and replaces the recursive one (residual replacement
+// keeping the search direction), and the solve stops only when that true
+// residual is below rtol * ||b||.
 //
 // One iteration is three kernels -- SpMV fused with the p.q partials; the
 // x/r update (every block folds the p.q partials itself) fused with the r.r
@@ -309,13 +309,13 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
       const bool broken = !(hist[chunk - 1] == hist[chunk - 1]);  // NaN: breakdown
       if (broken) { rc = set_error(FGB_EINVAL, "fgb_cg_solve: breakdown (NaN residual) after %lld iterations", (long long)it); break; }
       if (small || (replace_every && since_replace >= replace_every)) {
-        // reliable update: r = b - A x in FP64, rr[0] = r.r (slot 0 starts the
-        // next chunk), and the direction restarts from the true residual, so
-        // the drift the low-precision products left in p is dropped as well.
+        // reliable update: r = b - A x in FP64 and rr[0] = r.r (slot 0 starts
+        // the next chunk); the search direction is kept.  If p has vanished
+        // (the recursive residual reached zero), p.q = 0 gives alpha = 0 and
+        // the next update rebuilds p from the replaced residual.
         if (i32) launch_residual<int32_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
         else launch_residual<int64_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
         cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
-        cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p);
         double rr_true = 0;
         if ((e = cudaMemcpyAsync(&rr_true, bufs.rr, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess) { fail(FGB_ECUDA, "replacement sync", e); break; }
