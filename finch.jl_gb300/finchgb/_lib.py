@@ -52,6 +52,22 @@ class FgbCgResult(ctypes.Structure):
                 ("reserved", c_int32)]
 
 
+class FgbServerConfig(ctypes.Structure):
+    _fields_ = [("pool_bytes", c_size_t), ("max_inflight", c_int32), ("rows_per_item", c_int32),
+                ("blocks_per_sm", c_int32), ("idle_exit_us", c_int32), ("mode", c_int32),
+                ("reserved", c_int32)]
+
+
+class FgbRequest(ctypes.Structure):
+    _fields_ = [("op", c_int32), ("matrix", c_int32), ("matrix_b", c_int32), ("nk", c_int32),
+                ("input", c_void_p), ("output", c_void_p)]
+
+
+class FgbServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("launches", c_uint64),
+                ("batches_published", c_uint64), ("pool_used", c_uint64)]
+
+
 class FgbSparse(ctypes.Structure):
     _fields_ = [("nrows", c_int64), ("ncols", c_int64), ("nnz", c_int64), ("orient", c_int32),
                 ("index_base", c_int32), ("ptr_t", c_int32), ("idx_t", c_int32),
@@ -100,7 +116,19 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fgb_cg_solve": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p, c_void_p,
                              POINTER(FgbCgOptions), POINTER(FgbCgResult), c_void_p]),
+    "fgb_random_csr": (c_int, [c_void_p, c_uint64, c_int64, c_int64, c_double, c_int, c_void_p,
+                               c_void_p, c_void_p, POINTER(c_int64), c_void_p]),
+    "fgb_server_create": (c_int, [c_void_p, POINTER(FgbServerConfig), POINTER(c_void_p)]),
+    "fgb_server_register": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(c_int32)]),
+    "fgb_server_submit": (c_int, [c_void_p, POINTER(FgbRequest), POINTER(c_uint64)]),
+    "fgb_server_wait": (c_int, [c_void_p, c_uint64, c_int32, POINTER(c_double)]),
+    "fgb_server_stats_get": (c_int, [c_void_p, POINTER(FgbServerStats)]),
+    "fgb_server_destroy": (c_int, [c_void_p]),
 }
+
+# fgb_request_op / fgb_serve_mode
+REQ_SPMV, REQ_SPMM, REQ_MASKED_MUL = 0, 1, 2
+SERVE_BATCHED, SERVE_PER_CALL = 0, 1
 
 # fgb_map_op
 MAP_ADD, MAP_SUB, MAP_MUL, MAP_DIV, MAP_MIN, MAP_MAX = range(6)

@@ -296,6 +296,72 @@ FGB_API int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void
 FGB_API int fgb_scalar_op(fgb_ctx* ctx, int op, int dtype, const void* a, const void* b,
                           void* out, void* stream);
 
+/* ---- seeded inputs ------------------------------------------------------ */
+
+/* Random m x n CSR on the device with fsprand's distribution
+ * (src/interface/fsparse.jl:173-290): each (i,j) stored independently with
+ * probability p; values N(0,1) (F32) or U[0,1) (F64).  Pass 1 (idx == NULL)
+ * writes ptr (int32, 0-based, m+1) and *nnz (synchronous); pass 2 fills idx
+ * (int32, ascending per row) and val.  Depends only on (seed, m, n, p). */
+FGB_API int fgb_random_csr(fgb_ctx* ctx, uint64_t seed, int64_t m, int64_t n, double p, int val_t,
+                           int32_t* ptr, int32_t* idx, void* val, int64_t* nnz, void* stream);
+
+/* ---- serving: continuous batching of many small requests ------------- */
+
+typedef struct fgb_server fgb_server;
+
+typedef enum {
+  FGB_REQ_SPMV = 0,      /* y = A x                      (x: ncols, y: nrows)   */
+  FGB_REQ_SPMM = 1,      /* C = A B, B ncols x nk        (nk % 4 == 0, <= 128) */
+  FGB_REQ_MASKED_MUL = 2 /* A .* B2 on A's pattern       (out: nnz of A)       */
+} fgb_request_op;
+
+typedef enum {
+  FGB_SERVE_BATCHED = 0, /* persistent device loop, continuous batching */
+  FGB_SERVE_PER_CALL = 1 /* one launch + copies + sync per request      */
+} fgb_serve_mode;
+
+typedef struct fgb_server_config {
+  size_t pool_bytes;     /* HBM budget for in-flight inputs/outputs (admission) */
+  int32_t max_inflight;  /* request slots, <= 4096 */
+  int32_t rows_per_item; /* rows per work item (default 64) */
+  int32_t blocks_per_sm; /* persistent blocks per SM (default 4) */
+  int32_t idle_exit_us;  /* device loop exits after this long without work (default 20000) */
+  int32_t mode;          /* fgb_serve_mode */
+  int32_t reserved;
+} fgb_server_config;
+
+typedef struct fgb_request {
+  int32_t op;         /* fgb_request_op */
+  int32_t matrix;     /* id from fgb_server_register */
+  int32_t matrix_b;   /* second operand of FGB_REQ_MASKED_MUL */
+  int32_t nk;         /* SpMM width */
+  const void* input;  /* host FP32 x or row-major B (NULL for MASKED_MUL) */
+  void* output;       /* host FP32 result, written before fgb_server_wait returns */
+} fgb_request;
+
+typedef struct fgb_server_stats {
+  uint64_t submitted, completed, launches, batches_published, pool_used;
+} fgb_server_stats;
+
+/* Serving front end for compute() calls on resident tensors.  Admission is by
+ * HBM footprint (a request waits until its input and output fit in the pool
+ * and a slot is free); admitted requests are published to a device-side loop
+ * that overlaps their work; results are identical to running each request
+ * alone.  Every device wait is bounded (idle_exit_us). */
+FGB_API int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg, fgb_server** out);
+/* Registers a resident CSR matrix (device buffers, int32 ptr/idx, F32 values). */
+FGB_API int fgb_server_register(fgb_server* srv, const fgb_sparse* A, int32_t* id);
+/* Queues a request; returns at once with a ticket. */
+FGB_API int fgb_server_submit(fgb_server* srv, const fgb_request* req, uint64_t* ticket);
+/* Waits up to timeout_ms for a ticket (FGB_ETIMEOUT after that); on success
+ * the output is in host memory and *latency_s is submit-to-result time. */
+FGB_API int fgb_server_wait(fgb_server* srv, uint64_t ticket, int32_t timeout_ms,
+                            double* latency_s);
+FGB_API int fgb_server_stats_get(fgb_server* srv, fgb_server_stats* out);
+/* Stops the device loop (bounded) and frees everything. */
+FGB_API int fgb_server_destroy(fgb_server* srv);
+
 /* ---- conjugate gradients ------------------------------------------------ */
 
 typedef struct fgb_cg_options {
