@@ -624,8 +624,9 @@ int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
   if (r->matrix < 0 || r->matrix >= (int)s->mats.size())
     return set_error(FGB_EINVAL, "fgb_server_submit: unknown matrix %d", r->matrix);
   const DevMatrix& A = s->mats[r->matrix];
-  if (r->op == FGB_REQ_SPMM && (r->nk <= 0 || r->nk > 128 || (r->nk & 3)))
-    return set_error(FGB_EUNSUPPORTED, "fgb_server_submit: SpMM width must be a multiple of 4 up to 128");
+  // SpMM rows are split into nk/4 lanes per entry: nk/4 must be a power of two
+  if (r->op == FGB_REQ_SPMM && (r->nk < 4 || r->nk > 128 || (r->nk & 3) || ((r->nk >> 2) & ((r->nk >> 2) - 1))))
+    return set_error(FGB_EUNSUPPORTED, "fgb_server_submit: SpMM width must be 4, 8, 16, 32, 64 or 128");
   if (r->op == FGB_REQ_MASKED_MUL) {
     if (r->matrix_b < 0 || r->matrix_b >= (int)s->mats.size())
       return set_error(FGB_EINVAL, "fgb_server_submit: unknown matrix_b %d", r->matrix_b);

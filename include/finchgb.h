@@ -312,7 +312,7 @@ typedef struct fgb_server fgb_server;
 
 typedef enum {
   FGB_REQ_SPMV = 0,      /* y = A x                      (x: ncols, y: nrows)   */
-  FGB_REQ_SPMM = 1,      /* C = A B, B ncols x nk        (nk % 4 == 0, <= 128) */
+  FGB_REQ_SPMM = 1,      /* C = A B, B ncols x nk        (nk = 4, 8, ..., 128) */
   FGB_REQ_MASKED_MUL = 2 /* A .* B2 on A's pattern       (out: nnz of A)       */
 } fgb_request_op;
 
