@@ -584,6 +584,102 @@ def suite_cg() -> list[dict]:
     return out
 
 
+def serve_library(n_mats: int = 4096, n_partners: int = 512):
+    """4,096 resident CSR matrices, rows log-uniform in [64, 8192], square,
+    density U[0.5%, 5%], FP32 N(0,1), generated on the device; the first
+    n_partners also get a same-shape partner for masked multiplies."""
+    from finchgb.server import random_csr
+
+    rng = np.random.default_rng(SEED + 5)
+    ns = np.exp(rng.uniform(np.log(64), np.log(8192), n_mats)).astype(int)
+    ps = rng.uniform(0.005, 0.05, n_mats)
+    mats = [random_csr(SEED + 10 * k, int(n), int(n), float(p)) for k, (n, p) in enumerate(zip(ns, ps))]
+    partners = [random_csr(SEED + 10 * k + 7, int(ns[k]), int(ns[k]), float(ps[k]))
+                for k in range(n_partners)]
+    return mats, partners
+
+
+def serve_run(mode, mats, partners, plan, arena, window, arrivals=None):
+    """Runs the request plan through a server; returns (seconds, latencies)."""
+    import torch
+
+    from finchgb.server import Server
+
+    slice_floats = arena.numel() // window
+    lat = []
+    with Server(mode=mode, pool_bytes=4 << 30, max_inflight=min(window, 4096)) as srv:
+        ids = [srv.register(A) for A in mats]
+        pids = [srv.register(B) for B in partners]
+        tickets = []
+        t0 = time.perf_counter()
+        for i, (op, k, nk) in enumerate(plan):
+            if i >= window:
+                lat.append(srv.wait(tickets[i - window]))
+            if arrivals is not None:
+                while time.perf_counter() - t0 < arrivals[i]:
+                    pass
+            A = mats[k]
+            base = (i % window) * slice_floats
+            if op == "spmv":
+                inp = arena[base: base + A.ncols]
+                out = arena[base + A.ncols: base + A.ncols + A.nrows]
+                tickets.append(srv.submit(op, ids[k], inp, out))
+            elif op == "spmm":
+                inp = arena[base: base + A.ncols * nk]
+                out = arena[base + A.ncols * nk: base + (A.ncols + A.nrows) * nk]
+                tickets.append(srv.submit(op, ids[k], inp, out, nk=nk))
+            else:
+                out = arena[base: base + A.nnz]
+                tickets.append(srv.submit(op, ids[k], None, out, matrix_b=pids[k]))
+        for t in tickets[max(0, len(plan) - window):]:
+            lat.append(srv.wait(t))
+        dt = time.perf_counter() - t0
+        st = srv.stats()
+    return dt, np.array(lat), st
+
+
+def run_serve(args):
+    """Config 5: batched/served requests vs the plain per-call GPU path."""
+    import torch
+
+    from finchgb import build
+
+    build.build()
+    mats, partners = serve_library()
+    rng = np.random.default_rng(SEED + 6)
+    n_req = args.requests
+    plan = []
+    for _ in range(n_req):
+        op = ("spmv", "spmm", "masked_mul")[int(rng.integers(3))]
+        k = int(rng.integers(len(partners) if op == "masked_mul" else len(mats)))
+        plan.append((op, k, 32 if op == "spmm" else 0))
+    window = 1024
+    max_floats = max((A.ncols + A.nrows) * 32 for A in mats)
+    arena = torch.empty(window * max_floats, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    out = {"suite": "served_4096_csr", "requests": n_req, "mix": "1/3 SpMV, 1/3 SpMM(32), 1/3 masked multiply",
+           "matrices": len(mats), "stored_entries": int(sum(A.nnz for A in mats)),
+           "config": {"workload": "4096 CSR, rows log-uniform [64, 8192], density U[0.5%, 5%], FP32"}}
+    # closed loop (saturation): up to `window` requests in flight
+    for mode in ("batched", "per_call"):
+        dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
+        out[mode] = {"ops_per_s": round(n_req / dt, 1), "seconds": round(dt, 3),
+                     "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                     "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
+                     "launches": st["launches"], "batches": st["batches_published"]}
+    out["throughput_ratio_batched_vs_per_call"] = round(
+        out["batched"]["ops_per_s"] / out["per_call"]["ops_per_s"], 2)
+    # open loop: Poisson arrivals at half of each mode's capacity
+    for mode in ("batched", "per_call"):
+        lam = 0.5 * out[mode]["ops_per_s"]
+        arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
+        dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr)
+        out[mode]["poisson_rate_per_s"] = round(lam, 1)
+        out[mode]["poisson_p50_ms"] = round(1e3 * float(np.percentile(lat, 50)), 3)
+        out[mode]["poisson_p99_ms"] = round(1e3 * float(np.percentile(lat, 99)), 3)
+    print(json.dumps(out), flush=True)
+
+
 def run_suite(args):
     from finchgb import build
 
@@ -613,8 +709,12 @@ def main():
     ap.add_argument("--suite", action="store_true",
                     help="measure the other configurations (one JSON line each) instead")
     ap.add_argument("--suite-only", default="", help="comma-separated suite function names")
+    ap.add_argument("--serve", action="store_true", help="the batched/served configuration")
+    ap.add_argument("--requests", type=int, default=20000)
     args = ap.parse_args()
-    if args.suite:
+    if args.serve:
+        run_serve(args)
+    elif args.suite:
         run_suite(args)
     elif args.impl == "reference":
         run_reference(args)

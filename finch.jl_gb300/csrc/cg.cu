@@ -321,6 +321,12 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
             (e = cudaStreamSynchronize(s)) != cudaSuccess) { fail(FGB_ECUDA, "replacement sync", e); break; }
         res->replacements++;
         since_replace = 0;
+        // When the recursive residual has drifted far below the true one, the
+        // kept direction no longer matches r: restart it from the replaced r.
+        if (hist[chunk - 1] < 1e-6 * rr_true) {
+          cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p);
+          if ((e = cudaGetLastError()) != cudaSuccess) { fail(FGB_ECUDA, "restart", e); break; }
+        }
         res->true_rel_residual = sqrt(rr_true) / (bnorm > 0 ? bnorm : 1.0);
         if (sqrt(rr_true) <= target) {
           res->converged = 1;

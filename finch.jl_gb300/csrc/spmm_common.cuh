@@ -13,9 +13,12 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
 
 // Merge-path SpMM (spmm_merge.cu).
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
+// plan_ready: the item boundaries in `scratch` are already those of (A, path)
+// (computed by an earlier call on the same scratch), so only the slab kernels
+// and the fix-up run.
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
-               size_t scratch_bytes, cudaStream_t s);
+               size_t scratch_bytes, cudaStream_t s, bool plan_ready = false);
 
 template <class T, int V>
 struct VecT {

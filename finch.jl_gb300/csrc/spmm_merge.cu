@@ -191,7 +191,7 @@ size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t e
 template <class T, class VT, class PtrT, int L>
 static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                         T* C, int64_t ldc, int accumulate, int64_t path, char* scratch,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool plan_ready) {
   constexpr int V = sizeof(T) == 4 ? 4 : 2;
   const int64_t nrows = A->nrows, nnz = A->nnz;
   const int64_t n_items = (nrows + nnz + path - 1) / path;
@@ -200,10 +200,13 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
   int64_t* carry_row = (int64_t*)((char*)plan_k + align256(sizeof(int64_t) * (n_items + 1)));
   T* carry = (T*)((char*)carry_row + align256(sizeof(int64_t) * n_items));
   const PtrT* ptr = (const PtrT*)A->ptr;
-  merge_plan_k<PtrT><<<grid_for(n_items + 1, 256, ctx->num_sms, 4), 256, 0, s>>>(
-      nrows, nnz, ptr, A->index_base, path, n_items, plan_row, plan_k);
-  int rc = check_launch("merge_plan_k");
-  if (rc) return rc;
+  int rc = FGB_OK;
+  if (!plan_ready) {
+    merge_plan_k<PtrT><<<grid_for(n_items + 1, 256, ctx->num_sms, 4), 256, 0, s>>>(
+        nrows, nnz, ptr, A->index_base, path, n_items, plan_row, plan_k);
+    rc = check_launch("merge_plan_k");
+    if (rc) return rc;
+  }
   static thread_local int occ_cache[2][6] = {};
   int& occ = occ_cache[sizeof(T) == 8][L == 1 ? 0 : L == 2 ? 1 : L == 4 ? 2 : L == 8 ? 3 : L == 16 ? 4 : 5];
   if (occ == 0) {
@@ -230,13 +233,13 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
 template <class T, class VT, class PtrT>
 static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                        T* C, int64_t ldc, int accumulate, int lanes, int64_t path, char* scratch,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool plan_ready) {
   switch (lanes) {
-    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s);
-    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s);
-    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s);
-    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s);
-    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s);
+    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
+    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
+    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
+    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
+    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
   }
 }
 
@@ -244,7 +247,7 @@ static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ld
 // the vector width).  scratch == NULL allocates it on the stream.
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
-               size_t scratch_bytes, cudaStream_t s) {
+               size_t scratch_bytes, cudaStream_t s, bool plan_ready) {
   const size_t esz = dtype == FGB_F64 ? 8 : 4;
   const size_t need = spmm_merge_scratch_bytes(A->nrows, A->nnz, nk, esz, path);
   char* buf = (char*)scratch;
@@ -254,14 +257,14 @@ int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, in
   int rc;
   const bool i32 = A->ptr_t == FGB_I32;
   if (dtype == FGB_F64)
-    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s)
-             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s);
+    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
+             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
   else if (A->val_t == FGB_BF16)
-    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s)
-             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s);
+    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
+             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
   else
-    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s)
-             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s);
+    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
+             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
   if (!scratch) cudaFreeAsync(buf, s);
   return rc;
 }

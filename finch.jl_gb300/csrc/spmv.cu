@@ -78,6 +78,10 @@ __global__ void fill_identity(A* __restrict__ y, int64_t n) {
     y[i] = Semi<SR, A>::identity();
 }
 
+// Lanes per fiber chosen by the plan autotuner for the calls it times and
+// captures (0 = the heuristic below); set only around those calls.
+static thread_local int t_group_override = 0;
+
 static int pick_group(double avg) {
   if (avg <= 2.0) return 1;
   if (avg <= 8.0) return 4;
@@ -100,7 +104,7 @@ static int launch_typed(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void*
     int fm = FM_DEFAULT;
     if (flags & FGB_NO_FMA) fm = FM_NOFMA;
     if (flags & FGB_FMA) fm = FM_FMA;
-    int G = (flags & FGB_FINCH_ORDER) ? 1 : pick_group(avg);
+    int G = (flags & FGB_FINCH_ORDER) ? 1 : (t_group_override > 0 ? t_group_override : pick_group(avg));
     int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
     if (nf == 0) return FGB_OK;
 #define FGB_PULL(GG)                                                                    \
@@ -123,7 +127,8 @@ static int launch_typed(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void*
     if (rc) return rc;
   }
   if (nf == 0) return FGB_OK;
-  int G = avg <= 4.0 ? 1 : (avg <= 16.0 ? 8 : 32);
+  int G = t_group_override > 0 ? (t_group_override <= 1 ? 1 : t_group_override <= 8 ? 8 : 32)
+                               : (avg <= 4.0 ? 1 : (avg <= 16.0 ? 8 : 32));
   int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
 #define FGB_PUSH(GG)                                                                    \
   spmv_csc_push<SR, VT, A, PtrT, GG, PATTERN><<<grid, threads, 0, s>>>(nf, ptr, idx, val, \
@@ -202,3 +207,14 @@ extern "C" int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const v
     default: return set_error(FGB_EINVAL, "fgb_spmv: unknown semiring %d", semiring);
   }
 }
+
+namespace fgb {
+// fgb_spmv with the lanes per fiber fixed to `group` (1, 4, 8 or 32).
+int spmv_with_group(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* x, int x_t,
+                    void* y, int y_t, unsigned flags, int group, void* stream) {
+  t_group_override = group;
+  const int rc = fgb_spmv(ctx, semiring, A, x, x_t, y, y_t, flags, stream);
+  t_group_override = 0;
+  return rc;
+}
+}  // namespace fgb

@@ -52,6 +52,18 @@ class FgbCgResult(ctypes.Structure):
                 ("reserved", c_int32)]
 
 
+class FgbPlanDesc(ctypes.Structure):
+    _fields_ = [("op", c_int32), ("semiring", c_int32), ("dtype", c_int32), ("flags", c_uint),
+                ("A", c_void_p), ("in0", c_void_p), ("in1", c_void_p), ("out", c_void_p),
+                ("ld_in0", c_int64), ("ld_in1", c_int64), ("ld_out", c_int64), ("k", c_int64)]
+
+
+class FgbPlanInfo(ctypes.Structure):
+    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64),
+                ("tuned_ms", c_double), ("first_candidate_ms", c_double),
+                ("candidates", c_int32), ("from_cache", c_int32)]
+
+
 class FgbServerConfig(ctypes.Structure):
     _fields_ = [("pool_bytes", c_size_t), ("max_inflight", c_int32), ("rows_per_item", c_int32),
                 ("blocks_per_sm", c_int32), ("idle_exit_us", c_int32), ("mode", c_int32),
@@ -116,6 +128,10 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fgb_cg_solve": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p, c_void_p,
                              POINTER(FgbCgOptions), POINTER(FgbCgResult), c_void_p]),
+    "fgb_plan_create": (c_int, [c_void_p, POINTER(FgbPlanDesc), c_int32, POINTER(c_void_p)]),
+    "fgb_plan_execute": (c_int, [c_void_p, c_void_p]),
+    "fgb_plan_info_get": (c_int, [c_void_p, POINTER(FgbPlanInfo)]),
+    "fgb_plan_destroy": (c_int, [c_void_p]),
     "fgb_random_csr": (c_int, [c_void_p, c_uint64, c_int64, c_int64, c_double, c_int, c_void_p,
                                c_void_p, c_void_p, POINTER(c_int64), c_void_p]),
     "fgb_server_create": (c_int, [c_void_p, POINTER(FgbServerConfig), POINTER(c_void_p)]),

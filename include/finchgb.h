@@ -296,6 +296,51 @@ FGB_API int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void
 FGB_API int fgb_scalar_op(fgb_ctx* ctx, int op, int dtype, const void* a, const void* b,
                           void* out, void* stream);
 
+/* ---- plans: autotuned, graph-captured operations ------------------------ */
+
+typedef struct fgb_plan fgb_plan;
+
+typedef enum { FGB_PLAN_SPMV = 0, FGB_PLAN_SPMM = 1, FGB_PLAN_SDDMM = 2 } fgb_plan_op;
+
+/* One operation on fixed device operands:
+ *   SPMV:  out = A (*) in0 over `semiring`      (dtype of in0/out)
+ *   SPMM:  out = A @ in0, in0 n x k (ld_in0), out m x k (ld_out)
+ *   SDDMM: out = A .* (in0 @ in1^T), in0 m x k (ld_in0), in1 n x k (ld_in1) */
+typedef struct fgb_plan_desc {
+  int32_t op;
+  int32_t semiring;
+  int32_t dtype;
+  uint32_t flags;
+  const fgb_sparse* A;
+  const void* in0;
+  const void* in1;
+  void* out;
+  int64_t ld_in0, ld_in1, ld_out;
+  int64_t k;
+} fgb_plan_desc;
+
+typedef struct fgb_plan_info {
+  int32_t lanes;             /* chosen lanes per fiber / row group / entry */
+  int32_t reserved;
+  int64_t path;              /* chosen merge-path item (SpMM) or entry chunk (SDDMM) */
+  double tuned_ms;           /* time of the chosen schedule (-1 if not tuned) */
+  double first_candidate_ms; /* time of the first schedule tried */
+  int32_t candidates;        /* schedules in the search space */
+  int32_t from_cache;        /* 1 if the choice came from the tuning cache */
+} fgb_plan_info;
+
+/* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use
+ * the first schedule), precomputes what depends only on A, and captures the
+ * chosen launches into a CUDA graph bound to these operand pointers.  The
+ * choice is cached per shape class (and appended to the file named by
+ * FGB_TUNE_CACHE).  Writes `out` while tuning.  Synchronous. */
+FGB_API int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps,
+                            fgb_plan** out);
+/* Replays the captured operation on `stream`. */
+FGB_API int fgb_plan_execute(fgb_plan* plan, void* stream);
+FGB_API int fgb_plan_info_get(fgb_plan* plan, fgb_plan_info* out);
+FGB_API int fgb_plan_destroy(fgb_plan* plan);
+
 /* ---- seeded inputs ------------------------------------------------------ */
 
 /* Random m x n CSR on the device with fsprand's distribution

@@ -37,7 +37,7 @@ def make_requests(rng, mats, partners, count):
             reqs.append((op, k, inp, out, -1, 32))
         else:
             out = torch.empty(A.nnz, dtype=torch.float32).pin_memory()
-            reqs.append((op, k, None, out, partners[k], 0))
+            reqs.append((op, k, None, out, 1, 0))  # 1: use the partner of matrix k
     return reqs
 
 
