@@ -15,10 +15,12 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
 // plan_ready: the item boundaries in `scratch` are already those of (A, path)
 // (computed by an earlier call on the same scratch), so only the slab kernels
-// and the fix-up run.
+// and the fix-up run.  row_map (optional): row r of A is row row_map[r] of C
+// (A lists only some rows of the product, e.g. one column panel's rows).
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
-               size_t scratch_bytes, cudaStream_t s, bool plan_ready = false);
+               size_t scratch_bytes, cudaStream_t s, bool plan_ready = false,
+               const int32_t* row_map = nullptr);
 
 template <class T, int V>
 struct VecT {

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(MP_THREADS, MP_MIN_BLOCKS) spmm_merge_k(
     const VT* __restrict__ val, const T* __restrict__ B, int64_t ldb, T* __restrict__ C,
     int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, int64_t n_items,
     const int64_t* __restrict__ plan_row, const int64_t* __restrict__ plan_k,
-    int64_t* __restrict__ carry_row, T* __restrict__ carry) {
+    int64_t* __restrict__ carry_row, T* __restrict__ carry, const int32_t* __restrict__ row_map) {
   constexpr int P = 32 / L;                          // entries in flight per warp step
   constexpr int E = (MP_BATCH + L - 1) / L;          // so every sub-group gets >= BATCH
   constexpr int CH = 32 * E;                         // entries per chunk
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(MP_THREADS, MP_MIN_BLOCKS) spmm_merge_k(
       if (r >= r1) break;
       if (touched) reduce_subgroups<T, V, L>(acc);
       if (sub == 0 && active_col) {
-        T* dst = C + r * ldc + col;
+        T* dst = C + (row_map ? (int64_t)__ldg(row_map + r) : r) * ldc + col;
         if (accumulate) {
           const VecT<T, V> old = load_out<T, V>(dst);
 #pragma unroll
@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(MP_THREADS, MP_MIN_BLOCKS) spmm_merge_k(
     }
     // the row left open at the item's end (if any) carries its partial sum
     if (touched) reduce_subgroups<T, V, L>(acc);
-    if (lane == 0 && c0 == 0) carry_row[w] = r1 < nrows ? r1 : -1;
+    if (lane == 0 && c0 == 0)
+      carry_row[w] = r1 < nrows ? (row_map ? (int64_t)__ldg(row_map + r1) : r1) : -1;
     if (sub == 0 && active_col) {
       T* cdst = carry + w * nk + col;
 #pragma unroll
@@ -191,7 +192,7 @@ size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t e
 template <class T, class VT, class PtrT, int L>
 static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                         T* C, int64_t ldc, int accumulate, int64_t path, char* scratch,
-                        cudaStream_t s, bool plan_ready) {
+                        cudaStream_t s, bool plan_ready, const int32_t* row_map) {
   constexpr int V = sizeof(T) == 4 ? 4 : 2;
   const int64_t nrows = A->nrows, nnz = A->nnz;
   const int64_t n_items = (nrows + nnz + path - 1) / path;
@@ -221,7 +222,7 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
   for (int64_t c0 = 0; c0 < nk; c0 += (int64_t)L * V) {
     spmm_merge_k<T, VT, PtrT, L, V><<<(int)grid, MP_THREADS, 0, s>>>(
         nrows, ptr, (const int*)A->idx, (const VT*)A->val, B, ldb, C, ldc, c0, nk, A->index_base,
-        accumulate, n_items, plan_row, plan_k, carry_row, carry);
+        accumulate, n_items, plan_row, plan_k, carry_row, carry, row_map);
     rc = check_launch("spmm_merge_k");
     if (rc) return rc;
   }
@@ -233,13 +234,13 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
 template <class T, class VT, class PtrT>
 static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                        T* C, int64_t ldc, int accumulate, int lanes, int64_t path, char* scratch,
-                       cudaStream_t s, bool plan_ready) {
+                       cudaStream_t s, bool plan_ready, const int32_t* row_map) {
   switch (lanes) {
-    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
-    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
-    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
-    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
-    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready);
+    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
+    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
+    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
+    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
+    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
   }
 }
 
@@ -247,7 +248,7 @@ static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ld
 // the vector width).  scratch == NULL allocates it on the stream.
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
-               size_t scratch_bytes, cudaStream_t s, bool plan_ready) {
+               size_t scratch_bytes, cudaStream_t s, bool plan_ready, const int32_t* row_map) {
   const size_t esz = dtype == FGB_F64 ? 8 : 4;
   const size_t need = spmm_merge_scratch_bytes(A->nrows, A->nnz, nk, esz, path);
   char* buf = (char*)scratch;
@@ -257,14 +258,14 @@ int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, in
   int rc;
   const bool i32 = A->ptr_t == FGB_I32;
   if (dtype == FGB_F64)
-    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
-             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
+    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
+             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
   else if (A->val_t == FGB_BF16)
-    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
-             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
+    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
+             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
   else
-    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch)
-             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch);
+    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
+             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
   if (!scratch) cudaFreeAsync(buf, s);
   return rc;
 }

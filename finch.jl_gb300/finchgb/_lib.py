@@ -128,6 +128,10 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fgb_cg_solve": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p, c_void_p,
                              POINTER(FgbCgOptions), POINTER(FgbCgResult), c_void_p]),
+    "fgb_panels_create": (c_int, [c_void_p, POINTER(FgbSparse), c_int32, POINTER(c_void_p)]),
+    "fgb_panels_spmm": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_int64,
+                                c_int, c_uint, POINTER(FgbSpmmTuning), c_void_p]),
+    "fgb_panels_destroy": (c_int, [c_void_p]),
     "fgb_plan_create": (c_int, [c_void_p, POINTER(FgbPlanDesc), c_int32, POINTER(c_void_p)]),
     "fgb_plan_execute": (c_int, [c_void_p, c_void_p]),
     "fgb_plan_info_get": (c_int, [c_void_p, POINTER(FgbPlanInfo)]),

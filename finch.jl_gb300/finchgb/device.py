@@ -194,6 +194,42 @@ def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags:
     return C
 
 
+class Panels:
+    """Column-panel layout of a CSR matrix (fgb_panels_*) for SpMM with an
+    L2-resident slice of B per panel."""
+
+    def __init__(self, A: DeviceSparse, npanels: int):
+        self.A = A
+        self.npanels = npanels
+        h = ctypes.c_void_p()
+        d = A.desc()
+        L.call("fgb_panels_create", context(A.idx.device.index), ctypes.byref(d), npanels,
+               ctypes.byref(h))
+        self.h = h
+
+    def spmm(self, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0,
+             lanes: int = 0, path: int = 0) -> torch.Tensor:
+        nk = B.shape[1]
+        if C is None:
+            C = torch.empty((self.A.nrows, nk), dtype=B.dtype, device=B.device)
+            flags &= ~L.ACCUMULATE
+        tune = L.FgbSpmmTuning(lanes, 0, path)
+        L.call("fgb_panels_spmm", _ctx_for(B), self.h, _dptr(B), B.stride(0), nk, _dptr(C),
+               C.stride(0), dtype_code(B), flags, ctypes.byref(tune), stream_ptr())
+        return C
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.call("fgb_panels_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def sddmm(A: DeviceSparse, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
           flags: int = 0) -> torch.Tensor:
     """out[e] = A.val[e] * <X[i,:], Y[j,:]> over A's stored entries."""

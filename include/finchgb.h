@@ -296,6 +296,28 @@ FGB_API int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void
 FGB_API int fgb_scalar_op(fgb_ctx* ctx, int op, int dtype, const void* a, const void* b,
                           void* out, void* stream);
 
+/* ---- column panels: SpMM with an L2-resident slice of B ---------------- */
+
+typedef struct fgb_panels fgb_panels;
+
+/* Splits a CSR matrix's columns into `npanels` panels of consecutive
+ * columns, built on the device once.  Panel 0 is a CSR over all rows; panels
+ * 1.. list only their non-empty rows (a row map over a SparseList of rows,
+ * i.e. Finch's SparseList(SparseList(Element)) / DCSR).  Each panel of an
+ * SpMM then gathers only its 1/npanels slice of B's rows, which stays in L2;
+ * C rows touched by several panels are accumulated panel by panel.  The
+ * layout holds a copy of A's idx/val (sorted by panel).  Synchronous. */
+FGB_API int fgb_panels_create(fgb_ctx* ctx, const fgb_sparse* A, int32_t npanels,
+                              fgb_panels** out);
+/* C = (C +) A @ B through the panels (F32 with F32/BF16 values, or F64).
+ * nk, ldb, ldc and the B/C pointers must be 4-float (2-double) aligned.
+ * The merge-path item boundaries of every panel are computed on the first
+ * call and reused while nk and the item length stay the same. */
+FGB_API int fgb_panels_spmm(fgb_ctx* ctx, fgb_panels* panels, const void* B, int64_t ldb,
+                            int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags,
+                            const fgb_spmm_tuning* tune, void* stream);
+FGB_API int fgb_panels_destroy(fgb_panels* panels);
+
 /* ---- plans: autotuned, graph-captured operations ------------------------ */
 
 typedef struct fgb_plan fgb_plan;
