@@ -238,16 +238,29 @@ def run_gpu(args):
     B = torch.from_numpy(B_h).to(device)
     C = torch.empty((M, NK), dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream()
-    if args.schedule:
+    if args.schedule:  # fixed plain merge-path schedule LANES,PATH (profiling)
         lanes, path = (int(v) for v in args.schedule.split(","))
-        table = {}
+        table, plan, npanels = {}, None, 1
     else:
+        # the plain schedules' table (for the e2e leg and the record), then the
+        # library autotuner, whose search space adds column panels
         (lanes, path), table = autotune(A, B, C, verbose=args.sweep)
-    slabs = -(-NK // (4 * lanes))
-    launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
+        from finchgb.plan import Plan
+
+        plan = Plan.spmm(A, B, C, tune_reps=3)
+        info = plan.info()
+        npanels = info["panels"]
+    slabs = -(-NK // (4 * (32 if plan else lanes)))
+    if plan is None:
+        launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
+    else:  # per panel: the slab launches + fix-up (item boundaries precomputed)
+        launches_per_step = npanels * (slabs + 1)
 
     def step():
-        dev.spmm(A, B, C, lanes=lanes, path=path)
+        if plan is not None:
+            plan.execute()
+        else:
+            dev.spmm(A, B, C, lanes=lanes, path=path)
 
     def barrier():
         if world > 1:
@@ -286,10 +299,11 @@ def run_gpu(args):
             "data": "synthetic (seeded PCG64)",
             "config": {"workload": workload_name(args.rows), "nnz": int(A_h.nnz), "k": NK,
                        "algorithmic_bytes_per_step": nbytes,
-                       "schedule": {"lanes": lanes, "column_slab": 4 * lanes,
-                                    "merge_path_item": path,
-                                    "autotune_ms": {f"{k[0]}x{k[1]}": round(v, 4)
-                                                    for k, v in table.items()}},
+                       "schedule": ({"autotuner": "fgb_plan_create (tune_reps=3), graph replay",
+                                     **plan.info()} if plan is not None else
+                                    {"lanes": lanes, "merge_path_item": path}),
+                       "plain_schedules_ms": {f"{k[0]}x{k[1]}": round(v, 4)
+                                              for k, v in table.items()},
                        "l2": "inputs larger than L2 (1.16 GB per step vs 129 MB)",
                        "parallelism": f"replicas{world}"},
             "gpu_launches": args.steps * launches_per_step}
@@ -343,7 +357,8 @@ def run_gpu(args):
                        "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "steps": e2e_steps, "ms_per_step": round(e2e_ms / e2e_steps, 3),
                        "result_matches_device_run": ok}
-        line["gpu_launches"] += (e2e_steps) * launches_per_step
+        # the e2e leg runs the plain merge-path schedule: item plan + slabs + fix-up
+        line["gpu_launches"] += e2e_steps * (2 + -(-NK // (4 * lanes)))
 
     # ---- roofline of the SpMM (plan + per-slab merge kernels + fix-up)
     peak, peak_kind = load_peaks()
@@ -354,7 +369,9 @@ def run_gpu(args):
                         "unit": "GB/s", "frac": round(achieved / peak, 4),
                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": traffic, "traffic_source": traffic_src,
-                        "kernel": f"spmm_merge_k x{slabs} slabs + merge_plan_k + spmm_fixup_k",
+                        "kernel": (f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
+                                   if plan is not None and npanels > 1 else
+                                   f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
                         "algorithmic_bytes_per_launch": nbytes,
                         "avg_launch_ms": round(avg_ms, 4)}
     line["cpu_baseline"] = None

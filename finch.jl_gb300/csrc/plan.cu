@@ -33,6 +33,7 @@ int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, co
 struct Choice {
   int lanes = 0;
   int64_t path = 0;
+  int panels = 1;  // SpMM: column panels (1 = the plain merge-path schedule)
 };
 
 static std::mutex g_tune_mu;
@@ -58,7 +59,7 @@ static void tune_cache_load_locked() {
   std::ifstream in(path);
   std::string key;
   Choice c;
-  while (in >> key >> c.lanes >> c.path) g_tune_cache[key] = c;
+  while (in >> key >> c.lanes >> c.path >> c.panels) g_tune_cache[key] = c;
 }
 
 static void tune_cache_store_locked(const std::string& key, const Choice& c) {
@@ -66,7 +67,7 @@ static void tune_cache_store_locked(const std::string& key, const Choice& c) {
   const char* path = std::getenv("FGB_TUNE_CACHE");
   if (!path) return;
   std::ofstream out(path, std::ios::app);
-  out << key << ' ' << c.lanes << ' ' << c.path << '\n';
+  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << '\n';
 }
 
 }  // namespace fgb
@@ -74,6 +75,7 @@ static void tune_cache_store_locked(const std::string& key, const Choice& c) {
 using namespace fgb;
 
 struct fgb_plan {
+  std::map<int, fgb_panels*> panels;  // SpMM column-panel layouts by panel count
   fgb_ctx* ctx = nullptr;
   fgb_plan_desc d{};
   fgb_sparse A{};
@@ -96,6 +98,18 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
       return spmv_with_group(p->ctx, d.semiring, &p->A, d.in0, d.dtype, d.out, d.dtype, d.flags,
                              c.lanes, s);
     case FGB_PLAN_SPMM:
+      if (c.panels > 1) {
+        auto it = p->panels.find(c.panels);
+        if (it == p->panels.end()) {
+          fgb_panels* pn = nullptr;
+          const int rc = fgb_panels_create(p->ctx, &p->A, c.panels, &pn);
+          if (rc) return rc;
+          it = p->panels.emplace(c.panels, pn).first;
+        }
+        fgb_spmm_tuning t{c.lanes, 0, c.path};
+        return fgb_panels_spmm(p->ctx, it->second, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
+                               d.flags, &t, s);
+      }
       if (c.path > 0)
         return spmm_merge(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                           (d.flags & FGB_ACCUMULATE) ? 1 : 0, c.lanes, c.path, p->scratch,
@@ -126,7 +140,12 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       return out;
     }
     for (int l : {8, 16, 32})
-      for (int64_t path : {128, 256, 512, 1024}) out.push_back(Choice{l, path});
+      for (int64_t path : {128, 256, 512, 1024}) out.push_back(Choice{l, path, 1});
+    // column panels keep each panel's slice of B in L2 (worth it when B is not)
+    const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);
+    if (b_bytes > 32.0 * 1024 * 1024 && !(d.flags & FGB_ACCUMULATE))
+      for (int np : {4, 8, 16})
+        for (int64_t path : {256, 512, 1024}) out.push_back(Choice{32, path, np});
   } else {
     if (d.flags & FGB_FINCH_ORDER) return {Choice{0, 0}};
     for (int l : {8, 16, 32})
@@ -181,7 +200,8 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
       for (const Choice& c : cands)
-        if (c.lanes == it->second.lanes && c.path == it->second.path) {
+        if (c.lanes == it->second.lanes && c.path == it->second.path &&
+            c.panels == it->second.panels) {
           best = c;
           cached = true;
         }
@@ -243,7 +263,16 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     return rc;
   }
   p->choice = best;
+  for (auto it = p->panels.begin(); it != p->panels.end();) {  // keep only the chosen layout
+    if (it->first != best.panels) {
+      fgb_panels_destroy(it->second);
+      it = p->panels.erase(it);
+    } else {
+      ++it;
+    }
+  }
   p->info.lanes = best.lanes;
+  p->info.panels = best.panels;
   p->info.path = best.path;
   p->info.tuned_ms = best_ms;
   p->info.first_candidate_ms = first_ms;
@@ -271,6 +300,7 @@ int fgb_plan_destroy(fgb_plan* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->scratch) cudaFree(p->scratch);
+  for (auto& kv : p->panels) fgb_panels_destroy(kv.second);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
   return FGB_OK;

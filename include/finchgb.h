@@ -349,6 +349,8 @@ typedef struct fgb_plan_info {
   double first_candidate_ms; /* time of the first schedule tried */
   int32_t candidates;        /* schedules in the search space */
   int32_t from_cache;        /* 1 if the choice came from the tuning cache */
+  int32_t panels;            /* SpMM: column panels of the chosen schedule (1 = none) */
+  int32_t reserved2;
 } fgb_plan_info;
 
 /* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use
