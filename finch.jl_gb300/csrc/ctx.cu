@@ -82,6 +82,8 @@ int fgb_ctx_create(int device, fgb_ctx** out) {
   c->device = device;
   e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
   if (e != cudaSuccess) {
     delete c;
     return set_error(FGB_ECUDA, "fgb_ctx_create: %s", cudaGetErrorString(e));
@@ -97,11 +99,20 @@ int fgb_ctx_destroy(fgb_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
   }
+  if (ctx->d_err) cudaFree(ctx->d_err);
   delete ctx;
   return FGB_OK;
 }
 
 void* fgb_ctx_stream(fgb_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int fgb_ctx_device_error(fgb_ctx* ctx, int* flag) {
+  if (!ctx || !flag) return set_error(FGB_EINVAL, "fgb_ctx_device_error: null argument");
+  FGB_CUDA_TRY(cudaDeviceSynchronize());
+  FGB_CUDA_TRY(cudaMemcpy(flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  FGB_CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(int)));
+  return FGB_OK;
+}
 
 int fgb_ctx_num_sms(fgb_ctx* ctx) { return ctx ? ctx->num_sms : 0; }
 

@@ -15,6 +15,7 @@ struct fgb_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  int* d_err = nullptr;  // device flag: a kernel's bounded wait ran out (read by fgb_ctx_device_error)
   std::mutex mu;  // guards lazily created per-context state
 };
 

@@ -284,6 +284,7 @@ int fgb_panels_spmm(fgb_ctx* ctx, fgb_panels* pn, const void* B, int64_t ldb, in
   int lanes = tune && tune->lanes ? tune->lanes : 32;
   while (lanes > 4 && (int64_t)(lanes / 2) * vn >= nk) lanes /= 2;
   const int64_t path = tune && tune->path ? tune->path : 512;
+  const int variant = tune ? tune->variant : 0;
   cudaStream_t s = pick_stream(ctx, stream);
   bool ready = pn->scratch && pn->scratch_nk == nk && pn->scratch_path == path;
   if (!ready) {
@@ -310,7 +311,7 @@ int fgb_panels_spmm(fgb_ctx* ctx, fgb_panels* pn, const void* B, int64_t ldb, in
     const size_t bytes = (p + 1 < pn->npanels ? pn->scratch_off[p + 1] : pn->scratch_bytes) - pn->scratch_off[p];
     const int rc = spmm_merge(ctx, &d, B, ldb, nk, C, ldc, dtype, accumulate, lanes, path,
                               (char*)pn->scratch + pn->scratch_off[p], bytes, s, ready,
-                              p == 0 ? nullptr : pn->rows_all + pn->rows_off[p]);
+                              p == 0 ? nullptr : pn->rows_all + pn->rows_off[p], variant);
     if (rc) return rc;
   }
   return FGB_OK;

@@ -34,6 +34,7 @@ struct Choice {
   int lanes = 0;
   int64_t path = 0;
   int panels = 1;  // SpMM: column panels (1 = the plain merge-path schedule)
+  int variant = 0;  // SpMM: 0 register gathers, 1 TMA stage ring
 };
 
 static std::mutex g_tune_mu;
@@ -59,7 +60,7 @@ static void tune_cache_load_locked() {
   std::ifstream in(path);
   std::string key;
   Choice c;
-  while (in >> key >> c.lanes >> c.path >> c.panels) g_tune_cache[key] = c;
+  while (in >> key >> c.lanes >> c.path >> c.panels >> c.variant) g_tune_cache[key] = c;
 }
 
 static void tune_cache_store_locked(const std::string& key, const Choice& c) {
@@ -67,7 +68,7 @@ static void tune_cache_store_locked(const std::string& key, const Choice& c) {
   const char* path = std::getenv("FGB_TUNE_CACHE");
   if (!path) return;
   std::ofstream out(path, std::ios::app);
-  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << '\n';
+  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << ' ' << c.variant << '\n';
 }
 
 }  // namespace fgb
@@ -106,14 +107,14 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           if (rc) return rc;
           it = p->panels.emplace(c.panels, pn).first;
         }
-        fgb_spmm_tuning t{c.lanes, 0, c.path};
+        fgb_spmm_tuning t{c.lanes, c.variant, c.path};
         return fgb_panels_spmm(p->ctx, it->second, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                                d.flags, &t, s);
       }
       if (c.path > 0)
         return spmm_merge(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                           (d.flags & FGB_ACCUMULATE) ? 1 : 0, c.lanes, c.path, p->scratch,
-                          p->scratch_bytes, s, plan_ready);
+                          p->scratch_bytes, s, plan_ready, nullptr, c.variant);
       return spmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype, d.flags,
                        c.lanes, 0, s);
     case FGB_PLAN_SDDMM:
@@ -140,12 +141,16 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       return out;
     }
     for (int l : {8, 16, 32})
-      for (int64_t path : {128, 256, 512, 1024}) out.push_back(Choice{l, path, 1});
+      for (int64_t path : {128, 256, 512, 1024}) out.push_back(Choice{l, path, 1, 0});
+    if (d.dtype == FGB_F32)  // B rows staged by TMA into a shared-memory ring
+      for (int64_t path : {256, 512, 1024, 2048}) out.push_back(Choice{32, path, 1, 1});
     // column panels keep each panel's slice of B in L2 (worth it when B is not)
     const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);
     if (b_bytes > 32.0 * 1024 * 1024 && !(d.flags & FGB_ACCUMULATE))
       for (int np : {4, 8, 16})
-        for (int64_t path : {256, 512, 1024}) out.push_back(Choice{32, path, np});
+        for (int64_t path : {256, 512, 1024})
+          for (int v : {0, 1})
+            if (v == 0 || d.dtype == FGB_F32) out.push_back(Choice{32, path, np, v});
   } else {
     if (d.flags & FGB_FINCH_ORDER) return {Choice{0, 0}};
     for (int l : {8, 16, 32})
@@ -201,7 +206,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     if (it != g_tune_cache.end()) {
       for (const Choice& c : cands)
         if (c.lanes == it->second.lanes && c.path == it->second.path &&
-            c.panels == it->second.panels) {
+            c.panels == it->second.panels && c.variant == it->second.variant) {
           best = c;
           cached = true;
         }
@@ -273,6 +278,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   }
   p->info.lanes = best.lanes;
   p->info.panels = best.panels;
+  p->info.variant = best.variant;
   p->info.path = best.path;
   p->info.tuned_ms = best_ms;
   p->info.first_candidate_ms = first_ms;

@@ -220,6 +220,9 @@ __global__ void __launch_bounds__(SRV_THREADS) serve_loop_k(SrvArgs a) {
       __threadfence();
       const unsigned done = atomicAdd(a.done_items + it.slot, 1u) + 1u;
       if ((int)done == s.n_items) {
+        // re-arm the slot's counter before the host can see the request done
+        // (and hand the slot to the next request)
+        a.done_items[it.slot] = 0u;
         __threadfence_system();
         st_release_sys(&a.host->status[it.slot], s.seq);
       }
@@ -246,6 +249,7 @@ struct Ticket {
   int64_t rows = 0, n_items = 0;
   uint64_t item0 = 0;  // ring index of the request's first item
   uint64_t seq = 0;
+  float* out_mapped = nullptr;  // device alias of a pinned output: written in place, no copy back
   std::chrono::steady_clock::time_point t_submit, t_done;
   int state = 0;  // 0 queued, 1 in flight, 2 done, 3 failed
   int status = FGB_OK;
@@ -382,8 +386,9 @@ void run_per_call(fgb_server* s, std::vector<uint64_t>& batch, std::unique_lock<
   for (uint64_t id : batch) {
     Ticket& t = s->tickets[id];
     const fgb_request r = t.req;
+    float* out_dev = t.out_mapped ? t.out_mapped : (float*)(s->pool + t.out_off);
     const DevSlot slot{r.op, r.matrix, r.matrix_b, r.nk, (const float*)(s->pool + t.in_off),
-                       (float*)(s->pool + t.out_off), (int32_t)t.n_items, 0, t.seq};
+                       out_dev, (int32_t)t.n_items, 0, t.seq};
     lk.unlock();
     cudaError_t e = cudaSuccess;
     if (t.in_bytes) e = cudaMemcpyAsync(s->pool + t.in_off, r.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
@@ -392,7 +397,7 @@ void run_per_call(fgb_server* s, std::vector<uint64_t>& batch, std::unique_lock<
                                                                            s->cfg.rows_per_item);
       e = cudaGetLastError();
     }
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !t.out_mapped)
       e = cudaMemcpyAsync(r.output, s->pool + t.out_off, t.out_bytes, cudaMemcpyDeviceToHost, s->copy_stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
     lk.lock();
@@ -423,7 +428,7 @@ void worker_main(fgb_server* s) {
       if (slot < 0) break;
       size_t in_off = 0, out_off = 0;
       if (t.in_bytes && !s->alloc->alloc(t.in_bytes, &in_off)) break;
-      if (!s->alloc->alloc(t.out_bytes, &out_off)) {
+      if (t.out_bytes && !s->alloc->alloc(t.out_bytes, &out_off)) {
         if (t.in_bytes) s->alloc->release(in_off, t.in_bytes);
         break;
       }
@@ -452,13 +457,9 @@ void worker_main(fgb_server* s) {
         if (t.in_bytes && e == cudaSuccess)
           e = cudaMemcpyAsync(s->pool + t.in_off, t.req.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
         s->stage_slots[t.slot] = DevSlot{t.req.op, t.req.matrix, t.req.matrix_b, t.req.nk,
-                                        (const float*)(s->pool + t.in_off), (float*)(s->pool + t.out_off),
+                                        (const float*)(s->pool + t.in_off),
+                                        t.out_mapped ? t.out_mapped : (float*)(s->pool + t.out_off),
                                         (int32_t)t.n_items, 0, t.seq};
-        if (e == cudaSuccess)
-          e = cudaMemcpyAsync(s->d_slots + t.slot, s->stage_slots + t.slot, sizeof(DevSlot), cudaMemcpyHostToDevice, s->copy_stream);
-        // reset the slot's done counter by DMA (no kernel competes with the loop)
-        if (e == cudaSuccess)
-          e = cudaMemcpyAsync(s->d_done + t.slot, s->zero_word, sizeof(unsigned), cudaMemcpyHostToDevice, s->copy_stream);
         for (int64_t b = 0; b < t.n_items; ++b) {
           const int64_t pos = (s->published + n_new) % SRV_ITEM_CAP;
           s->stage_items[pos] = DevItem{(uint32_t)t.slot, (uint32_t)(b * s->cfg.rows_per_item),
@@ -466,6 +467,11 @@ void worker_main(fgb_server* s) {
           ++n_new;
         }
       }
+      // one copy of the slot table (in-flight slots are rewritten unchanged;
+      // the device re-arms each slot's done counter itself)
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->d_slots, s->stage_slots, sizeof(DevSlot) * s->cfg.max_inflight,
+                            cudaMemcpyHostToDevice, s->copy_stream);
       // the new items occupy ring positions [published, published + n_new)
       const int64_t p0 = s->published % SRV_ITEM_CAP;
       const int64_t first = std::min<int64_t>(n_new, SRV_ITEM_CAP - p0);
@@ -513,14 +519,19 @@ void worker_main(fgb_server* s) {
         progressed = true;
         std::atomic_thread_fence(std::memory_order_acquire);
         cudaError_t e = cudaSuccess;
+        bool copies = false;
         for (uint64_t id : done) {
           Ticket& t = s->tickets[id];
-          if (e == cudaSuccess)
+          if (e == cudaSuccess && !t.out_mapped) {
             e = cudaMemcpyAsync(t.req.output, s->pool + t.out_off, t.out_bytes, cudaMemcpyDeviceToHost, s->copy_stream);
+            copies = true;
+          }
         }
-        lk.unlock();
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
-        lk.lock();
+        if (copies) {
+          lk.unlock();
+          if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
+          lk.lock();
+        }
         if (e != cudaSuccess) fail_worker(s, FGB_ECUDA, "result copies", e);
         for (uint64_t id : done) finish(s, s->tickets[id], e == cudaSuccess ? FGB_OK : FGB_ECUDA);
         s->inflight.swap(still);
@@ -644,6 +655,15 @@ int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
   t.n_items = (A.nrows + s->cfg.rows_per_item - 1) / s->cfg.rows_per_item;
   t.in_bytes = req_in_bytes(s, *r);
   t.out_bytes = req_out_bytes(s, *r, A.nnz);
+  // a page-locked output is written by the device in place (no copy back)
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, r->output) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+      attr.devicePointer) {
+    t.out_mapped = (float*)attr.devicePointer;
+    t.out_bytes = 0;
+  } else {
+    cudaGetLastError();
+  }
   if (t.in_bytes + t.out_bytes + 512 > s->cfg.pool_bytes)
     return set_error(FGB_ENOMEM, "fgb_server_submit: request needs %zu bytes, pool holds %zu",
                      t.in_bytes + t.out_bytes, s->cfg.pool_bytes);

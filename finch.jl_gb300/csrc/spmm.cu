@@ -178,7 +178,7 @@ static void default_merge_tuning(const fgb_sparse* A, int64_t nk, size_t esz, in
 template <class T, class VT>
 static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
                      void* C, int64_t ldc, unsigned flags, int lanes, int64_t path,
-                     cudaStream_t s) {
+                     cudaStream_t s, int variant) {
   const int accumulate = (flags & FGB_ACCUMULATE) ? 1 : 0;
   int fm = FM_DEFAULT;
   if (flags & FGB_NO_FMA) fm = FM_NOFMA;
@@ -192,7 +192,7 @@ static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
     if (!(flags & FGB_FINCH_ORDER) && vec_ok) {
       default_merge_tuning(A, nk, sizeof(T), &lanes, &path);
       return spmm_merge(ctx, A, B, ldb, nk, C, ldc, sizeof(T) == 8 ? FGB_F64 : FGB_F32,
-                        accumulate, lanes, path, nullptr, 0, s);
+                        accumulate, lanes, path, nullptr, 0, s, false, nullptr, variant);
     }
     if (lanes <= 0) lanes = default_lanes(nk, sizeof(T) == 4 ? 4 : 2, A->ncols * nk * (int64_t)sizeof(T));
     if (A->ptr_t == FGB_I32)
@@ -219,7 +219,8 @@ static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
 }
 
 int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
-              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream) {
+              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream,
+              int variant) {
   if (!ctx) return set_error(FGB_EINVAL, "fgb_spmm: null ctx");
   int rc = check_sparse(A, "fgb_spmm: A", true);
   if (rc) return rc;
@@ -228,11 +229,11 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
     return set_error(FGB_EINVAL, "fgb_spmm: null B or C");
   cudaStream_t s = pick_stream(ctx, stream);
   if (dtype == FGB_F32) {
-    if (A->val_t == FGB_F32) return run_typed<float, float>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
+    if (A->val_t == FGB_F32) return run_typed<float, float>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s, variant);
     if (A->val_t == FGB_BF16)
-      return run_typed<float, __nv_bfloat16>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
+      return run_typed<float, __nv_bfloat16>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s, variant);
   } else if (dtype == FGB_F64) {
-    if (A->val_t == FGB_F64) return run_typed<double, double>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s);
+    if (A->val_t == FGB_F64) return run_typed<double, double>(ctx, A, B, ldb, nk, C, ldc, flags, lanes, path, s, variant);
   }
   return set_error(FGB_EUNSUPPORTED, "fgb_spmm: no kernel for val %d / dtype %d", A->val_t, dtype);
 }
@@ -249,8 +250,10 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
                            const fgb_spmm_tuning* tune, void* stream) {
   int lanes = tune ? tune->lanes : 0;
   int64_t path = tune ? tune->path : 0;
+  const int variant = tune ? tune->variant : 0;
+  if (variant != 0 && variant != 1) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0 or 1");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
   if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");
-  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, lanes, path, stream);
+  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, lanes, path, stream, variant);
 }

@@ -9,7 +9,8 @@ namespace fgb {
 
 // fgb_spmm's dispatcher (spmm.cu); lanes/path 0 = defaults.
 int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
-              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream);
+              int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream,
+              int variant = 0);
 
 // Merge-path SpMM (spmm_merge.cu).
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
@@ -20,7 +21,13 @@ size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t e
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
                size_t scratch_bytes, cudaStream_t s, bool plan_ready = false,
-               const int32_t* row_map = nullptr);
+               const int32_t* row_map = nullptr, int variant = 0);
+
+// Stage-ring (TMA gather4) kernels over planned merge-path items (spmm_tma.cu).
+int spmm_tma_items(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
+                   void* C, int64_t ldc, int accumulate, int64_t n_items, const int64_t* plan_row,
+                   const int64_t* plan_k, int64_t* carry_row, void* carry, const int32_t* row_map,
+                   int* err, cudaStream_t s);
 
 template <class T, int V>
 struct VecT {

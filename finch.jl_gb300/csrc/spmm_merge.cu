@@ -192,7 +192,7 @@ size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t e
 template <class T, class VT, class PtrT, int L>
 static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                         T* C, int64_t ldc, int accumulate, int64_t path, char* scratch,
-                        cudaStream_t s, bool plan_ready, const int32_t* row_map) {
+                        cudaStream_t s, bool plan_ready, const int32_t* row_map, int variant) {
   constexpr int V = sizeof(T) == 4 ? 4 : 2;
   const int64_t nrows = A->nrows, nnz = A->nnz;
   const int64_t n_items = (nrows + nnz + path - 1) / path;
@@ -219,6 +219,11 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
   const int64_t grid_need = (warps_needed * 32 + MP_THREADS - 1) / MP_THREADS;
   if (grid > grid_need) grid = grid_need;
   if (grid < 1) grid = 1;
+  if (variant == 1 && sizeof(T) == 4) {  // B rows staged through shared memory by TMA
+    rc = spmm_tma_items(ctx, A, B, ldb, nk, C, ldc, accumulate, n_items, plan_row, plan_k,
+                        carry_row, carry, row_map, ctx->d_err, s);
+    if (rc) return rc;
+  } else
   for (int64_t c0 = 0; c0 < nk; c0 += (int64_t)L * V) {
     spmm_merge_k<T, VT, PtrT, L, V><<<(int)grid, MP_THREADS, 0, s>>>(
         nrows, ptr, (const int*)A->idx, (const VT*)A->val, B, ldb, C, ldc, c0, nk, A->index_base,
@@ -234,13 +239,13 @@ static int launch_merge(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t l
 template <class T, class VT, class PtrT>
 static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ldb, int64_t nk,
                        T* C, int64_t ldc, int accumulate, int lanes, int64_t path, char* scratch,
-                       cudaStream_t s, bool plan_ready, const int32_t* row_map) {
+                       cudaStream_t s, bool plan_ready, const int32_t* row_map, int variant) {
   switch (lanes) {
-    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
-    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
-    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
-    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
-    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map);
+    case 2: return launch_merge<T, VT, PtrT, 2>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map, variant);
+    case 4: return launch_merge<T, VT, PtrT, 4>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map, variant);
+    case 8: return launch_merge<T, VT, PtrT, 8>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map, variant);
+    case 16: return launch_merge<T, VT, PtrT, 16>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map, variant);
+    default: return launch_merge<T, VT, PtrT, 32>(ctx, A, B, ldb, nk, C, ldc, accumulate, path, scratch, s, plan_ready, row_map, variant);
   }
 }
 
@@ -248,7 +253,8 @@ static int merge_lanes(fgb_ctx* ctx, const fgb_sparse* A, const T* B, int64_t ld
 // the vector width).  scratch == NULL allocates it on the stream.
 int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
                int64_t ldc, int dtype, int accumulate, int lanes, int64_t path, void* scratch,
-               size_t scratch_bytes, cudaStream_t s, bool plan_ready, const int32_t* row_map) {
+               size_t scratch_bytes, cudaStream_t s, bool plan_ready, const int32_t* row_map,
+               int variant) {
   const size_t esz = dtype == FGB_F64 ? 8 : 4;
   const size_t need = spmm_merge_scratch_bytes(A->nrows, A->nnz, nk, esz, path);
   char* buf = (char*)scratch;
@@ -258,14 +264,14 @@ int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, in
   int rc;
   const bool i32 = A->ptr_t == FGB_I32;
   if (dtype == FGB_F64)
-    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
-             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
+    rc = i32 ? merge_lanes<double, double, int32_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant)
+             : merge_lanes<double, double, int64_t>(ctx, A, (const double*)B, ldb, nk, (double*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant);
   else if (A->val_t == FGB_BF16)
-    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
-             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
+    rc = i32 ? merge_lanes<float, __nv_bfloat16, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant)
+             : merge_lanes<float, __nv_bfloat16, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant);
   else
-    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map)
-             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map);
+    rc = i32 ? merge_lanes<float, float, int32_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant)
+             : merge_lanes<float, float, int64_t>(ctx, A, (const float*)B, ldb, nk, (float*)C, ldc, accumulate, lanes, path, buf, s, plan_ready && scratch, row_map, variant);
   if (!scratch) cudaFreeAsync(buf, s);
   return rc;
 }

@@ -38,7 +38,7 @@ class FinchGBError(RuntimeError):
 
 
 class FgbSpmmTuning(ctypes.Structure):
-    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64)]
+    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("path", c_int64)]
 
 
 class FgbCgOptions(ctypes.Structure):
@@ -62,7 +62,7 @@ class FgbPlanInfo(ctypes.Structure):
     _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64),
                 ("tuned_ms", c_double), ("first_candidate_ms", c_double),
                 ("candidates", c_int32), ("from_cache", c_int32), ("panels", c_int32),
-                ("reserved2", c_int32)]
+                ("variant", c_int32)]
 
 
 class FgbServerConfig(ctypes.Structure):
@@ -96,6 +96,7 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_ctx_destroy": (c_int, [c_void_p]),
     "fgb_ctx_stream": (c_void_p, [c_void_p]),
     "fgb_ctx_num_sms": (c_int, [c_void_p]),
+    "fgb_ctx_device_error": (c_int, [c_void_p, POINTER(c_int)]),
     "fgb_malloc": (c_int, [c_void_p, c_size_t, POINTER(c_void_p)]),
     "fgb_free": (c_int, [c_void_p, c_void_p]),
     "fgb_host_alloc": (c_int, [c_void_p, c_size_t, POINTER(c_void_p)]),

@@ -181,14 +181,14 @@ def spmv(A: DeviceSparse, x: torch.Tensor, y: torch.Tensor | None = None,
 
 
 def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0,
-         lanes: int = 0, path: int = 0) -> torch.Tensor:
+         lanes: int = 0, path: int = 0, variant: int = 0) -> torch.Tensor:
     """C (+)= A @ B for row-major B (n x nk); lanes/path override the schedule."""
     nk = B.shape[1]
     if C is None:
         C = torch.empty((A.nrows, nk), dtype=B.dtype, device=B.device)
         flags &= ~L.ACCUMULATE
     d = A.desc()
-    tune = L.FgbSpmmTuning(lanes, 0, path)
+    tune = L.FgbSpmmTuning(lanes, variant, path)
     L.call("fgb_spmm_ex", _ctx_for(B), ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
            C.stride(0), dtype_code(B), flags, ctypes.byref(tune), stream_ptr())
     return C
@@ -208,12 +208,12 @@ class Panels:
         self.h = h
 
     def spmm(self, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0,
-             lanes: int = 0, path: int = 0) -> torch.Tensor:
+             lanes: int = 0, path: int = 0, variant: int = 0) -> torch.Tensor:
         nk = B.shape[1]
         if C is None:
             C = torch.empty((self.A.nrows, nk), dtype=B.dtype, device=B.device)
             flags &= ~L.ACCUMULATE
-        tune = L.FgbSpmmTuning(lanes, 0, path)
+        tune = L.FgbSpmmTuning(lanes, variant, path)
         L.call("fgb_panels_spmm", _ctx_for(B), self.h, _dptr(B), B.stride(0), nk, _dptr(C),
                C.stride(0), dtype_code(B), flags, ctypes.byref(tune), stream_ptr())
         return C

@@ -129,6 +129,10 @@ FGB_API int fgb_ctx_create(int device, fgb_ctx** out);
 FGB_API int fgb_ctx_destroy(fgb_ctx* ctx);
 /* The context's stream (a cudaStream_t). */
 FGB_API void* fgb_ctx_stream(fgb_ctx* ctx);
+/* Synchronises the device, then returns in *flag whether any kernel of this
+ * context gave up a bounded wait since the last call (1) or not (0), and
+ * clears the flag.  A kernel that gives up reports here instead of hanging. */
+FGB_API int fgb_ctx_device_error(fgb_ctx* ctx, int* flag);
 FGB_API int fgb_ctx_num_sms(fgb_ctx* ctx);
 
 /* Device buffers: the storage behind device-resident level buffers (what
@@ -196,9 +200,10 @@ FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
  * lanes * vector-width, one launch per slab, so the gathered slab of B stays
  * L2-resident.  Zero fields take the defaults. */
 typedef struct fgb_spmm_tuning {
-  int32_t lanes;    /* 2, 4, 8, 16 or 32 */
-  int32_t reserved; /* 0 */
-  int64_t path;     /* merge-path item length */
+  int32_t lanes;   /* 2, 4, 8, 16 or 32 */
+  int32_t variant; /* 0: B rows gathered into registers; 1: B rows staged into a
+                      shared-memory ring by TMA tile::gather4 (fp32) */
+  int64_t path;    /* merge-path item length */
 } fgb_spmm_tuning;
 
 /* fgb_spmm with an explicit schedule (NULL = defaults).  The result does not
@@ -350,7 +355,7 @@ typedef struct fgb_plan_info {
   int32_t candidates;        /* schedules in the search space */
   int32_t from_cache;        /* 1 if the choice came from the tuning cache */
   int32_t panels;            /* SpMM: column panels of the chosen schedule (1 = none) */
-  int32_t reserved2;
+  int32_t variant;           /* SpMM: 0 register gathers, 1 TMA stage ring */
 } fgb_plan_info;
 
 /* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use

@@ -1,5 +1,6 @@
 """GPU parity of SpMM, SDDMM, elementwise merges and elementwise+reduce
 (through the C ABI) against the oracle."""
+import ctypes
 import json
 from pathlib import Path
 
@@ -99,12 +100,31 @@ def test_spmm_zipf_rows(gpu_lib):
     C = to_host(dev.spmm(A, to_dev(B), flags=L.FINCH_ORDER))
     assert np.array_equal(C, want)
     scale = spmm_scale(r, B)
-    for lanes in (2, 4, 8, 16, 32):
+    for lanes, variant in [(2, 0), (4, 0), (8, 0), (16, 0), (32, 0), (32, 1)]:
         for path in (1, 7, 64, 256, 4096):
-            C1 = to_host(dev.spmm(A, to_dev(B), lanes=lanes, path=path))
+            C1 = to_host(dev.spmm(A, to_dev(B), lanes=lanes, path=path, variant=variant))
             assert_close(C1, want, scale, np.float32)
-            C2 = to_host(dev.spmm(A, to_dev(B), lanes=lanes, path=path))
+            C2 = to_host(dev.spmm(A, to_dev(B), lanes=lanes, path=path, variant=variant))
             assert np.array_equal(C1, C2)  # deterministic carry fix-up
+    flag = ctypes.c_int(1)
+    L.call("fgb_ctx_device_error", dev.context(), ctypes.byref(flag))
+    assert flag.value == 0  # no bounded wait ran out
+
+
+@pytest.mark.parametrize("nk", [128, 64, 32, 20, 256])
+def test_spmm_tma_stage_ring(gpu_lib, nk):
+    """B rows staged through shared memory by TMA gather4: same results as
+    the register-gather schedule within tolerance, for every slab width."""
+    rng = np.random.default_rng(nk + 17)
+    r = zipf_csr(rng, 9000, 7000, mean=16, cap=5000)
+    B = rng.standard_normal((7000, nk)).astype(np.float32)
+    A = upload(r)
+    want = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, r.val, B, nthreads=oracle.max_threads())
+    C = to_host(dev.spmm(A, to_dev(B), lanes=32, path=300, variant=1))
+    assert_close(C, want, spmm_scale(r, B), np.float32)
+    flag = ctypes.c_int(1)
+    L.call("fgb_ctx_device_error", dev.context(), ctypes.byref(flag))
+    assert flag.value == 0
 
 
 def test_spmm_merge_accumulate_and_empty(gpu_lib):
@@ -236,4 +256,6 @@ def test_spmm_column_panels(gpu_lib, npanels, nk):
     Cd = to_dev(C0)
     pn.spmm(Bd, Cd, flags=L.ACCUMULATE, path=128)
     assert_close(to_host(Cd), want + C0, scale + np.abs(C0), np.float32)
+    C3 = to_host(pn.spmm(Bd, variant=1, path=256))  # TMA stage ring per panel
+    assert_close(C3, want, scale, np.float32)
     pn.close()
