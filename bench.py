@@ -616,42 +616,96 @@ def serve_library(n_mats: int = 4096, n_partners: int = 512):
     return mats, partners
 
 
-def serve_run(mode, mats, partners, plan, arena, window, arrivals=None):
-    """Runs the request plan through a server; returns (seconds, latencies)."""
-    import torch
+def serve_layout(plan, mats, arena_floats):
+    """Places the requests' host buffers in a pinned arena used as a ring.
 
+    Request i gets [off[i], off[i] + need[i]) (input then output, or the
+    masked product's values); a request that would cross the end starts the
+    next lap at 0.  dep[i] is the last earlier request whose range may share
+    memory with request i: it must be complete before i is submitted."""
+    need = np.array([mats[k].nnz if op == "masked_mul" else (mats[k].ncols + mats[k].nrows) * max(nk, 1)
+                     for op, k, nk in plan], dtype=np.int64)
+    need = (need + 3) // 4 * 4  # 16-byte aligned starts
+    assert need.max() <= arena_floats
+    virt = np.empty(len(plan), dtype=np.int64)
+    v = 0
+    for i, n in enumerate(need):
+        if v % arena_floats + n > arena_floats:
+            v += arena_floats - v % arena_floats
+        virt[i] = v
+        v += n
+    dep = np.searchsorted(virt, virt + need - arena_floats, side="left") - 1
+    return virt % arena_floats, dep
+
+
+def serve_run(mode, mats, partners, plan, arena, window, arrivals=None, batch=128):
+    """Runs the request plan through a server; returns (seconds, latencies, stats).
+
+    The FgbRequest records (pointers into a pinned arena) are built before the
+    clock starts, the same for both modes.  Closed loop: requests go in groups
+    of `batch` through fgb_server_submit_batch, at most `window` in flight.
+    Open loop: every request whose Poisson arrival time has passed is
+    submitted as one group."""
+    from finchgb import _lib as L
     from finchgb.server import Server
 
-    slice_floats = arena.numel() // window
+    off, dep = serve_layout(plan, mats, arena.numel())
     lat = []
     with Server(mode=mode, pool_bytes=4 << 30, max_inflight=min(window, 4096)) as srv:
         ids = [srv.register(A) for A in mats]
         pids = [srv.register(B) for B in partners]
-        tickets = []
-        t0 = time.perf_counter()
+        reqs = (L.FgbRequest * len(plan))()
         for i, (op, k, nk) in enumerate(plan):
-            if i >= window:
-                lat.append(srv.wait(tickets[i - window]))
-            if arrivals is not None:
-                while time.perf_counter() - t0 < arrivals[i]:
-                    pass
             A = mats[k]
-            base = (i % window) * slice_floats
+            base = int(off[i])
             if op == "spmv":
-                inp = arena[base: base + A.ncols]
-                out = arena[base + A.ncols: base + A.ncols + A.nrows]
-                tickets.append(srv.submit(op, ids[k], inp, out))
+                reqs[i] = srv.request(op, ids[k], arena[base: base + A.ncols],
+                                      arena[base + A.ncols: base + A.ncols + A.nrows])
             elif op == "spmm":
-                inp = arena[base: base + A.ncols * nk]
-                out = arena[base + A.ncols * nk: base + (A.ncols + A.nrows) * nk]
-                tickets.append(srv.submit(op, ids[k], inp, out, nk=nk))
+                reqs[i] = srv.request(op, ids[k], arena[base: base + A.ncols * nk],
+                                      arena[base + A.ncols * nk: base + (A.ncols + A.nrows) * nk], nk=nk)
             else:
-                out = arena[base: base + A.nnz]
-                tickets.append(srv.submit(op, ids[k], None, out, matrix_b=pids[k]))
-        for t in tickets[max(0, len(plan) - window):]:
-            lat.append(srv.wait(t))
+                reqs[i] = srv.request(op, ids[k], None, arena[base: base + A.nnz], matrix_b=pids[k])
+        size = ctypes.sizeof(L.FgbRequest)
+        base_addr = ctypes.addressof(reqs)
+        tickets: list[int] = []
+        t_submit = t_wait = 0.0
+        waited = 0
+        n = len(plan)
+        t0 = time.perf_counter()
+        i = 0
+        while i < n:
+            if arrivals is None:
+                j = min(n, i + batch)
+            else:
+                now = time.perf_counter() - t0
+                while arrivals[i] > now:
+                    now = time.perf_counter() - t0
+                j = i + 1
+                while j < n and arrivals[j] <= now and j - i < batch:
+                    j += 1
+            while j > i + 1 and dep[i:j].max() >= i:  # no overlap inside a group
+                j -= 1
+            # at most `window` requests in flight, and none whose arena range
+            # the group reuses
+            upto = max(j - window, int(dep[i:j].max()) + 1)
+            if upto > waited:
+                tw = time.perf_counter()
+                lat.extend(srv.wait_batch(tickets[waited:upto]))
+                t_wait += time.perf_counter() - tw
+                waited = upto
+            grp = (L.FgbRequest * (j - i)).from_address(base_addr + i * size)
+            ts = time.perf_counter()
+            tickets.extend(srv.submit_batch(grp))
+            t_submit += time.perf_counter() - ts
+            i = j
+        tw = time.perf_counter()
+        lat.extend(srv.wait_batch(tickets[waited:]))
+        t_wait += time.perf_counter() - tw
         dt = time.perf_counter() - t0
         st = srv.stats()
+        st["client_submit_s"] = round(t_submit, 4)
+        st["client_wait_s"] = round(t_wait, 4)
     return dt, np.array(lat), st
 
 
@@ -671,8 +725,7 @@ def run_serve(args):
         k = int(rng.integers(len(partners) if op == "masked_mul" else len(mats)))
         plan.append((op, k, 32 if op == "spmm" else 0))
     window = 1024
-    max_floats = max((A.ncols + A.nrows) * 32 for A in mats)
-    arena = torch.empty(window * max_floats, dtype=torch.float32).pin_memory()
+    arena = torch.empty(512 << 20, dtype=torch.float32).pin_memory()  # 2 GiB ring
     torch.cuda.synchronize()
     out = {"suite": "served_4096_csr", "requests": n_req, "mix": "1/3 SpMV, 1/3 SpMM(32), 1/3 masked multiply",
            "matrices": len(mats), "stored_entries": int(sum(A.nnz for A in mats)),
@@ -683,7 +736,8 @@ def run_serve(args):
         out[mode] = {"ops_per_s": round(n_req / dt, 1), "seconds": round(dt, 3),
                      "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
                      "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
-                     "launches": st["launches"], "batches": st["batches_published"]}
+                     "launches": st["launches"], "batches": st["batches_published"],
+                     "client_submit_s": st["client_submit_s"], "client_wait_s": st["client_wait_s"]}
     out["throughput_ratio_batched_vs_per_call"] = round(
         out["batched"]["ops_per_s"] / out["per_call"]["ops_per_s"], 2)
     # open loop: Poisson arrivals at half of each mode's capacity

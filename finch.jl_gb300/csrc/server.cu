@@ -5,11 +5,17 @@
 // by HBM footprint: a request is admitted when a request slot is free and
 // its input + output fit in the server's device pool; otherwise it waits in
 // the host queue and is admitted as soon as completions free memory.
+// Page-locked buffers are read and written by the device directly: such an
+// output takes no pool memory and needs no copy back.
 //
 // Batched mode (the device-side request loop).  A persistent kernel runs on
-// every SM.  The host publishes admitted requests as work items -- blocks of
-// rows_per_item rows of one request -- into a ring in device memory and then
-// bumps a `published` counter in mapped host memory.  Each block of the
+// every SM.  For each group of admitted requests the host writes one stage
+// record per request into a page-locked ring and launches one stage kernel,
+// which copies page-locked inputs into the pool, writes the slot
+// descriptors and the work items -- blocks of rows_per_item rows of one
+// request -- into device rings, and, from its last block, bumps the
+// `published` counter in mapped host memory.  The host never waits for
+// these copies.  Each block of the
 // kernel claims the next published item with a compare-and-swap on a device
 // counter, computes its rows (8 warps, one row per warp at a time), and the
 // block finishing a request's last item raises that request's status in
@@ -42,6 +48,7 @@ constexpr int SRV_MAX_SLOTS = 4096;
 constexpr int64_t SRV_ITEM_CAP = int64_t(1) << 20;
 constexpr int SRV_MAX_MATRICES = 1 << 16;
 constexpr int SRV_THREADS = 256;
+constexpr int SRV_MAX_TAKE = 8;  // work items one claim may take
 
 struct __align__(16) DevMatrix {
   const int32_t* ptr;
@@ -89,6 +96,8 @@ struct SrvArgs {
   HostShared* host;                 // device alias of the mapped block
   unsigned long long* next_item;    // device counter
   unsigned int* done_items;         // per slot
+  unsigned int* exit_epoch;         // device word: the last launch told to exit
+  unsigned int epoch;               // this launch
   uint64_t idle_ns;
 };
 
@@ -108,16 +117,15 @@ __device__ __forceinline__ void st_release_sys(volatile uint64_t* p, uint64_t v)
   asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// y[r] = sum_j A[r,j] x[j]
-__device__ void srv_spmv_row(const DevMatrix& A, const float* __restrict__ x, float* __restrict__ y,
-                             int r, int lane) {
+// y[r] = sum_j A[r,j] x[j]; returns y[r] in every lane
+__device__ float srv_spmv_row(const DevMatrix& A, const float* __restrict__ x, int r, int lane) {
   const int q0 = __ldg(A.ptr + r) - A.base, q1 = __ldg(A.ptr + r + 1) - A.base;
   float acc = 0.f;
   for (int q = q0 + lane; q < q1; q += 32)
     acc = __fmaf_rn(__ldg(A.val + q), __ldcg(x + (__ldg(A.idx + q) - A.base)), acc);
 #pragma unroll
   for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
-  if (lane == 0) y[r] = acc;
+  return acc;
 }
 
 // C[r, 0:nk] = sum_j A[r,j] B[j, 0:nk]; nk a multiple of 4, at most 128.
@@ -166,67 +174,188 @@ __device__ void srv_masked_row(const DevMatrix& A, const DevMatrix& Bm, float* _
   }
 }
 
+constexpr int SRV_YCHUNK = 256;  // SpMV rows staged in shared memory per store pass
+
 __device__ void srv_process(const SrvArgs& a, const DevSlot& s, const DevItem& it) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const DevMatrix A = ldcg_struct(a.mats + s.matrix);
+  if (s.op == FGB_REQ_SPMV) {
+    // one value per row: staged so that the block stores whole lines (the
+    // output may live in host memory, where scattered 4-byte stores are slow)
+    __shared__ float s_y[SRV_YCHUNK];
+    for (int r0 = (int)it.row_begin; r0 < (int)it.row_end; r0 += SRV_YCHUNK) {
+      const int n = min(SRV_YCHUNK, (int)it.row_end - r0);
+      for (int k = warp; k < n; k += SRV_THREADS / 32) {
+        const float y = srv_spmv_row(A, s.in, r0 + k, lane);
+        if (lane == 0) s_y[k] = y;
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < n; k += SRV_THREADS) s.out[r0 + k] = s_y[k];
+      __syncthreads();
+    }
+    return;
+  }
   const DevMatrix Bm = s.op == FGB_REQ_MASKED_MUL ? ldcg_struct(a.mats + s.matrix_b) : A;
   for (int r = (int)it.row_begin + warp; r < (int)it.row_end; r += SRV_THREADS / 32) {
-    if (s.op == FGB_REQ_SPMV) srv_spmv_row(A, s.in, s.out, r, lane);
-    else if (s.op == FGB_REQ_SPMM) srv_spmm_row(A, s.in, s.out, s.nk, r, lane);
+    if (s.op == FGB_REQ_SPMM) srv_spmm_row(A, s.in, s.out, s.nk, r, lane);
     else srv_masked_row(A, Bm, s.out, r, lane);
   }
 }
 
 // The device-side request loop.
-__global__ void __launch_bounds__(SRV_THREADS) serve_loop_k(SrvArgs a) {
+// 5 blocks' worth of registers per SM at most: with the default 4 blocks per
+// SM there is room left for the stage kernel to run beside the loop.
+//
+// Idle exit is collective: a block leaves only when the shared item counter
+// has not moved for idle_ns (no block claimed anything), and the first block
+// to see that raises exit_epoch to this launch's epoch so that every block
+// leaves.  The host relaunches when it sees the kernel finished with work
+// outstanding; a kernel never keeps running on a few blocks.
+__global__ void __launch_bounds__(SRV_THREADS, 5) serve_loop_k(SrvArgs a) {
   __shared__ unsigned long long s_item;
+  __shared__ unsigned s_take;
   __shared__ int s_exit;
   uint64_t cached_pub = 0;
   uint64_t idle_since = globaltimer();
+  unsigned long long last_cur = ~0ull;
   while (true) {
     if (threadIdx.x == 0) {
       int exit_now = 0;
-      unsigned long long got = ~0ull;
+      unsigned long long got = 0;
+      unsigned take = 0;
       unsigned backoff = 64;
+      unsigned long long cur = *(volatile unsigned long long*)a.next_item;
       while (true) {
-        const unsigned long long cur = *(volatile unsigned long long*)a.next_item;
         if (cur < cached_pub) {
-          if (atomicCAS(a.next_item, cur, cur + 1) == cur) {
+          // guided claiming: a share of the backlog, so that a deep backlog
+          // costs few compare-and-swaps on the shared counter
+          const unsigned long long share = (cached_pub - cur) / (2ull * gridDim.x);
+          const unsigned want = share < 1 ? 1u : (share > SRV_MAX_TAKE ? (unsigned)SRV_MAX_TAKE : (unsigned)share);
+          const unsigned long long old = atomicCAS(a.next_item, cur, cur + want);
+          if (old == cur) {
             got = cur;
+            take = want;
             break;
           }
-          continue;  // lost the race for item `cur`; try the next one
+          cur = old;  // lost the race: retry from the counter's current value
+          continue;
         }
         cached_pub = ld_acquire_sys(&a.host->published);
         if (cached_pub > cur) continue;
-        if (a.host->stop) { exit_now = 1; break; }
-        if (globaltimer() - idle_since > a.idle_ns) { exit_now = 1; break; }
+        if (a.host->stop || *(volatile unsigned*)a.exit_epoch >= a.epoch) { exit_now = 1; break; }
+        const uint64_t now = globaltimer();
+        if (cur != last_cur) {  // another block claimed an item: not idle
+          last_cur = cur;
+          idle_since = now;
+        }
+        if (now - idle_since > a.idle_ns) {
+          atomicMax(a.exit_epoch, a.epoch);
+          exit_now = 1;
+          break;
+        }
         __nanosleep(backoff);
         if (backoff < 4096) backoff <<= 1;
+        cur = *(volatile unsigned long long*)a.next_item;
       }
       s_item = got;
+      s_take = take;
       s_exit = exit_now;
     }
     __syncthreads();
     const int exit_now = s_exit;
-    const unsigned long long item = s_item;
+    const unsigned long long first = s_item;
+    const unsigned take = s_take;
     __syncthreads();
     if (exit_now) return;
-    const DevItem it = ldcg_struct(a.items + item % SRV_ITEM_CAP);
-    const DevSlot s = ldcg_struct(a.slots + it.slot);
-    srv_process(a, s, it);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      const unsigned done = atomicAdd(a.done_items + it.slot, 1u) + 1u;
-      if ((int)done == s.n_items) {
-        // re-arm the slot's counter before the host can see the request done
-        // (and hand the slot to the next request)
-        a.done_items[it.slot] = 0u;
-        __threadfence_system();
-        st_release_sys(&a.host->status[it.slot], s.seq);
+    for (unsigned k = 0; k < take; ++k) {
+      const DevItem it = ldcg_struct(a.items + (first + k) % SRV_ITEM_CAP);
+      const DevSlot s = ldcg_struct(a.slots + it.slot);
+      srv_process(a, s, it);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(a.done_items + it.slot, 1u) + 1u;
+        if ((int)done == s.n_items) {
+          // re-arm the slot's counter before the host can see the request done
+          // (and hand the slot to the next request)
+          a.done_items[it.slot] = 0u;
+          __threadfence_system();
+          st_release_sys(&a.host->status[it.slot], s.seq);
+        }
       }
-      idle_since = globaltimer();
+    }
+    if (threadIdx.x == 0) idle_since = globaltimer();
+  }
+}
+
+// One admitted request, written by the host into a page-locked ring and read
+// by the stage kernel.
+struct __align__(16) StageReq {
+  DevSlot desc;
+  const float* src;  // device alias of a page-locked input (null: none or copied by DMA)
+  float* dst;        // the input's pool range
+  uint64_t bytes;    // bytes the stage kernel copies from src to dst
+  uint64_t item0;    // ring index of the request's first work item
+  int32_t slot, rows;
+  int32_t rows_per_item, pad;
+};
+
+constexpr int STAGE_CAP = 2 * SRV_MAX_SLOTS;
+constexpr uint32_t STAGE_CHUNK = 32u << 10;  // input bytes per stage block
+constexpr int STAGE_THREADS = 256;
+
+struct StageArgs {
+  const StageReq* reqs;  // device alias of the ring
+  uint32_t first, cap;
+  DevSlot* slots;
+  DevItem* items;
+  unsigned* blocks_done;  // device counter, 0 between launches
+  HostShared* host;
+  uint64_t publish_to;
+};
+
+// Grid (x: STAGE_CHUNK input chunks, y: requests of the group).  Block x == 0
+// of each request also writes its slot descriptor and work items.  The last
+// block to finish publishes the group's items to the device loop.
+__global__ void __launch_bounds__(STAGE_THREADS, 8) serve_stage_k(StageArgs g) {
+  const StageReq* rq = g.reqs + (g.first + blockIdx.y) % g.cap;
+  if (blockIdx.x == 0) {
+    const int slot = rq->slot;
+    if (threadIdx.x < (int)(sizeof(DevSlot) / 16))
+      __stcg(reinterpret_cast<uint4*>(g.slots + slot) + threadIdx.x,
+             reinterpret_cast<const uint4*>(&rq->desc)[threadIdx.x]);
+    const int rpi = rq->rows_per_item, rows = rq->rows;
+    const uint64_t item0 = rq->item0;
+    for (int b = threadIdx.x; b < rq->desc.n_items; b += blockDim.x) {
+      const uint4 it = make_uint4((uint32_t)slot, (uint32_t)(b * rpi), (uint32_t)min(rows, (b + 1) * rpi), 0u);
+      __stcg(reinterpret_cast<uint4*>(g.items + (item0 + b) % SRV_ITEM_CAP), it);
+    }
+  }
+  const uint64_t bytes = rq->bytes, c0 = (uint64_t)blockIdx.x * STAGE_CHUNK;
+  if (c0 < bytes) {
+    const uint64_t len = bytes - c0 < STAGE_CHUNK ? bytes - c0 : STAGE_CHUNK;
+    const char* src = reinterpret_cast<const char*>(rq->src) + c0;
+    char* dst = reinterpret_cast<char*>(rq->dst) + c0;
+    uint64_t done = 0;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+      const uint64_t n16 = len >> 4;
+      const uint4* s4 = reinterpret_cast<const uint4*>(src);
+      uint4* d4 = reinterpret_cast<uint4*>(dst);
+      for (uint64_t k = threadIdx.x; k < n16; k += blockDim.x) __stcg(d4 + k, __ldg(s4 + k));
+      done = n16 << 4;
+    }
+    const uint32_t* s1 = reinterpret_cast<const uint32_t*>(src + done);  // inputs are float arrays
+    uint32_t* d1 = reinterpret_cast<uint32_t*>(dst + done);
+    for (uint64_t k = threadIdx.x; k < (len - done) >> 2; k += blockDim.x) __stcg(d1 + k, __ldg(s1 + k));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned total = gridDim.x * gridDim.y;
+    if (atomicAdd(g.blocks_done, 1u) == total - 1) {
+      *g.blocks_done = 0u;  // re-armed for the next stage launch (same stream)
+      __threadfence_system();
+      st_release_sys(&g.host->published, g.publish_to);
     }
   }
 }
@@ -250,7 +379,8 @@ struct Ticket {
   uint64_t item0 = 0;  // ring index of the request's first item
   uint64_t seq = 0;
   float* out_mapped = nullptr;  // device alias of a pinned output: written in place, no copy back
-  std::chrono::steady_clock::time_point t_submit, t_done;
+  const float* in_mapped = nullptr;  // device alias of a pinned input: copied by the stage kernel
+  std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
   int state = 0;  // 0 queued, 1 in flight, 2 done, 3 failed
   int status = FGB_OK;
 };
@@ -310,12 +440,14 @@ struct fgb_server {
   char* pool = nullptr;
   HostShared* host = nullptr;   // host view
   HostShared* host_dev = nullptr;  // device view
-  DevItem* stage_items = nullptr;  // pinned staging
-  DevSlot* stage_slots = nullptr;
-  unsigned* zero_word = nullptr;   // pinned 0, copied to reset a slot's done counter
+  StageReq* stage = nullptr;       // page-locked ring of stage records (host view)
+  StageReq* stage_dev = nullptr;   // device view
+  uint64_t stage_head = 0;         // records written so far
+  std::vector<uint64_t> stage_pub; // per ring position: the published count its group reaches
   cudaStream_t copy_stream = nullptr, kernel_stream = nullptr;
   cudaEvent_t kernel_done = nullptr;
   bool kernel_launched = false;
+  unsigned loop_epoch = 0;         // launches of the device loop so far
   // host bookkeeping
   std::vector<DevMatrix> mats;
   std::mutex mu;
@@ -323,8 +455,14 @@ struct fgb_server {
   std::deque<uint64_t> queue;
   std::unordered_map<uint64_t, Ticket> tickets;
   std::vector<uint64_t> slot_owner;  // ticket per slot (0 = free)
+  std::vector<int> free_slots;       // stack of slots with slot_owner == 0
   std::vector<uint64_t> slot_seq;
-  std::vector<uint64_t> inflight;
+  struct Inflight {
+    uint64_t id, seq, item0;
+    int slot;
+  };
+  std::vector<Inflight> inflight;  // admitted, not yet complete (admission order); worker only
+  std::vector<uint64_t> done_scratch;
   uint64_t next_ticket = 1;
   uint64_t published = 0;
   PoolAllocator* alloc = nullptr;
@@ -359,6 +497,8 @@ SrvArgs make_args(fgb_server* s) {
   a.host = s->host_dev;
   a.next_item = s->d_next;
   a.done_items = s->d_done;
+  a.exit_epoch = (unsigned*)(s->d_next + 2);
+  a.epoch = s->loop_epoch;
   a.idle_ns = (uint64_t)s->cfg.idle_exit_us * 1000ull;
   return a;
 }
@@ -372,8 +512,11 @@ void finish(fgb_server* s, Ticket& t, int status) {
   t.state = status == FGB_OK ? 2 : 3;
   t.status = status;
   t.t_done = std::chrono::steady_clock::now();
+  s->stats.queue_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t.t_admit - t.t_submit).count();
+  s->stats.service_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t.t_done - t.t_admit).count();
   if (t.slot >= 0) {
     s->slot_owner[t.slot] = 0;
+    s->free_slots.push_back(t.slot);
     t.slot = -1;
   }
   if (t.in_bytes) s->alloc->release(t.in_off, t.in_bytes);
@@ -411,21 +554,27 @@ void run_per_call(fgb_server* s, std::vector<uint64_t>& batch, std::unique_lock<
 void worker_main(fgb_server* s) {
   cudaSetDevice(s->ctx->device);
   std::unique_lock<std::mutex> lk(s->mu);
+  using clk = std::chrono::steady_clock;
+  auto ns_since = [](clk::time_point t0) {
+    return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(clk::now() - t0).count();
+  };
   while (!s->quit.load()) {
     bool progressed = false;
+    s->stats.iterations++;
+    const auto t_admit = clk::now();
     // A) admission: FIFO while a slot and pool memory are available
     std::vector<uint64_t> admitted;
     // ring positions still owned by in-flight requests start at the oldest one
     uint64_t ring_tail = s->published;
-    for (uint64_t id : s->inflight) ring_tail = std::min(ring_tail, s->tickets[id].item0);
+    for (const auto& f : s->inflight) ring_tail = std::min(ring_tail, f.item0);
     int64_t new_items = 0;
     while (!s->queue.empty() && s->worker_error == FGB_OK) {
       Ticket& t = s->tickets[s->queue.front()];
       if ((int64_t)(s->published - ring_tail) + new_items + t.n_items > SRV_ITEM_CAP) break;
-      int slot = -1;
-      for (int k = 0; k < s->cfg.max_inflight; ++k)
-        if (!s->slot_owner[k]) { slot = k; break; }
-      if (slot < 0) break;
+      if (s->free_slots.empty()) break;
+      // the stage record this request would overwrite must have been consumed
+      if (s->stage_pub[(s->stage_head + admitted.size()) % STAGE_CAP] > s->host->published) break;
+      const int slot = s->free_slots.back();
       size_t in_off = 0, out_off = 0;
       if (t.in_bytes && !s->alloc->alloc(t.in_bytes, &in_off)) break;
       if (t.out_bytes && !s->alloc->alloc(t.out_bytes, &out_off)) {
@@ -437,8 +586,10 @@ void worker_main(fgb_server* s) {
       t.out_off = out_off;
       t.seq = ++s->slot_seq[slot];
       t.state = 1;
+      t.t_admit = clk::now();
       t.item0 = s->published + new_items;
       new_items += t.n_items;
+      s->free_slots.pop_back();
       s->slot_owner[slot] = s->queue.front();
       admitted.push_back(s->queue.front());
       s->queue.pop_front();
@@ -449,57 +600,62 @@ void worker_main(fgb_server* s) {
         run_per_call(s, admitted, lk);
         continue;
       }
-      // copy inputs, write slot descriptors and items, then publish
+      // one stage record per request, then one stage kernel for the group;
+      // pageable inputs go by DMA on the same stream first
       cudaError_t e = cudaSuccess;
       int64_t n_new = 0;
+      const uint64_t first = s->stage_head % STAGE_CAP;
+      uint64_t max_chunks = 1;
       for (uint64_t id : admitted) {
         Ticket& t = s->tickets[id];
-        if (t.in_bytes && e == cudaSuccess)
-          e = cudaMemcpyAsync(s->pool + t.in_off, t.req.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
-        s->stage_slots[t.slot] = DevSlot{t.req.op, t.req.matrix, t.req.matrix_b, t.req.nk,
-                                        (const float*)(s->pool + t.in_off),
-                                        t.out_mapped ? t.out_mapped : (float*)(s->pool + t.out_off),
-                                        (int32_t)t.n_items, 0, t.seq};
-        for (int64_t b = 0; b < t.n_items; ++b) {
-          const int64_t pos = (s->published + n_new) % SRV_ITEM_CAP;
-          s->stage_items[pos] = DevItem{(uint32_t)t.slot, (uint32_t)(b * s->cfg.rows_per_item),
-                                        (uint32_t)std::min<int64_t>(t.rows, (b + 1) * s->cfg.rows_per_item), 0};
-          ++n_new;
-        }
+        float* in_pool = (float*)(s->pool + t.in_off);
+        if (t.in_bytes && !t.in_mapped && e == cudaSuccess)
+          e = cudaMemcpyAsync(in_pool, t.req.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
+        StageReq& rq = s->stage[s->stage_head % STAGE_CAP];
+        rq.desc = DevSlot{t.req.op, t.req.matrix, t.req.matrix_b, t.req.nk, in_pool,
+                          t.out_mapped ? t.out_mapped : (float*)(s->pool + t.out_off),
+                          (int32_t)t.n_items, 0, t.seq};
+        rq.src = t.in_mapped;
+        rq.dst = in_pool;
+        rq.bytes = t.in_mapped ? t.in_bytes : 0;
+        rq.item0 = t.item0;
+        rq.slot = t.slot;
+        rq.rows = (int32_t)t.rows;
+        rq.rows_per_item = s->cfg.rows_per_item;
+        rq.pad = 0;
+        max_chunks = std::max<uint64_t>(max_chunks, (rq.bytes + STAGE_CHUNK - 1) / STAGE_CHUNK);
+        n_new += t.n_items;
+        ++s->stage_head;
       }
-      // one copy of the slot table (in-flight slots are rewritten unchanged;
-      // the device re-arms each slot's done counter itself)
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->d_slots, s->stage_slots, sizeof(DevSlot) * s->cfg.max_inflight,
-                            cudaMemcpyHostToDevice, s->copy_stream);
-      // the new items occupy ring positions [published, published + n_new)
-      const int64_t p0 = s->published % SRV_ITEM_CAP;
-      const int64_t first = std::min<int64_t>(n_new, SRV_ITEM_CAP - p0);
-      if (e == cudaSuccess && first > 0)
-        e = cudaMemcpyAsync(s->d_items + p0, s->stage_items + p0, sizeof(DevItem) * first, cudaMemcpyHostToDevice, s->copy_stream);
-      if (e == cudaSuccess && n_new > first)
-        e = cudaMemcpyAsync(s->d_items, s->stage_items, sizeof(DevItem) * (n_new - first), cudaMemcpyHostToDevice, s->copy_stream);
-      lk.unlock();
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
-      lk.lock();
+      const uint64_t publish_to = s->published + n_new;
+      for (uint64_t k = 0; k < admitted.size(); ++k) s->stage_pub[(first + k) % STAGE_CAP] = publish_to;
+      if (e == cudaSuccess) {
+        StageArgs g{s->stage_dev, (uint32_t)first, (uint32_t)STAGE_CAP, s->d_slots, s->d_items,
+                    (unsigned*)(s->d_next + 1), s->host_dev, publish_to};
+        serve_stage_k<<<dim3((unsigned)max_chunks, (unsigned)admitted.size()), STAGE_THREADS, 0, s->copy_stream>>>(g);
+        e = cudaGetLastError();
+      }
       if (e != cudaSuccess) {
-        fail_worker(s, FGB_ECUDA, "admission copies", e);
+        fail_worker(s, FGB_ECUDA, "stage launch", e);
         for (uint64_t id : admitted) finish(s, s->tickets[id], FGB_ECUDA);
         s->cv_done.notify_all();
         continue;
       }
-      s->published += n_new;
-      std::atomic_thread_fence(std::memory_order_release);
-      s->host->published = s->published;  // the device loop may now claim them
-      for (uint64_t id : admitted) s->inflight.push_back(id);
+      s->published = publish_to;  // the stage kernel makes it visible to the device loop
+      for (uint64_t id : admitted) {
+        const Ticket& t = s->tickets[id];
+        s->inflight.push_back({id, t.seq, t.item0, t.slot});
+      }
       s->stats.batches_published++;
     }
+    s->stats.admit_ns += ns_since(t_admit);
     // B) keep the device loop running while work is outstanding
     if (s->cfg.mode == FGB_SERVE_BATCHED && !s->inflight.empty()) {
       const bool running = s->kernel_launched && cudaEventQuery(s->kernel_done) == cudaErrorNotReady;
       if (!running) {
         cudaGetLastError();
         const int grid = s->ctx->num_sms * s->cfg.blocks_per_sm;
+        ++s->loop_epoch;
         serve_loop_k<<<grid, SRV_THREADS, 0, s->kernel_stream>>>(make_args(s));
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaEventRecord(s->kernel_done, s->kernel_stream);
@@ -508,14 +664,25 @@ void worker_main(fgb_server* s) {
         s->stats.launches++;
       }
     }
-    // C) completions: copy outputs back, free slots and pool memory
+    // C) completions: the status words are scanned without the lock (the
+    // in-flight list belongs to this thread, and submitters and waiters must
+    // not queue behind the scan); copies back and releases take it again
     if (!s->inflight.empty()) {
-      std::vector<uint64_t> done, still;
-      for (uint64_t id : s->inflight) {
-        Ticket& t = s->tickets[id];
-        if (s->host->status[t.slot] == t.seq) done.push_back(id); else still.push_back(id);
+      lk.unlock();
+      const auto t_scan = clk::now();
+      std::vector<uint64_t>& done = s->done_scratch;
+      done.clear();
+      size_t keep = 0;
+      for (size_t k = 0; k < s->inflight.size(); ++k) {
+        const auto f = s->inflight[k];
+        if (s->host->status[f.slot] == f.seq) done.push_back(f.id); else s->inflight[keep++] = f;
       }
+      s->inflight.resize(keep);
+      const uint64_t scan_ns = ns_since(t_scan);
+      lk.lock();
+      s->stats.scan_ns += scan_ns;
       if (!done.empty()) {
+        const auto t_fin = clk::now();
         progressed = true;
         std::atomic_thread_fence(std::memory_order_acquire);
         cudaError_t e = cudaSuccess;
@@ -534,8 +701,8 @@ void worker_main(fgb_server* s) {
         }
         if (e != cudaSuccess) fail_worker(s, FGB_ECUDA, "result copies", e);
         for (uint64_t id : done) finish(s, s->tickets[id], e == cudaSuccess ? FGB_OK : FGB_ECUDA);
-        s->inflight.swap(still);
         s->cv_done.notify_all();
+        s->stats.finish_ns += ns_since(t_fin);
       }
     }
     if (!progressed) {
@@ -563,6 +730,13 @@ int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg_in, fgb_server*
   if (cfg.max_inflight > SRV_MAX_SLOTS) return set_error(FGB_EINVAL, "fgb_server_create: max_inflight above %d", SRV_MAX_SLOTS);
   if (cfg.rows_per_item <= 0) cfg.rows_per_item = 64;
   if (cfg.blocks_per_sm <= 0) cfg.blocks_per_sm = 4;
+  {
+    // leave one block's room per SM for the stage kernel
+    int occ = 0;
+    FGB_CUDA_TRY(cudaSetDevice(ctx->device));
+    FGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_loop_k, SRV_THREADS, 0));
+    cfg.blocks_per_sm = std::max(1, std::min(cfg.blocks_per_sm, occ - 1));
+  }
   if (cfg.idle_exit_us <= 0) cfg.idle_exit_us = 20000;
   if (cfg.mode != FGB_SERVE_BATCHED && cfg.mode != FGB_SERVE_PER_CALL)
     return set_error(FGB_EINVAL, "fgb_server_create: unknown mode");
@@ -577,10 +751,8 @@ int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg_in, fgb_server*
   if (e == cudaSuccess) e = cudaMalloc((void**)&s->pool, cfg.pool_bytes);
   if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->host, sizeof(HostShared), cudaHostAllocMapped | cudaHostAllocPortable);
   if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->host_dev, s->host, 0);
-  if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->stage_items, sizeof(DevItem) * SRV_ITEM_CAP, cudaHostAllocPortable);
-  if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->stage_slots, sizeof(DevSlot) * SRV_MAX_SLOTS, cudaHostAllocPortable);
-  if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->zero_word, 256, cudaHostAllocPortable);
-  if (e == cudaSuccess) memset(s->zero_word, 0, 256);
+  if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->stage, sizeof(StageReq) * STAGE_CAP, cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&s->stage_dev, s->stage, 0);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->kernel_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->kernel_done, cudaEventDisableTiming);
@@ -604,7 +776,9 @@ int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg_in, fgb_server*
   s->d_done = (unsigned*)p;
   s->alloc = new PoolAllocator(cfg.pool_bytes);
   s->slot_owner.assign(cfg.max_inflight, 0);
+  for (int k = cfg.max_inflight - 1; k >= 0; --k) s->free_slots.push_back(k);
   s->slot_seq.assign(cfg.max_inflight, 0);
+  s->stage_pub.assign(STAGE_CAP, 0);
   s->worker = std::thread(worker_main, s);
   *out = s;
   return FGB_OK;
@@ -628,9 +802,32 @@ int fgb_server_register(fgb_server* s, const fgb_sparse* A, int32_t* id) {
   return FGB_OK;
 }
 
-int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
-  if (!s || !r || !ticket) return set_error(FGB_EINVAL, "fgb_server_submit: null argument");
-  std::lock_guard<std::mutex> lk(s->mu);
+}  // extern "C"
+
+// Device aliases of page-locked request buffers (null for pageable memory);
+// looked up before the server lock is taken.
+struct MappedBufs {
+  const float* in = nullptr;
+  float* out = nullptr;
+};
+
+static void* device_alias(const void* p) {
+  cudaPointerAttributes attr{};
+  if (p && cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeHost)
+    return attr.devicePointer;
+  cudaGetLastError();
+  return nullptr;
+}
+
+static MappedBufs probe_mapped(const fgb_request* r) {
+  MappedBufs m;
+  m.out = (float*)device_alias(r->output);
+  if (r->op != FGB_REQ_MASKED_MUL) m.in = (const float*)device_alias(r->input);
+  return m;
+}
+
+// Validates and queues one request; the caller holds s->mu.
+static int submit_locked(fgb_server* s, const fgb_request* r, const MappedBufs& mb, uint64_t* ticket) {
   if (s->worker_error) return set_error(s->worker_error, "fgb_server_submit: server failed: %s", s->worker_msg);
   if (r->matrix < 0 || r->matrix >= (int)s->mats.size())
     return set_error(FGB_EINVAL, "fgb_server_submit: unknown matrix %d", r->matrix);
@@ -655,15 +852,13 @@ int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
   t.n_items = (A.nrows + s->cfg.rows_per_item - 1) / s->cfg.rows_per_item;
   t.in_bytes = req_in_bytes(s, *r);
   t.out_bytes = req_out_bytes(s, *r, A.nnz);
-  // a page-locked output is written by the device in place (no copy back)
-  cudaPointerAttributes attr{};
-  if (cudaPointerGetAttributes(&attr, r->output) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
-      attr.devicePointer) {
-    t.out_mapped = (float*)attr.devicePointer;
+  // a page-locked output is written by the device in place (no copy back);
+  // a page-locked input is copied into the pool by the stage kernel
+  if (mb.out) {
+    t.out_mapped = mb.out;
     t.out_bytes = 0;
-  } else {
-    cudaGetLastError();
   }
+  if (t.in_bytes) t.in_mapped = mb.in;
   if (t.in_bytes + t.out_bytes + 512 > s->cfg.pool_bytes)
     return set_error(FGB_ENOMEM, "fgb_server_submit: request needs %zu bytes, pool holds %zu",
                      t.in_bytes + t.out_bytes, s->cfg.pool_bytes);
@@ -673,13 +868,12 @@ int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
   s->queue.push_back(id);
   s->stats.submitted++;
   *ticket = id;
-  s->cv_work.notify_one();
   return FGB_OK;
 }
 
-int fgb_server_wait(fgb_server* s, uint64_t ticket, int32_t timeout_ms, double* latency_s) {
-  if (!s) return set_error(FGB_EINVAL, "fgb_server_wait: null server");
-  std::unique_lock<std::mutex> lk(s->mu);
+// Waits for one ticket; the caller holds `lk` on s->mu.
+static int wait_locked(fgb_server* s, std::unique_lock<std::mutex>& lk, uint64_t ticket,
+                       int32_t timeout_ms, double* latency_s) {
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return set_error(FGB_EINVAL, "fgb_server_wait: unknown ticket %llu", (unsigned long long)ticket);
   const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
@@ -692,6 +886,53 @@ int fgb_server_wait(fgb_server* s, uint64_t ticket, int32_t timeout_ms, double* 
   s->tickets.erase(it);
   if (latency_s) *latency_s = std::chrono::duration<double>(t.t_done - t.t_submit).count();
   if (t.status != FGB_OK) return set_error(t.status, "fgb_server_wait: request failed: %s", s->worker_msg);
+  return FGB_OK;
+}
+
+extern "C" {
+
+int fgb_server_submit(fgb_server* s, const fgb_request* r, uint64_t* ticket) {
+  if (!s || !r || !ticket) return set_error(FGB_EINVAL, "fgb_server_submit: null argument");
+  const MappedBufs mb = probe_mapped(r);
+  std::lock_guard<std::mutex> lk(s->mu);
+  const int rc = submit_locked(s, r, mb, ticket);
+  if (rc == FGB_OK) s->cv_work.notify_one();
+  return rc;
+}
+
+int fgb_server_submit_batch(fgb_server* s, const fgb_request* reqs, int32_t n, uint64_t* tickets,
+                            int32_t* n_accepted) {
+  if (!s || (n > 0 && (!reqs || !tickets)) || !n_accepted)
+    return set_error(FGB_EINVAL, "fgb_server_submit_batch: null argument");
+  std::vector<MappedBufs> mb((size_t)std::max(n, 0));
+  for (int32_t k = 0; k < n; ++k) mb[k] = probe_mapped(reqs + k);
+  std::lock_guard<std::mutex> lk(s->mu);
+  int rc = FGB_OK;
+  int32_t k = 0;
+  for (; k < n; ++k)
+    if ((rc = submit_locked(s, reqs + k, mb[k], tickets + k)) != FGB_OK) break;
+  *n_accepted = k;
+  if (k) s->cv_work.notify_one();
+  return rc;
+}
+
+int fgb_server_wait(fgb_server* s, uint64_t ticket, int32_t timeout_ms, double* latency_s) {
+  if (!s) return set_error(FGB_EINVAL, "fgb_server_wait: null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  return wait_locked(s, lk, ticket, timeout_ms, latency_s);
+}
+
+int fgb_server_wait_batch(fgb_server* s, const uint64_t* tickets, int32_t n, int32_t timeout_ms,
+                          double* latencies_s) {
+  if (!s || (n > 0 && !tickets)) return set_error(FGB_EINVAL, "fgb_server_wait_batch: null argument");
+  std::unique_lock<std::mutex> lk(s->mu);
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
+  for (int32_t k = 0; k < n; ++k) {
+    const auto left = std::chrono::duration_cast<std::chrono::milliseconds>(deadline - std::chrono::steady_clock::now());
+    const int rc = wait_locked(s, lk, tickets[k], (int32_t)std::max<int64_t>(0, left.count()),
+                               latencies_s ? latencies_s + k : nullptr);
+    if (rc) return rc;
+  }
   return FGB_OK;
 }
 
@@ -719,9 +960,7 @@ int fgb_server_destroy(fgb_server* s) {
   if (s->kernel_done) cudaEventDestroy(s->kernel_done);
   if (s->kernel_stream) cudaStreamDestroy(s->kernel_stream);
   if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
-  if (s->stage_items) cudaFreeHost(s->stage_items);
-  if (s->stage_slots) cudaFreeHost(s->stage_slots);
-  if (s->zero_word) cudaFreeHost(s->zero_word);
+  if (s->stage) cudaFreeHost(s->stage);
   if (s->host) cudaFreeHost(s->host);
   if (s->pool) cudaFree(s->pool);
   if (s->dev_state) cudaFree(s->dev_state);

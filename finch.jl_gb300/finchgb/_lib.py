@@ -78,7 +78,9 @@ class FgbRequest(ctypes.Structure):
 
 class FgbServerStats(ctypes.Structure):
     _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("launches", c_uint64),
-                ("batches_published", c_uint64), ("pool_used", c_uint64)]
+                ("batches_published", c_uint64), ("pool_used", c_uint64), ("admit_ns", c_uint64),
+                ("scan_ns", c_uint64), ("finish_ns", c_uint64), ("iterations", c_uint64),
+                ("queue_ns", c_uint64), ("service_ns", c_uint64)]
 
 
 class FgbSparse(ctypes.Structure):
@@ -144,6 +146,10 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_server_register": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(c_int32)]),
     "fgb_server_submit": (c_int, [c_void_p, POINTER(FgbRequest), POINTER(c_uint64)]),
     "fgb_server_wait": (c_int, [c_void_p, c_uint64, c_int32, POINTER(c_double)]),
+    "fgb_server_submit_batch": (c_int, [c_void_p, POINTER(FgbRequest), c_int32, POINTER(c_uint64),
+                                        POINTER(c_int32)]),
+    "fgb_server_wait_batch": (c_int, [c_void_p, POINTER(c_uint64), c_int32, c_int32,
+                                      POINTER(c_double)]),
     "fgb_server_stats_get": (c_int, [c_void_p, POINTER(FgbServerStats)]),
     "fgb_server_destroy": (c_int, [c_void_p]),
 }

@@ -69,6 +69,30 @@ class Server:
         self._pending[t.value] = (inp, out)  # keep the buffers alive
         return t.value
 
+    @staticmethod
+    def request(op: str, matrix: int, inp, out, matrix_b: int = -1, nk: int = 0) -> L.FgbRequest:
+        return L.FgbRequest(OPS[op], matrix, matrix_b, nk, _hptr(inp), _hptr(out))
+
+    def submit_batch(self, reqs) -> list[int]:
+        """Queues a ctypes array (or list) of FgbRequest under one lock."""
+        n = len(reqs)
+        arr = reqs if isinstance(reqs, ctypes.Array) else (L.FgbRequest * n)(*reqs)
+        tickets = (ctypes.c_uint64 * n)()
+        acc = ctypes.c_int32()
+        rc = self.lib.fgb_server_submit_batch(self.h, arr, n, tickets, ctypes.byref(acc))
+        L.check(rc, "fgb_server_submit_batch")
+        return list(tickets)
+
+    def wait_batch(self, tickets, timeout_ms: int = 60_000) -> list[float]:
+        n = len(tickets)
+        t = (ctypes.c_uint64 * n)(*tickets)
+        lat = (ctypes.c_double * n)()
+        rc = self.lib.fgb_server_wait_batch(self.h, t, n, timeout_ms, lat)
+        L.check(rc, "fgb_server_wait_batch")
+        for x in tickets:
+            self._pending.pop(x, None)
+        return list(lat)
+
     def wait(self, ticket: int, timeout_ms: int = 60_000) -> float:
         """Waits for a ticket; returns its submit-to-result latency in seconds."""
         lat = ctypes.c_double()

@@ -399,7 +399,7 @@ typedef struct fgb_server_config {
   size_t pool_bytes;     /* HBM budget for in-flight inputs/outputs (admission) */
   int32_t max_inflight;  /* request slots, <= 4096 */
   int32_t rows_per_item; /* rows per work item (default 64) */
-  int32_t blocks_per_sm; /* persistent blocks per SM (default 4) */
+  int32_t blocks_per_sm; /* persistent blocks per SM (default 4; capped one below occupancy) */
   int32_t idle_exit_us;  /* device loop exits after this long without work (default 20000) */
   int32_t mode;          /* fgb_serve_mode */
   int32_t reserved;
@@ -416,6 +416,12 @@ typedef struct fgb_request {
 
 typedef struct fgb_server_stats {
   uint64_t submitted, completed, launches, batches_published, pool_used;
+  /* dispatcher time (ns): admitting and staging, scanning for completions,
+   * and releasing completed requests; and its loop iterations */
+  uint64_t admit_ns, scan_ns, finish_ns, iterations;
+  /* summed over completed requests (ns): submit to admission (queueing),
+   * admission to completion seen (service) */
+  uint64_t queue_ns, service_ns;
 } fgb_server_stats;
 
 /* Serving front end for compute() calls on resident tensors.  Admission is by
@@ -426,8 +432,16 @@ typedef struct fgb_server_stats {
 FGB_API int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg, fgb_server** out);
 /* Registers a resident CSR matrix (device buffers, int32 ptr/idx, F32 values). */
 FGB_API int fgb_server_register(fgb_server* srv, const fgb_sparse* A, int32_t* id);
-/* Queues a request; returns at once with a ticket. */
+/* Queues a request; returns at once with a ticket.  A page-locked output
+ * buffer is written by the device in place (no copy back, no pool memory). */
 FGB_API int fgb_server_submit(fgb_server* srv, const fgb_request* req, uint64_t* ticket);
+/* Queues n requests under one lock; *n_accepted of them got tickets (all, or
+ * those before the first rejected one, whose status is returned). */
+FGB_API int fgb_server_submit_batch(fgb_server* srv, const fgb_request* reqs, int32_t n,
+                                    uint64_t* tickets, int32_t* n_accepted);
+/* Waits for n tickets within one overall timeout; latencies_s may be NULL. */
+FGB_API int fgb_server_wait_batch(fgb_server* srv, const uint64_t* tickets, int32_t n,
+                                  int32_t timeout_ms, double* latencies_s);
 /* Waits up to timeout_ms for a ticket (FGB_ETIMEOUT after that); on success
  * the output is in host memory and *latency_s is submit-to-result time. */
 FGB_API int fgb_server_wait(fgb_server* srv, uint64_t ticket, int32_t timeout_ms,

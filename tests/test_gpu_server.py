@@ -21,22 +21,25 @@ def host_csr(A):
             A.val.cpu().numpy())
 
 
-def make_requests(rng, mats, partners, count):
+def make_requests(rng, mats, partners, count, pinned=True):
+    """Pinned outputs are written in place by the device; pageable ones go
+    through pool memory and a copy back, so both paths are exercised."""
+    pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
     reqs = []
     for t in range(count):
         k = int(rng.integers(len(mats)))
         A = mats[k]
         op = ("spmv", "spmm", "masked_mul")[t % 3]
         if op == "spmv":
-            inp = torch.from_numpy(rng.standard_normal(A.ncols).astype(np.float32)).pin_memory()
-            out = torch.empty(A.nrows, dtype=torch.float32).pin_memory()
+            inp = pin(torch.from_numpy(rng.standard_normal(A.ncols).astype(np.float32)))
+            out = pin(torch.empty(A.nrows, dtype=torch.float32))
             reqs.append((op, k, inp, out, -1, 0))
         elif op == "spmm":
-            inp = torch.from_numpy(rng.standard_normal((A.ncols, 32)).astype(np.float32)).pin_memory()
-            out = torch.empty((A.nrows, 32), dtype=torch.float32).pin_memory()
+            inp = pin(torch.from_numpy(rng.standard_normal((A.ncols, 32)).astype(np.float32)))
+            out = pin(torch.empty((A.nrows, 32), dtype=torch.float32))
             reqs.append((op, k, inp, out, -1, 32))
         else:
-            out = torch.empty(A.nnz, dtype=torch.float32).pin_memory()
+            out = pin(torch.empty(A.nnz, dtype=torch.float32))
             reqs.append((op, k, None, out, 1, 0))  # 1: use the partner of matrix k
     return reqs
 
@@ -53,15 +56,21 @@ def library(gpu_lib):
     return mats, partners
 
 
-def run(server_mode, mats, partners, reqs, **kw):
+def run(server_mode, mats, partners, reqs, batch=False, **kw):
     with Server(mode=server_mode, **kw) as srv:
         ids = [srv.register(A) for A in mats]
         pids = [srv.register(B) for B in partners]
-        tickets = []
-        for op, k, inp, out, kb, nk in reqs:
-            tickets.append(srv.submit(op, ids[k], inp, out, matrix_b=pids[k] if kb >= 0 else -1,
-                                      nk=nk))
-        lat = [srv.wait(t) for t in tickets]
+        if batch:
+            recs = [srv.request(op, ids[k], inp, out, matrix_b=pids[k] if kb >= 0 else -1, nk=nk)
+                    for op, k, inp, out, kb, nk in reqs]
+            tickets = srv.submit_batch(recs)
+            lat = srv.wait_batch(tickets)
+        else:
+            tickets = []
+            for op, k, inp, out, kb, nk in reqs:
+                tickets.append(srv.submit(op, ids[k], inp, out,
+                                          matrix_b=pids[k] if kb >= 0 else -1, nk=nk))
+            lat = [srv.wait(t) for t in tickets]
         st = srv.stats()
     return lat, st
 
@@ -106,11 +115,31 @@ def test_same_alone_and_in_the_mix(library):
 def test_admission_queues_when_pool_is_small(library):
     mats, partners = library
     rng = np.random.default_rng(2)
-    reqs = make_requests(rng, mats, partners, 30)
+    reqs = make_requests(rng, mats, partners, 30, pinned=False)
     need = max(r[3].numel() * 4 + (0 if r[2] is None else r[2].numel() * 4) for r in reqs)
     lat, st = run("batched", mats, partners, reqs, pool_bytes=2 * need + 4096, max_inflight=4)
     assert st["completed"] == 30 and st["pool_used"] == 0
     assert st["batches_published"] >= 8  # admitted a few at a time
+    got = [r[3].clone() for r in reqs]
+    for r in reqs:
+        r[3].fill_(float("nan"))
+    run("per_call", mats, partners, reqs)
+    for a, r in zip(got, reqs):
+        assert torch.equal(a, r[3])
+
+
+def test_batch_submit_matches_single_submit(library):
+    mats, partners = library
+    rng = np.random.default_rng(3)
+    reqs = make_requests(rng, mats, partners, 90)
+    lat, st = run("batched", mats, partners, reqs, batch=True)
+    assert st["completed"] == 90 and len(lat) == 90 and min(lat) >= 0
+    got = [r[3].clone() for r in reqs]
+    for r in reqs:
+        r[3].fill_(float("nan"))
+    run("batched", mats, partners, reqs)
+    for a, r in zip(got, reqs):
+        assert torch.equal(a, r[3])
 
 
 def test_oversized_request_and_bad_ids(library):
