@@ -238,8 +238,11 @@ def run_gpu(args):
     B = torch.from_numpy(B_h).to(device)
     C = torch.empty((M, NK), dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream()
-    if args.schedule:  # fixed plain merge-path schedule LANES,PATH (profiling)
-        lanes, path = (int(v) for v in args.schedule.split(","))
+    fixed_variant = 0
+    if args.schedule:  # fixed schedule LANES,PATH[,VARIANT] through fgb_spmm_ex (profiling)
+        vals = [int(v) for v in args.schedule.split(",")]
+        lanes, path = vals[0], vals[1]
+        fixed_variant = vals[2] if len(vals) > 2 else 0
         table, plan, npanels = {}, None, 1
     else:
         # the plain schedules' table (for the e2e leg and the record), then the
@@ -250,9 +253,15 @@ def run_gpu(args):
         plan = Plan.spmm(A, B, C, tune_reps=3)
         info = plan.info()
         npanels = info["panels"]
-    slabs = -(-NK // (4 * (32 if plan else lanes)))
-    if plan is None:
+    variant = info["variant"] if plan is not None else fixed_variant
+    plan_lanes = info["lanes"] if plan is not None else lanes
+    slabs = -(-NK // (4 * plan_lanes))
+    if plan is None and variant == 2:  # schedule built per call: counted as its kernels
+        launches_per_step = 10 + slabs
+    elif plan is None:
         launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
+    elif variant == 2:  # one launch per column slab + the partial-sum fix-up
+        launches_per_step = slabs + 1
     else:  # per panel: the slab launches + fix-up (item boundaries precomputed)
         launches_per_step = npanels * (slabs + 1)
 
@@ -260,7 +269,7 @@ def run_gpu(args):
         if plan is not None:
             plan.execute()
         else:
-            dev.spmm(A, B, C, lanes=lanes, path=path)
+            dev.spmm(A, B, C, lanes=lanes, path=path, variant=fixed_variant)
 
     def barrier():
         if world > 1:
@@ -308,43 +317,78 @@ def run_gpu(args):
                        "parallelism": f"replicas{world}"},
             "gpu_launches": args.steps * launches_per_step}
 
-    # ---- e2e: host buffers through the C ABI -> host result
+    # ---- e2e: host buffers through the C ABI -> host result.  Two buffer
+    # sets with a plan each (the second plan's schedule comes from the tune
+    # cache); every step uploads A and B from pinned memory, runs the plan
+    # and reads C back, and step i+1's uploads overlap step i's SpMM and
+    # read-back (copy-in, compute and copy-out streams).
     if not args.no_e2e:
         ctx = dev.context()
         lib = L.load()
-        ptr32 = torch.from_numpy(A_h.ptr.astype(np.int32)).pin_memory()
-        idx32 = torch.from_numpy(A_h.idx.astype(np.int32)).pin_memory()
-        val_h = torch.from_numpy(A_h.val).pin_memory()
+        host_A = [torch.from_numpy(A_h.ptr.astype(np.int32)).pin_memory(),
+                  torch.from_numpy(A_h.idx.astype(np.int32)).pin_memory(),
+                  torch.from_numpy(A_h.val).pin_memory()]
         B_pin = torch.from_numpy(B_h).pin_memory()
-        C_pin = torch.empty((M, NK), dtype=torch.float32).pin_memory()
-        d_ptr = torch.empty(ptr32.shape, dtype=torch.int32, device=device)
-        d_idx = torch.empty(idx32.shape, dtype=torch.int32, device=device)
-        d_val = torch.empty(val_h.shape, dtype=torch.float32, device=device)
-        d_B = torch.empty(B_pin.shape, dtype=torch.float32, device=device)
-        d_C = torch.empty((M, NK), dtype=torch.float32, device=device)
-        A_e = dev.DeviceSparse(M, A_h.ncols, d_ptr, d_idx, d_val, "csr", 1)
-        desc = A_e.desc()
-        tune = L.FgbSpmmTuning(lanes, 0, path)
-        h2d_pairs = [(d_ptr, ptr32), (d_idx, idx32), (d_val, val_h), (d_B, B_pin)]
-        h2d = sum(h.numel() * h.element_size() for _, h in h2d_pairs)
-        d2h = C_pin.numel() * C_pin.element_size()
+        C_pin = [torch.empty((M, NK), dtype=torch.float32).pin_memory() for _ in range(2)]
+        sets = []
+        for b in range(2):
+            if b == 0 and plan is not None:
+                A_b, B_b, C_b, plan_b = A, B, C, plan
+            else:
+                A_b = dev.DeviceSparse.from_host(A_h.nrows, A_h.ncols, A_h.ptr, A_h.idx, A_h.val,
+                                                 orient="csr")
+                B_b = torch.empty_like(B)
+                C_b = torch.empty_like(C)
+                B_b.copy_(B)
+                if plan is not None:
+                    plan_b = Plan.spmm(A_b, B_b, C_b, tune_reps=3)
+                else:
+                    plan_b = None
+            assert A_b.ptr.dtype == torch.int32 and A_b.base == 1
+            sets.append((A_b, B_b, C_b, plan_b))
+        h2d = sum(h.numel() * h.element_size() for h in host_A) + B_pin.numel() * B_pin.element_size()
+        d2h = C_pin[0].numel() * C_pin[0].element_size()
+        s_in, s_comp, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        ev_in = [torch.cuda.Event() for _ in range(2)]
+        ev_comp = [torch.cuda.Event() for _ in range(2)]
+        ev_out = [torch.cuda.Event() for _ in range(2)]
+        for b in range(2):  # all events start signalled
+            for ev in (ev_in[b], ev_comp[b], ev_out[b]):
+                ev.record(stream)
 
-        def e2e_step():
-            s = dev.stream_ptr()
-            for d, h in h2d_pairs:
-                L.check(lib.fgb_upload(ctx, d.data_ptr(), h.data_ptr(), h.numel() * h.element_size(), s))
-            L.check(lib.fgb_spmm_ex(ctx, ctypes.byref(desc), d_B.data_ptr(), NK, NK, d_C.data_ptr(),
-                                    NK, L.F32, 0, ctypes.byref(tune), s))
-            L.check(lib.fgb_download(ctx, C_pin.data_ptr(), d_C.data_ptr(), d2h, s))
+        def e2e_step(i):
+            b = i % 2
+            A_b, B_b, C_b, plan_b = sets[b]
+            s_in.wait_event(ev_comp[b])  # the SpMM two steps back has read this set
+            for d, h in zip((A_b.ptr, A_b.idx, A_b.val, B_b), (*host_A, B_pin)):
+                L.check(lib.fgb_upload(ctx, d.data_ptr(), h.data_ptr(), h.numel() * h.element_size(),
+                                       s_in.cuda_stream))
+            ev_in[b].record(s_in)
+            s_comp.wait_event(ev_in[b])
+            s_comp.wait_event(ev_out[b])  # C of two steps back has been read out
+            with torch.cuda.stream(s_comp):
+                if plan_b is not None:
+                    plan_b.execute()
+                else:
+                    dev.spmm(A_b, B_b, C_b, lanes=lanes, path=path, variant=fixed_variant)
+            ev_comp[b].record(s_comp)
+            s_out.wait_event(ev_comp[b])
+            L.check(lib.fgb_download(ctx, C_pin[b].data_ptr(), C_b.data_ptr(), d2h, s_out.cuda_stream))
+            ev_out[b].record(s_out)
 
-        for _ in range(3):
-            e2e_step()
+        for i in range(3):
+            e2e_step(i)
+        for st in (s_in, s_comp, s_out):
+            stream.wait_stream(st)
         barrier()
+        e2e_steps = max(4, args.steps // 2)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e2e_steps = max(3, args.steps // 4)
         e0.record(stream)
-        for _ in range(e2e_steps):
-            e2e_step()
+        s_in.wait_stream(stream)
+        for i in range(e2e_steps):
+            e2e_step(i)
+        for st in (s_in, s_comp, s_out):
+            stream.wait_stream(st)
         e1.record(stream)
         barrier()
         e2e_ms = e0.elapsed_time(e1)
@@ -352,13 +396,14 @@ def run_gpu(args):
             t = torch.tensor([e2e_ms], device=device)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
-        ok = bool(np.array_equal(C_pin[:2000].numpy(), C[:2000].cpu().numpy()))
+        last = (e2e_steps - 1) % 2
+        ok = bool(np.array_equal(C_pin[last].numpy(), C.cpu().numpy()))
         line["e2e"] = {"value": round(nbytes * e2e_steps * world / (e2e_ms / 1e3) / 1e9, 1),
                        "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "steps": e2e_steps, "ms_per_step": round(e2e_ms / e2e_steps, 3),
+                       "pipeline": "2 buffer sets; copy-in / SpMM / copy-out streams overlap",
                        "result_matches_device_run": ok}
-        # the e2e leg runs the plain merge-path schedule: item plan + slabs + fix-up
-        line["gpu_launches"] += e2e_steps * (2 + -(-NK // (4 * lanes)))
+        line["gpu_launches"] += e2e_steps * launches_per_step
 
     # ---- roofline of the SpMM (plan + per-slab merge kernels + fix-up)
     peak, peak_kind = load_peaks()
@@ -369,7 +414,8 @@ def run_gpu(args):
                         "unit": "GB/s", "frac": round(achieved / peak, 4),
                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": traffic, "traffic_source": traffic_src,
-                        "kernel": (f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
+                        "kernel": (f"spmm_vrow_k x{slabs} column slabs + vrow_fixup_k" if variant == 2 else
+                                   f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
                                    if plan is not None and npanels > 1 else
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
                         "algorithmic_bytes_per_launch": nbytes,

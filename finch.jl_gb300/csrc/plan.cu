@@ -34,7 +34,7 @@ struct Choice {
   int lanes = 0;
   int64_t path = 0;
   int panels = 1;  // SpMM: column panels (1 = the plain merge-path schedule)
-  int variant = 0;  // SpMM: 0 register gathers, 1 TMA stage ring
+  int variant = 0;  // SpMM: 0 register gathers, 1 TMA stage ring, 2 virtual-row slabs
 };
 
 static std::mutex g_tune_mu;
@@ -77,6 +77,9 @@ using namespace fgb;
 
 struct fgb_plan {
   std::map<int, fgb_panels*> panels;  // SpMM column-panel layouts by panel count
+  std::map<int64_t, VrowSchedule> vrows;  // SpMM virtual-row schedules by length
+  void* partial = nullptr;            // their partial sums (largest candidate)
+  size_t partial_bytes = 0;
   fgb_ctx* ctx = nullptr;
   fgb_plan_desc d{};
   fgb_sparse A{};
@@ -111,6 +114,27 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
         return fgb_panels_spmm(p->ctx, it->second, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                                d.flags, &t, s);
       }
+      if (c.variant == 2) {
+        auto it = p->vrows.find(c.path);
+        if (it == p->vrows.end()) {  // built outside capture (the timing pass comes first)
+          VrowSchedule v;
+          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s);
+          if (rc) return rc;
+          it = p->vrows.emplace(c.path, v).first;
+          const size_t need = spmm_vrow_scratch_bytes(v, d.k);
+          if (need > p->partial_bytes) {
+            cudaStreamSynchronize(s);
+            cudaFree(p->partial);
+            p->partial = nullptr;
+            p->partial_bytes = 0;
+            if (cudaMalloc(&p->partial, need) != cudaSuccess)
+              return set_error(FGB_ENOMEM, "fgb_plan: partial sums (%zu bytes)", need);
+            p->partial_bytes = need;
+          }
+        }
+        return spmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out,
+                         (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s);
+      }
       if (c.path > 0)
         return spmm_merge(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                           (d.flags & FGB_ACCUMULATE) ? 1 : 0, c.lanes, c.path, p->scratch,
@@ -144,6 +168,9 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t path : {128, 256, 512, 1024}) out.push_back(Choice{l, path, 1, 0});
     if (d.dtype == FGB_F32)  // B rows staged by TMA into a shared-memory ring
       for (int64_t path : {256, 512, 1024, 2048}) out.push_back(Choice{32, path, 1, 1});
+    if (d.dtype == FGB_F32 && p->A.val_t == FGB_F32 && p->A.nrows <= INT32_MAX)
+      for (int l : {4, 8})  // column slabs over length-sorted virtual rows
+        for (int64_t t : {32, 64, 128}) out.push_back(Choice{l, t, 1, 2});
     // column panels keep each panel's slice of B in L2 (worth it when B is not)
     const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);
     if (b_bytes > 32.0 * 1024 * 1024 && !(d.flags & FGB_ACCUMULATE))
@@ -185,7 +212,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   if (p->d.op == FGB_PLAN_SPMM) {
     const size_t esz = p->d.dtype == FGB_F64 ? 8 : 4;
     for (const Choice& c : cands)
-      if (c.path > 0)
+      if (c.path > 0 && c.variant != 2)
         p->scratch_bytes = std::max(p->scratch_bytes,
                                     spmm_merge_scratch_bytes(p->A.nrows, p->A.nnz, p->d.k, esz, c.path));
     if (p->scratch_bytes) {
@@ -268,6 +295,14 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     return rc;
   }
   p->choice = best;
+  for (auto it = p->vrows.begin(); it != p->vrows.end();) {  // and the chosen schedule
+    if (best.variant != 2 || it->first != best.path) {
+      vrow_free(&it->second);
+      it = p->vrows.erase(it);
+    } else {
+      ++it;
+    }
+  }
   for (auto it = p->panels.begin(); it != p->panels.end();) {  // keep only the chosen layout
     if (it->first != best.panels) {
       fgb_panels_destroy(it->second);
@@ -306,6 +341,8 @@ int fgb_plan_destroy(fgb_plan* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->scratch) cudaFree(p->scratch);
+  if (p->partial) cudaFree(p->partial);
+  for (auto& kv : p->vrows) vrow_free(&kv.second);
   for (auto& kv : p->panels) fgb_panels_destroy(kv.second);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;

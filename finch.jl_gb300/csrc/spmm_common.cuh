@@ -23,6 +23,25 @@ int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, in
                size_t scratch_bytes, cudaStream_t s, bool plan_ready = false,
                const int32_t* row_map = nullptr, int variant = 0);
 
+// Virtual-row column-slab SpMM (spmm_vrow.cu): rows cut into virtual rows of
+// at most T entries, sorted by length class; built once per matrix.
+struct VrowSchedule {
+  int64_t nv = 0, nl = 0;  // virtual rows; partial-sum slots (chunks after a row's first)
+  int T = 0;
+  int32_t* row = nullptr;  // per virtual row (sorted): row, entry offset in the row,
+  int32_t* off = nullptr;  // partial slot (-1: writes C)
+  int32_t* slot = nullptr;
+  int64_t* part_row = nullptr;  // per partial slot: its row (slots of a row in order)
+  void* mem = nullptr;
+};
+int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s);
+void vrow_free(VrowSchedule* v);
+size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk);
+// slab: 16 or 32 columns per launch; partial: spmm_vrow_scratch_bytes.
+int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
+              int64_t nk, void* C, int64_t ldc, int accumulate, int slab, void* partial,
+              cudaStream_t s);
+
 // Stage-ring (TMA gather4) kernels over planned merge-path items (spmm_tma.cu).
 int spmm_tma_items(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,
                    void* C, int64_t ldc, int accumulate, int64_t n_items, const int64_t* plan_row,

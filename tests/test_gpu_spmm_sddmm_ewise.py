@@ -127,6 +127,57 @@ def test_spmm_tma_stage_ring(gpu_lib, nk):
     assert flag.value == 0
 
 
+@pytest.mark.parametrize("nk", [128, 20, 36, 256])
+def test_spmm_virtual_rows(gpu_lib, nk):
+    """Variant 2 (column slabs over length-sorted virtual rows): within
+    tolerance of the oracle for both slab widths and several virtual-row
+    lengths (long rows split into partial sums), deterministic, and the same
+    with 64-bit row pointers."""
+    rng = np.random.default_rng(nk + 5)
+    r = zipf_csr(rng, 12000, 9000, mean=16, cap=5000)
+    B = rng.standard_normal((9000, nk)).astype(np.float32)
+    A = upload(r)
+    want = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, r.val, B, nthreads=oracle.max_threads())
+    scale = spmm_scale(r, B)
+    Bd = to_dev(B)
+    for lanes in (4, 8):
+        for T in (8, 64, 200):
+            C1 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=2))
+            assert_close(C1, want, scale, np.float32)
+            C2 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=2))
+            assert np.array_equal(C1, C2)
+    A64 = dev.DeviceSparse(A.nrows, A.ncols, torch.from_numpy(r.ptr.astype(np.int64)).cuda(), A.idx,
+                           A.val, "csr", 1)
+    C3 = to_host(dev.spmm(A64, Bd, lanes=4, path=64, variant=2))
+    assert np.array_equal(C3, to_host(dev.spmm(A, Bd, lanes=4, path=64, variant=2)))
+
+
+def test_spmm_virtual_rows_accumulate_strides_empty(gpu_lib):
+    rng = np.random.default_rng(31)
+    D = np.zeros((500, 300))
+    D[5, :] = rng.standard_normal(300)  # one row split into many virtual rows
+    D[7, 3] = 1.5
+    D[100:140] = np.where(rng.random((40, 300)) < 0.1, rng.standard_normal((40, 300)), 0.0)
+    r = csr_from_dense(D)
+    r.val = r.val.astype(np.float32)
+    Bfull = rng.standard_normal((300, 72)).astype(np.float32)
+    C0 = rng.standard_normal((500, 72)).astype(np.float32)
+    A = upload(r)
+    Cd = to_dev(C0)
+    dev.spmm(A, to_dev(Bfull)[:, :48], Cd[:, :48], flags=L.ACCUMULATE, lanes=8, path=16, variant=2)
+    B48 = np.ascontiguousarray(Bfull[:, :48])
+    want = oracle.spmm_csr(500, 300, r.ptr, r.idx, r.val, B48, C=np.ascontiguousarray(C0[:, :48]),
+                           init=False)
+    got = to_host(Cd)
+    assert_close(got[:, :48], want, spmm_scale(r, B48) + np.abs(C0[:, :48]), np.float32)
+    assert np.array_equal(got[:, 48:], C0[:, 48:])  # untouched beyond nk
+    empty = upload(csr_from_dense(np.zeros((40, 30), dtype=np.float32)))
+    Ce = dev.spmm(empty, to_dev(rng.standard_normal((30, 16)).astype(np.float32)), variant=2)
+    assert not to_host(Ce).any()
+    with pytest.raises(L.FinchGBError):
+        dev.spmm(A, to_dev(B48), flags=L.FINCH_ORDER, variant=2)
+
+
 def test_spmm_merge_accumulate_and_empty(gpu_lib):
     rng = np.random.default_rng(8)
     D = np.zeros((300, 200))
