@@ -121,16 +121,16 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s);
           if (rc) return rc;
           it = p->vrows.emplace(c.path, v).first;
-          const size_t need = spmm_vrow_scratch_bytes(v, d.k);
-          if (need > p->partial_bytes) {
-            cudaStreamSynchronize(s);
-            cudaFree(p->partial);
-            p->partial = nullptr;
-            p->partial_bytes = 0;
-            if (cudaMalloc(&p->partial, need) != cudaSuccess)
-              return set_error(FGB_ENOMEM, "fgb_plan: partial sums (%zu bytes)", need);
-            p->partial_bytes = need;
-          }
+        }
+        const size_t need = spmm_vrow_scratch_bytes(it->second, d.k);
+        if (need > p->partial_bytes) {  // never during capture: the same choice ran before it
+          cudaStreamSynchronize(s);
+          cudaFree(p->partial);
+          p->partial = nullptr;
+          p->partial_bytes = 0;
+          if (cudaMalloc(&p->partial, need) != cudaSuccess)
+            return set_error(FGB_ENOMEM, "fgb_plan: partial sums (%zu bytes)", need);
+          p->partial_bytes = need;
         }
         return spmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out,
                          (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s);
@@ -169,7 +169,7 @@ std::vector<Choice> candidates(const fgb_plan* p) {
     if (d.dtype == FGB_F32)  // B rows staged by TMA into a shared-memory ring
       for (int64_t path : {256, 512, 1024, 2048}) out.push_back(Choice{32, path, 1, 1});
     if (d.dtype == FGB_F32 && p->A.val_t == FGB_F32 && p->A.nrows <= INT32_MAX)
-      for (int l : {4, 8})  // column slabs over length-sorted virtual rows
+      for (int l : {2, 4, 8})  // column slabs over length-sorted virtual rows
         for (int64_t t : {32, 64, 128}) out.push_back(Choice{l, t, 1, 2});
     // column panels keep each panel's slice of B in L2 (worth it when B is not)
     const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);

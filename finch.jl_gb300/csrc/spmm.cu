@@ -236,13 +236,13 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
     rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s);
     if (rc) return rc;
     void* part = nullptr;
+    const int slab = 4 * (lanes > 0 ? lanes : 4);
     const size_t pb = spmm_vrow_scratch_bytes(v, nk);
     if (pb && cudaMalloc(&part, pb) != cudaSuccess) {
       vrow_free(&v);
       return set_error(FGB_ENOMEM, "fgb_spmm: partial sums (%zu bytes)", pb);
     }
-    rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0,
-                   4 * (lanes > 0 ? lanes : 4), part, s);
+    rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0, slab, part, s);
     cudaError_t e = cudaStreamSynchronize(s);  // before the schedule is freed
     cudaFree(part);
     vrow_free(&v);
@@ -273,8 +273,8 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
   int64_t path = tune ? tune->path : 0;
   const int variant = tune ? tune->variant : 0;
   if (variant < 0 || variant > 2) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1 or 2");
-  if (variant == 2 && lanes != 0 && lanes != 4 && lanes != 8)
-    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant 2 takes lanes 4 or 8");
+  if (variant == 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant 2 takes lanes 2, 4 or 8");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
   if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");

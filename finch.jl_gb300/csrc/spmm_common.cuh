@@ -28,16 +28,16 @@ int spmm_merge(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, in
 struct VrowSchedule {
   int64_t nv = 0, nl = 0;  // virtual rows; partial-sum slots (chunks after a row's first)
   int T = 0;
-  int32_t* row = nullptr;  // per virtual row (sorted): row, entry offset in the row,
-  int32_t* off = nullptr;  // partial slot (-1: writes C)
-  int32_t* slot = nullptr;
+  int4* vr = nullptr;      // per virtual row (sorted): row, first entry, length, partial
+                           // slot (-1: writes C)
   int64_t* part_row = nullptr;  // per partial slot: its row (slots of a row in order)
   void* mem = nullptr;
 };
 int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s);
 void vrow_free(VrowSchedule* v);
+// partial: the long rows' partial sums (spmm_vrow_scratch_bytes).
 size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk);
-// slab: 16 or 32 columns per launch; partial: spmm_vrow_scratch_bytes.
+// slab: 8, 16 or 32 columns per launch.
 int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
               int64_t nk, void* C, int64_t ldc, int accumulate, int slab, void* partial,
               cudaStream_t s);

@@ -3,10 +3,10 @@
 // For a B much larger than L2 whose rows are gathered at random (columns of
 // A spread over all of B), walking C's full width per stored entry re-reads
 // most B rows from HBM once per entry.  This schedule cuts C's columns into
-// slabs of SW = 16 or 32 and runs one launch per slab: while a launch runs,
-// only B's slab (ncols * SW * 4 bytes) is gathered, and it stays in L2;
-// A is re-read once per slab instead (its index and value streams are small
-// next to the B rows).
+// slabs of SW = 8, 16 or 32 and runs one launch per slab: while a launch
+// runs, only B's slab is gathered, so more of it stays in L2; A is re-read
+// once per slab instead (its index and value streams are small next to the
+// B rows).
 //
 // Inside a launch, rows are cut into virtual rows of at most T stored
 // entries and handed to sub-groups of L = SW/4 lanes (each lane owns 4
@@ -48,14 +48,14 @@ __device__ __forceinline__ uint8_t vrow_class(int64_t len) {
 }
 
 template <class PtrT>
-__global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int T,
+__global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int base, int T,
                             const int64_t* __restrict__ voff, const int64_t* __restrict__ loff,
                             uint8_t* __restrict__ key, int32_t* __restrict__ ord,
-                            int32_t* __restrict__ u_row, int32_t* __restrict__ u_off,
-                            int32_t* __restrict__ u_slot, int64_t* __restrict__ part_row) {
+                            int4* __restrict__ unsorted, int64_t* __restrict__ part_row) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
        r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t len = ld_ptr(ptr, r + 1) - ld_ptr(ptr, r);
+    const int64_t b0 = ld_ptr(ptr, r) - base;
+    const int64_t len = ld_ptr(ptr, r + 1) - base - b0;
     const int64_t v0 = voff[r], l0 = loff[r];
     const int64_t nch = voff[r + 1] - v0;
     for (int64_t c = 0; c < nch; ++c) {
@@ -63,36 +63,29 @@ __global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int T,
       const int64_t clen = len - c * T < T ? len - c * T : T;
       key[v] = vrow_class(clen);
       ord[v] = (int32_t)v;
-      u_row[v] = (int32_t)r;
-      u_off[v] = (int32_t)(c * T);
-      u_slot[v] = c == 0 ? -1 : (int32_t)(l0 + c - 1);
+      unsorted[v] = make_int4((int)r, (int)(b0 + c * T), (int)clen, c == 0 ? -1 : (int)(l0 + c - 1));
       if (c > 0) part_row[l0 + c - 1] = r;
     }
   }
 }
 
 __global__ void vrow_gather_k(int64_t nv, const int32_t* __restrict__ ord,
-                              const int32_t* __restrict__ u_row, const int32_t* __restrict__ u_off,
-                              const int32_t* __restrict__ u_slot, int32_t* __restrict__ row,
-                              int32_t* __restrict__ off, int32_t* __restrict__ slot) {
+                              const int4* __restrict__ unsorted, int4* __restrict__ vr) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t v = ord[i];
-    row[i] = u_row[v];
-    off[i] = u_off[v];
-    slot[i] = u_slot[v];
-  }
+       i += (int64_t)gridDim.x * blockDim.x)
+    vr[i] = unsorted[ord[i]];
 }
 
 // One launch: C[:, c0 : c0 + 4L] (or the partial sums) for every virtual row.
-template <class PtrT, int L>
-__global__ void __launch_bounds__(VR_THREADS, 4) spmm_vrow_k(
-    int64_t nv, const int32_t* __restrict__ vr_row, const int32_t* __restrict__ vr_off,
-    const int32_t* __restrict__ vr_slot, const PtrT* __restrict__ ptr, const int* __restrict__ idx,
+// NB gathers of B are in flight per lane; fewer blocks per SM leave room for
+// more (the 128-byte gathers of 32-column slabs want the extra depth).
+template <int L, int NB, int MINB>
+__global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
+    int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx,
     const float* __restrict__ val, const float* __restrict__ B, int64_t ldb, float* __restrict__ C,
-    int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, int T, float* __restrict__ partial) {
-  constexpr int PER = VR_BATCH / L > 0 ? VR_BATCH / L : 1;  // entries each lane loads per batch
-  constexpr int NB = PER * L;                                // entries per batch
+    int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, float* __restrict__ partial) {
+  constexpr int PER = NB / L;  // entries each lane loads per batch
+  static_assert(PER * L == NB, "batch must be a multiple of the sub-group");
   const int lane = threadIdx.x & 31, sl = lane % L;
   const unsigned gmask = group_mask<L>();
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
@@ -103,10 +96,10 @@ __global__ void __launch_bounds__(VR_THREADS, 4) spmm_vrow_k(
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
   for (int64_t v = gid; v < nv; v += ngroups) {
-    const int64_t r = __ldg(vr_row + v);
-    const int64_t rs = ld_ptr(ptr, r) - base + __ldg(vr_off + v);
-    const int64_t rend = ld_ptr(ptr, r + 1) - base;
-    const int len = (int)(rend - rs < (int64_t)T ? rend - rs : (int64_t)T);
+    const int4 rec = __ldg(vr + v);  // row, first entry, length, partial slot
+    const int len = rec.z;
+    const int* ix = idx + rec.y;
+    const float* vx = val + rec.y;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int t = 0; t < len; t += NB) {
       int j[PER];
@@ -117,8 +110,8 @@ __global__ void __launch_bounds__(VR_THREADS, 4) spmm_vrow_k(
         j[q] = 0;
         a[q] = 0.f;
         if (p < len) {
-          j[q] = ld_stream_i32(idx + rs + p, pol_stream) - base;
-          a[q] = ld_stream_f32(val + rs + p, pol_stream);
+          j[q] = ld_stream_i32(ix + p, pol_stream) - base;
+          a[q] = ld_stream_f32(vx + p, pol_stream);
         }
       }
       float4 b[NB];
@@ -140,9 +133,8 @@ __global__ void __launch_bounds__(VR_THREADS, 4) spmm_vrow_k(
       }
     }
     if (!active) continue;
-    const int32_t slot = __ldg(vr_slot + v);
-    if (slot < 0) {
-      float* dst = C + r * ldc + col;
+    if (rec.w < 0) {
+      float* dst = C + (int64_t)rec.x * ldc + col;
       if (accumulate) {
         const float4 o = *reinterpret_cast<const float4*>(dst);
         acc.x += o.x;
@@ -152,22 +144,56 @@ __global__ void __launch_bounds__(VR_THREADS, 4) spmm_vrow_k(
       }
       st_stream_f32x4(dst, acc, pol_stream);
     } else {
-      *reinterpret_cast<float4*>(partial + (int64_t)slot * nk + col) = acc;
+      *reinterpret_cast<float4*>(partial + (int64_t)rec.w * nk + col) = acc;
     }
   }
 }
 
-// Adds each row's partial sums (slots in chunk order) to that row of C.
+// Adds each long row's partial sums to that row of C: one warp per row (the
+// warp of its first slot), slots summed in order, 4 columns per lane.
 __global__ void vrow_fixup_k(int64_t nl, int64_t nk, const int64_t* __restrict__ part_row,
                              const float* __restrict__ partial, float* __restrict__ C, int64_t ldc) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nl * nk;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t w = t / nk, c = t - w * nk;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nl; w += nwarps) {
     const int64_t r = part_row[w];
-    if (w > 0 && part_row[w - 1] == r) continue;
-    float sum = partial[w * nk + c];
-    for (int64_t w2 = w + 1; w2 < nl && part_row[w2] == r; ++w2) sum += partial[w2 * nk + c];
-    C[r * ldc + c] += sum;
+    if (w > 0 && part_row[w - 1] == r) continue;  // not the row's first slot
+    int64_t n = 1;  // the row's slots: [w, w + n)
+    while (true) {
+      const int64_t q = w + n + lane;
+      const unsigned m = __ballot_sync(0xffffffffu, q < nl && part_row[q] == r);
+      if (m == 0xffffffffu) {
+        n += 32;
+        continue;
+      }
+      n += __ffs(~m) - 1;
+      break;
+    }
+    for (int64_t c = (int64_t)lane * 4; c < nk; c += 128) {
+      const float* p = partial + w * nk + c;
+      float4 sum = *reinterpret_cast<const float4*>(p);
+      for (int64_t k0 = 1; k0 < n; k0 += 8) {
+        float4 x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (k0 + u < n) x[u] = *reinterpret_cast<const float4*>(p + (k0 + u) * nk);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (k0 + u < n) {
+            sum.x += x[u].x;
+            sum.y += x[u].y;
+            sum.z += x[u].z;
+            sum.w += x[u].w;
+          }
+      }
+      float4* dst = reinterpret_cast<float4*>(C + r * ldc + c);
+      float4 o = *dst;
+      o.x += sum.x;
+      o.y += sum.y;
+      o.z += sum.z;
+      o.w += sum.w;
+      *dst = o;
+    }
   }
 }
 
@@ -218,20 +244,18 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
     cudaFree(cub_tmp);
     return set_error(FGB_EUNSUPPORTED, "vrow schedule: too many virtual rows");
   }
-  // persistent: row, off, slot (sorted), part_row; temporary: keys, order, unsorted copies
-  const size_t keep = a256(4 * nv) * 3 + a256(8 * (nl > 0 ? nl : 1));
+  // persistent: the sorted records and part_row; temporary: keys, order, unsorted records
+  const size_t keep = a256(16 * nv) + a256(8 * (nl > 0 ? nl : 1));
   char* mem = nullptr;
   if ((e = cudaMalloc(&mem, keep)) != cudaSuccess) return fail("alloc");
-  out->row = (int32_t*)mem;
-  out->off = (int32_t*)(mem + a256(4 * nv));
-  out->slot = (int32_t*)(mem + 2 * a256(4 * nv));
-  out->part_row = (int64_t*)(mem + 3 * a256(4 * nv));
+  out->vr = (int4*)mem;
+  out->part_row = (int64_t*)(mem + a256(16 * nv));
   out->mem = mem;
   out->nv = nv;
   out->nl = nl;
   out->T = T;
   char* tmp = nullptr;
-  const size_t tmp_bytes = a256(nv) * 2 + a256(4 * nv) * 5;
+  const size_t tmp_bytes = a256(nv) * 2 + a256(4 * nv) * 2 + a256(16 * nv);
   if ((e = cudaMalloc(&tmp, tmp_bytes)) != cudaSuccess) {
     cudaFree(mem);
     out->mem = nullptr;
@@ -240,11 +264,9 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   uint8_t* key = (uint8_t*)tmp;
   uint8_t* key2 = (uint8_t*)(tmp + a256(nv));
   int32_t* ord = (int32_t*)(tmp + 2 * a256(nv));
-  int32_t* ord2 = ord + a256(4 * nv) / 4;
-  int32_t* u_row = ord2 + a256(4 * nv) / 4;
-  int32_t* u_off = u_row + a256(4 * nv) / 4;
-  int32_t* u_slot = u_off + a256(4 * nv) / 4;
-  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, T, voff, loff, key, ord, u_row, u_off, u_slot,
+  int32_t* ord2 = (int32_t*)(tmp + 2 * a256(nv) + a256(4 * nv));
+  int4* unsorted = (int4*)(tmp + 2 * a256(nv) + 2 * a256(4 * nv));
+  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, A->index_base, T, voff, loff, key, ord, unsorted,
                                          out->part_row);
   b2 = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, 4, s);
@@ -261,8 +283,7 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   }
   e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, key, key2, ord, ord2, (int)nv, 0, 4, s);
   if (e == cudaSuccess) {
-    vrow_gather_k<<<grid_for(nv, 256, ctx->num_sms), 256, 0, s>>>(nv, ord2, u_row, u_off, u_slot,
-                                                                  out->row, out->off, out->slot);
+    vrow_gather_k<<<grid_for(nv, 256, ctx->num_sms), 256, 0, s>>>(nv, ord2, unsorted, out->vr);
     e = cudaStreamSynchronize(s);
   }
   cudaFree(tmp);
@@ -283,7 +304,8 @@ int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cuda
   *out = VrowSchedule{};
   if (A->orient != FGB_CSR) return set_error(FGB_EUNSUPPORTED, "vrow schedule: CSR only");
   if (T < 8 || T > 4096) return set_error(FGB_EINVAL, "vrow schedule: chunk %d outside [8, 4096]", T);
-  if (A->nrows > INT32_MAX) return set_error(FGB_EUNSUPPORTED, "vrow schedule: too many rows");
+  if (A->nrows > INT32_MAX || A->nnz > INT32_MAX)
+    return set_error(FGB_EUNSUPPORTED, "vrow schedule: needs fewer than 2^31 rows and entries");
   return A->ptr_t == FGB_I32 ? vrow_build_t<int32_t>(ctx, A, T, out, s)
                              : vrow_build_t<int64_t>(ctx, A, T, out, s);
 }
@@ -293,26 +315,25 @@ void vrow_free(VrowSchedule* v) {
   if (v) *v = VrowSchedule{};
 }
 
-template <class PtrT, int L>
+template <int L, int NB, int MINB>
 static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* B,
                        int64_t ldb, int64_t nk, float* C, int64_t ldc, int accumulate, float* partial,
                        cudaStream_t s) {
   static int occ = -1;  // per process: one device model
   if (occ < 0) {
     int o = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmm_vrow_k<PtrT, L>, VR_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmm_vrow_k<L, NB, MINB>, VR_THREADS, 0);
     occ = o > 0 ? o : 1;
   }
   const int64_t need = (v.nv * L + VR_THREADS - 1) / VR_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
-  for (int64_t c0 = 0; c0 < nk; c0 += 4 * L) {
-    spmm_vrow_k<PtrT, L><<<grid, VR_THREADS, 0, s>>>(
-        v.nv, v.row, v.off, v.slot, (const PtrT*)A->ptr, (const int*)A->idx, (const float*)A->val, B,
-        ldb, C, ldc, c0, nk, A->index_base, accumulate, v.T, partial);
-  }
+  for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
+    spmm_vrow_k<L, NB, MINB><<<grid, VR_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx,
+                                                        (const float*)A->val, B, ldb, C, ldc, c0, nk,
+                                                        A->index_base, accumulate, partial);
   if (v.nl > 0)
-    vrow_fixup_k<<<grid_for(v.nl * nk, 256, ctx->num_sms), 256, 0, s>>>(v.nl, nk, v.part_row, partial,
-                                                                        C, ldc);
+    vrow_fixup_k<<<grid_for(v.nl * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nl, nk, v.part_row, partial,
+                                                                         C, ldc);
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
 }
@@ -329,17 +350,13 @@ int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const vo
   if (nk % 4 || ldb % 4 || ldc % 4 || (uintptr_t)B % 16 || (uintptr_t)C % 16)
     return set_error(FGB_EUNSUPPORTED, "spmm vrow: needs 16-byte aligned rows of B and C");
   if (v.nl > 0 && !partial) return set_error(FGB_EINVAL, "spmm vrow: no partial-sum scratch");
-  const bool p32 = A->ptr_t == FGB_I32;
   const float* b = (const float*)B;
   float* c = (float*)C;
   float* part = (float*)partial;
-  if (slab == 16)
-    return p32 ? launch_vrow<int32_t, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s)
-               : launch_vrow<int64_t, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  if (slab == 32)
-    return p32 ? launch_vrow<int32_t, 8>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s)
-               : launch_vrow<int64_t, 8>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  return set_error(FGB_EINVAL, "spmm vrow: slab %d not in {16, 32}", slab);
+  if (slab == 8) return launch_vrow<2, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  if (slab == 16) return launch_vrow<4, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  if (slab == 32) return launch_vrow<8, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  return set_error(FGB_EINVAL, "spmm vrow: slab %d not in {8, 16, 32}", slab);
 }
 
 }  // namespace fgb

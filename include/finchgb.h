@@ -200,11 +200,11 @@ FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
  * lanes * vector-width, one launch per slab, so the gathered slab of B stays
  * L2-resident.  Zero fields take the defaults. */
 typedef struct fgb_spmm_tuning {
-  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variant 2: 4 or 8) */
+  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variant 2: 2, 4 or 8) */
   int32_t variant; /* 0: B rows gathered into registers; 1: B rows staged into a
-                      shared-memory ring by TMA tile::gather4 (fp32); 2: rows cut
-                      into virtual rows of at most `path` entries, sorted by
-                      length, one launch per column slab of 4 * lanes (fp32) */
+                      shared-memory ring by TMA tile::gather4 (fp32); 2: rows
+                      cut into virtual rows of at most `path` entries, sorted
+                      by length, one launch per column slab of 4 * lanes (fp32) */
   int64_t path;    /* merge-path item length (variant 2: virtual-row length) */
 } fgb_spmm_tuning;
 
