@@ -71,7 +71,7 @@ def load_peaks() -> tuple[float, str]:
 
 def load_traffic() -> tuple[int | None, str | None]:
     """Per-step DRAM bytes of the SpMM kernels from the committed ncu summary."""
-    p = ROOT / "profiles" / "spmm_merge_zipf1M_k128.md"
+    p = ROOT / "profiles" / "spmm_vrow_zipf1M_k128.md"
     if not p.exists():
         return None, None
     for line in p.read_text().splitlines():
