@@ -591,12 +591,38 @@ def suite_semiring() -> list[dict]:
         return x
 
     ms20 = _timed_ms(lambda: rounds(20), reps=3, warm=1)
+    x_push = rounds(20)
     per_round_bytes = 8 * g.nnz + 4 * (n + 1) + 3 * 4 * n + 2 * 4 * n
     f0 = torch.zeros(n, dtype=torch.uint8, device="cuda")
     f0[0] = 1
     yb = torch.empty_like(f0)
     ms_or = _timed_ms(lambda: dev.spmv(Ap, f0, yb, semiring=L.OR_AND), reps=20)
     or_bytes = 4 * g.nnz + 4 * (n + 1) + 2 * n
+    # pull over a CSR copy built once on the device (rows = targets: no atomics)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Ar = Ad.transposed_storage()
+    torch.cuda.synchronize()
+    ms_transpose = 1e3 * (time.perf_counter() - t0)
+    Arp = dev.DeviceSparse(n, n, Ar.ptr, Ar.idx, None, "csr", Ar.base)
+
+    from finchgb.plan import Plan
+
+    xp = x0.clone()
+    yp = torch.empty_like(xp)
+    plan_mp = Plan.spmv(Ar, xp, yp, semiring=L.MIN_PLUS)  # autotuned lanes per row, graph replay
+
+    def rounds_pull(nr=20):
+        xp.copy_(x0)
+        for _ in range(nr):
+            plan_mp.execute()
+            dev.dense_map(L.MAP_MIN, xp, yp, xp)
+        return xp
+
+    ms20_pull = _timed_ms(lambda: rounds_pull(20), reps=3, warm=1)
+    same = bool(torch.equal(rounds_pull(20), x_push))
+    plan_or = Plan.spmv(Arp, f0, yb, semiring=L.OR_AND)
+    ms_or_pull = _timed_ms(plan_or.execute, reps=20)
     threads = oracle.max_threads()
     xh = np.full(n, sentinel, dtype=np.int32)
     xh[0] = 0
@@ -611,10 +637,22 @@ def suite_semiring() -> list[dict]:
              "cpu_baseline": {"value": round(per_round_bytes / t_round / 1e9, 3), "unit": "GB/s",
                               "cores": 1, "kind": "port",
                               "sample": "one round: Finch's serial CSC min-plus nest (oracle)"}},
+            {"suite": "bellman_ford_minplus_4M", "variant": "csr_pull", "metric": "minplus_round_gbps",
+             "value": round(20 * per_round_bytes / (ms20_pull / 1e3) / 1e9, 1), "unit": "GB/s",
+             "dtype": "i32", "ms_per_20_rounds": round(ms20_pull, 3),
+             "one_time_csr_copy_ms": round(ms_transpose, 3), "equal_to_push": same,
+             "lanes_per_row": plan_mp.info()["lanes"],
+             "config": {"workload": "same graph; CSR copy built once on the device"},
+             "roofline": _roof(20 * per_round_bytes, ms20_pull)},
             {"suite": "reachability_or_and_4M", "metric": "or_and_spmv_gbps",
              "value": round(or_bytes / (ms_or / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "bool",
              "ms_per_call": round(ms_or, 4), "config": {"workload": "same graph, Pattern level"},
-             "roofline": _roof(or_bytes, ms_or)}]
+             "roofline": _roof(or_bytes, ms_or)},
+            {"suite": "reachability_or_and_4M", "variant": "csr_pull", "metric": "or_and_spmv_gbps",
+             "value": round(or_bytes / (ms_or_pull / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "bool",
+             "ms_per_call": round(ms_or_pull, 4), "lanes_per_row": plan_or.info()["lanes"],
+             "config": {"workload": "same graph, Pattern level, CSR copy"},
+             "roofline": _roof(or_bytes, ms_or_pull)}]
 
 
 def suite_cg() -> list[dict]:

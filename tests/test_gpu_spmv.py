@@ -140,6 +140,47 @@ def test_minplus_bellman_ford_rounds(gpu_lib):
     assert (xh < sentinel).sum() > n // 2  # the search actually reached most nodes
 
 
+@pytest.mark.parametrize("sr,dtype", [(L.MIN_PLUS, np.int32), (L.PLUS_TIMES, np.int64),
+                                      (L.MAX_PLUS, np.int64), (L.PLUS_TIMES, np.float32)])
+def test_short_row_blocks(gpu_lib, sr, dtype):
+    """CSR pull on short rows with irregular ones among them: empty rows, one
+    row of 2000 entries, a row count that is not a multiple of 32, and
+    accumulation.  Exact for integer semirings."""
+    rng = np.random.default_rng(41 + sr)
+    m, n = 3007, 2500
+    D = np.where(rng.random((m, n)) < 0.002, 1.0, 0.0)
+    D[40, :2000] = 1.0   # 2000 entries in the second block of rows
+    D[64:96] = 0.0       # a whole block of empty rows
+    D[3006, ::3] = 1.0   # the last (partial) block
+    from finchgb.workloads import csr_from_dense
+
+    b = csr_from_dense(D)
+    if np.dtype(dtype).kind == "i":
+        info = np.iinfo(dtype)
+        b.val = rng.integers(info.min // 2, info.max // 2, size=b.nnz, dtype=dtype)
+        x = rng.integers(info.min // 2, info.max // 2, size=n, dtype=dtype)
+    else:
+        b.val = rng.standard_normal(b.nnz).astype(dtype)
+        x = rng.standard_normal(n).astype(dtype)
+    assert b.nnz / m <= 16  # the short-row kernel's range
+    A = upload(b)
+    y = to_host(dev.spmv(A, to_dev(x), semiring=sr))
+    want = oracle_spmv(sr, b, x)
+    if np.dtype(dtype).kind == "i":
+        assert np.array_equal(y, want)
+        y0 = rng.integers(-1000, 1000, size=m).astype(dtype)
+        yd = to_dev(y0)
+        dev.spmv(A, to_dev(x), yd, semiring=sr, flags=L.ACCUMULATE)
+        add = {L.MIN_PLUS: np.minimum, L.MAX_PLUS: np.maximum}.get(sr)
+        if add is None:
+            exp = (y0.astype(np.int64) + want.astype(np.int64)).astype(dtype)  # wraps like Julia
+        else:
+            exp = add(y0, want)
+        assert np.array_equal(to_host(yd), exp)
+    else:
+        assert_close(y, want, abs_terms(b, x), np.float32)
+
+
 @pytest.mark.parametrize("ptr_i64", [False, True])
 def test_edge_cases(gpu_lib, ptr_i64):
     # empty matrix, empty fibers, a long fiber, 1x1
