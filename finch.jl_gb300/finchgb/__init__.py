@@ -2,7 +2,7 @@
 
 Finch-facing API (mirrors Finch.jl names):
   levels     Dense, SparseList, SparseCOO, Element, Pattern
-  tensors    Tensor, swizzle, csr, fsprand, transfer, gpu
+  tensors    Tensor, swizzle, csr, fsparse, fsprand, transfer, gpu
   front ends einsum (@einsum), lazy/compute, finch (@finch programs),
              tensordot, reduce, permutedims, broadcast, minimum, maximum
   scheduler  GB300Scheduler, set_scheduler, with_scheduler, Scalar
@@ -18,13 +18,13 @@ from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, r
 from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, default_scheduler,
                         einsum, finch, get_scheduler, set_scheduler, with_scheduler)
 from .tensors import (GPU, Dense, Element, Pattern, SparseCOO, SparseList, SwizzleArray, Tensor,
-                      csr, fsprand, gpu, swizzle, transfer)
+                      csr, fsparse, fsprand, gpu, swizzle, transfer)
 
 __all__ = [
     "FinchGBError", "FinchGBUnsupported", "DeviceSparse", "context", "spmv", "spmm", "sddmm",
     "ewise", "ewise_reduce", "LazyTensor", "lazy", "compute", "einsum", "finch", "tensordot",
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",
     "default_scheduler", "get_scheduler", "set_scheduler", "with_scheduler", "GPU", "Dense",
-    "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsprand",
+    "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsparse", "fsprand",
     "gpu", "swizzle", "transfer", "_lib",
 ]

@@ -27,6 +27,8 @@ CSR, CSC = 0, 1
 ACCUMULATE, FINCH_ORDER, FMA, NO_FMA = 0x1, 0x2, 0x4, 0x8
 # fgb_ewise_op
 EW_MUL, EW_ADD = 0, 1
+# fgb_combine
+COMBINE_ADD, COMBINE_OR, COMBINE_MIN, COMBINE_MAX, COMBINE_LAST = range(5)
 
 
 class FinchGBError(RuntimeError):
@@ -108,6 +110,9 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_stream_sync": (c_int, [c_void_p, c_void_p]),
     "fgb_narrow_index": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p]),
     "fgb_transpose": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_coo_assemble": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_int, c_void_p, c_void_p, c_int,
+                                 c_int, c_void_p, c_int, POINTER(FgbSparse), POINTER(c_int64),
+                                 c_void_p]),
     "fgb_spmv": (c_int, [c_void_p, c_int, POINTER(FgbSparse), c_void_p, c_int, c_void_p, c_int,
                          c_uint, c_void_p]),
     "fgb_spmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,

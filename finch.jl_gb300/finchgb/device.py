@@ -168,6 +168,29 @@ def _ctx_for(t: torch.Tensor):
     return context(t.device.index)
 
 
+def coo_assemble(nrows: int, ncols: int, I: torch.Tensor, J: torch.Tensor,
+                 V: torch.Tensor | None, orient: str = "csc", combine: int = L.COMBINE_ADD,
+                 in_base: int = 1, out_base: int = 1) -> DeviceSparse:
+    """fsparse(I, J, V, (nrows, ncols), combine) assembled in HBM as CSC
+    (Finch's Dense(SparseList)) or CSR; I/J are device int32/int64
+    coordinates with base `in_base`, V device values (None: Pattern)."""
+    ctx = context(I.device.index)
+    dev = I.device
+    n_in = int(I.numel())
+    nfib = ncols if orient == "csc" else nrows
+    ptr_t = torch.int32 if n_in + out_base < 2**31 - 1 else torch.int64
+    ptr = torch.empty(nfib + 1, dtype=ptr_t, device=dev)
+    idx = torch.empty(max(n_in, 1), dtype=torch.int32, device=dev)
+    val = None if V is None else torch.empty(max(n_in, 1), dtype=V.dtype, device=dev)
+    out = L.FgbSparse(nrows, ncols, 0, L.CSC if orient == "csc" else L.CSR, out_base,
+                      dtype_code(ptr), L.I32, dtype_code(val), 0, _dptr(ptr), _dptr(idx), _dptr(val))
+    nnz = ctypes.c_int64()
+    L.call("fgb_coo_assemble", ctx, nrows, ncols, n_in, dtype_code(I), _dptr(I), _dptr(J), in_base,
+           dtype_code(V), _dptr(V), combine, ctypes.byref(out), ctypes.byref(nnz), stream_ptr())
+    k = nnz.value
+    return DeviceSparse(nrows, ncols, ptr, idx[:k], None if val is None else val[:k], orient, out_base)
+
+
 def spmv(A: DeviceSparse, x: torch.Tensor, y: torch.Tensor | None = None,
          semiring: int = L.PLUS_TIMES, flags: int = 0) -> torch.Tensor:
     """y <<add>>= A (*) x over `semiring` (y is created and initialised if None)."""

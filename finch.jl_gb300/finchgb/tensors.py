@@ -21,7 +21,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .workloads import SparseBuffers, coo_to_csr, csc_from_dense
+from .workloads import SparseBuffers, csc_from_dense
 
 
 # ---------------------------------------------------------------- levels
@@ -131,6 +131,7 @@ class Tensor:
         self.ddata = None
         self.dsparse = None
         self.coo = None
+        self.combine = "+"
         if _buf is not None:
             self.shape = (_buf.nrows, _buf.ncols) if self.kind != "sparse1" else (_buf.ncols,)
             return
@@ -193,7 +194,16 @@ class Tensor:
         if self.kind == "coo":
             out = np.full(self.shape, self.fill_value, dtype=self.dtype)
             I, J, V = self.coo
-            out[I - 1, J - 1] = V
+            if len(I):
+                # fsparse folds duplicates with `combine`, in input order
+                key = (np.asarray(J, np.int64) - 1) * self.shape[0] + (np.asarray(I, np.int64) - 1)
+                order = np.argsort(key, kind="stable")
+                k, v = key[order], np.asarray(V)[order]
+                heads = np.flatnonzero(np.r_[True, k[1:] != k[:-1]])
+                ends = np.r_[heads[1:], k.size]
+                folded = [_fold(self.combine, v[a:b]) for a, b in zip(heads, ends)]
+                uk = k[heads]
+                out[uk % self.shape[0], uk // self.shape[0]] = folded
             return out
         buf = self.host_buffers()
         D = buf.todense()
@@ -300,6 +310,49 @@ def csr(A, fill_value=0.0, dtype=None) -> SwizzleArray:
     return swizzle(Tensor(Dense(SparseList(el)), A.T), 2, 1)
 
 
+_COMBINE = {"+": 0, "|": 1, "min": 2, "max": 3, "last": 4}
+
+
+def _fold(combine: str, v: np.ndarray):
+    acc = v[0]
+    for t in v[1:]:
+        if combine == "+":
+            acc = acc + t if v.dtype != np.bool_ else (acc | t)
+        elif combine == "|":
+            acc = acc | t
+        elif combine == "min":
+            acc = t if t < acc else acc
+        elif combine == "max":
+            acc = t if t > acc else acc
+        else:
+            acc = t
+    return acc
+
+
+def fsparse(I, J, V, shape=None, combine: str = "+", fill_value=None) -> Tensor:
+    """Finch's fsparse(I, J, V, (m, n), combine) (src/interface/fsparse.jl):
+    a COO tensor whose duplicate coordinates are folded with `combine` (+, |,
+    min, max or last; + means | for Bool).  Coordinates are 1-based.  The
+    triplets stay as given until the tensor is moved to the GPU, where they
+    are sorted and folded in HBM (fgb_coo_assemble)."""
+    I = np.asarray(I, dtype=np.int64)
+    J = np.asarray(J, dtype=np.int64)
+    V = np.asarray(V)
+    if combine not in _COMBINE:
+        raise ValueError(f"combine must be one of {sorted(_COMBINE)}")
+    if shape is None:
+        shape = (int(I.max()) if I.size else 0, int(J.max()) if J.size else 0)
+    if I.size and (I.min() < 1 or J.min() < 1 or I.max() > shape[0] or J.max() > shape[1]):
+        raise ValueError("fsparse: a coordinate lies outside the shape")  # Finch: 1 <= I <= M
+    fill = np.zeros((), V.dtype)[()] if fill_value is None else fill_value
+    t = Tensor.__new__(Tensor)
+    t.fmt = SparseCOO(2, Element(fill, V.dtype))
+    t.kind, t.fill_value, t.dtype = "coo", fill, V.dtype
+    t.data, t.buf, t.ddata, t.dsparse = None, None, None, None
+    t.coo, t.combine, t.shape = (I, J, V), combine, (int(shape[0]), int(shape[1]))
+    return t
+
+
 def fsprand(rng, m: int, n: int, p: float, dtype=np.float64) -> Tensor:
     """Finch's fsprand + Tensor(Dense(SparseList(Element(0))), ...)."""
     from .workloads import fsprand as _fsprand
@@ -342,11 +395,17 @@ def transfer(device, t):
         tt = torch.from_numpy(src if src.dtype != np.bool_ else src.astype(np.uint8))
         t.ddata = tt.to(torch.device("cuda", idx))
         return t
-    if t.kind == "coo":
+    if t.kind == "coo":  # assembled in HBM: sort, fold duplicates, build ptr
         I, J, V = t.coo
-        b = coo_to_csr(t.shape[1], t.shape[0], J, I, V)  # CSR of A^T == CSC of A
-        t.buf = SparseBuffers(t.shape[0], t.shape[1], b.ptr, b.idx, b.val, "csc")
-        t.kind = "csc"
+        d = torch.device("cuda", idx)
+        Id = torch.from_numpy(np.ascontiguousarray(I, dtype=np.int64)).to(d)
+        Jd = torch.from_numpy(np.ascontiguousarray(J, dtype=np.int64)).to(d)
+        Vh = np.ascontiguousarray(V)
+        Vd = torch.from_numpy(Vh if Vh.dtype != np.bool_ else Vh.astype(np.uint8)).to(d)
+        t.dsparse = dev.coo_assemble(t.shape[0], t.shape[1], Id, Jd, Vd, orient="csc",
+                                     combine=_COMBINE[t.combine])
+        t.kind, t.coo, t.buf = "csc", None, None
+        return t
     b = t.buf
     val = b.val
     t.dsparse = dev.DeviceSparse.from_host(b.nrows, b.ncols, b.ptr, b.idx, val, orient=b.orient,

@@ -166,6 +166,32 @@ FGB_API int fgb_narrow_index(fgb_ctx* ctx, const int64_t* src, int32_t* dst, int
 FGB_API int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr, int32_t* out_idx,
                   void* out_val, void* stream);
 
+/* Duplicate handling of fgb_coo_assemble: Julia's `combine` for fsparse. */
+typedef enum fgb_combine {
+  FGB_COMBINE_ADD = 0, /* +  (the default; | for Bool values) */
+  FGB_COMBINE_OR = 1,  /* |  (Bool) */
+  FGB_COMBINE_MIN = 2, /* min (NaN-propagating, -0.0 < +0.0) */
+  FGB_COMBINE_MAX = 3, /* max */
+  FGB_COMBINE_LAST = 4 /* the last duplicate in input order wins */
+} fgb_combine;
+
+/* COO triplets -> SparseList on the device: `fsparse(I, J, V, (m, n),
+ * combine)` followed by the copy into Dense(SparseList(Element)) (out->orient
+ * CSC) or its row-major swizzle (CSR), replacing the host path through
+ * src/interface/fsparse.jl:60-100 and the COO -> CSC copy of
+ * src/interface/copy.jl:77-113.  Entries come out sorted by (fiber,
+ * coordinate); duplicates are folded left to right in input order with
+ * `combine`, so float sums equal foldl's.  I, J: n_in device coordinates
+ * (idx_t I32 or I64, base in_base); val: n_in values of val_t, NULL with
+ * val_t FGB_NONE for a Pattern.  `out` describes caller buffers: nrows,
+ * ncols, orient, index_base, ptr_t (I32/I64) with ptr of n_fibers + 1, idx_t
+ * I32 and val_t = val_t, idx/val with room for n_in entries.  On return
+ * *nnz_out = out->nnz = the stored count.  A coordinate outside the shape is
+ * EINVAL.  Synchronous (the count is returned to the host). */
+FGB_API int fgb_coo_assemble(fgb_ctx* ctx, int64_t nrows, int64_t ncols, int64_t n_in, int idx_t,
+                             const void* I, const void* J, int in_base, int val_t, const void* val,
+                             int combine, fgb_sparse* out, int64_t* nnz_out, void* stream);
+
 /* ---- compute ------------------------------------------------------------ */
 
 /* Semiring SpMV: y[i] <<add>>= mul(A[i,j], x[j]) for A m x n.

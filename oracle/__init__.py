@@ -63,6 +63,8 @@ def lib() -> ctypes.CDLL:
             L.orc_ewise.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
             L.orc_ewise_reduce.argtypes = [i32, i32, i64, i64, vp, vp, vp, vp, vp, vp, vp, i64, vp]
             L.orc_max_threads.argtypes = []
+            L.orc_coo_assemble.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp, vp, vp, vp]
+            L.orc_coo_assemble.restype = i64
             _lib = L
     return _lib
 
@@ -171,3 +173,21 @@ def ewise_reduce(dims, m, n, pa, ia, va, pb=None, ib=None, vb=None, Bd=None):
                            None if vb is None else _p(np.ascontiguousarray(vb)),
                            _p(Bd), 0 if Bd is None else Bd.shape[1], _p(y))
     return y
+
+
+def coo_assemble(m, n, I, J, V, csc=True, combine=0):
+    """fsparse(I, J, V, (m, n), combine) copied into Dense(SparseList) (csc) or
+    its row-major swizzle: returns 1-based (ptr, idx, val); val is None for a
+    Pattern (V None).  Raises ValueError for out-of-range coordinates."""
+    I, J = _i64(I), _i64(J)
+    nin = I.size
+    nfib = n if csc else m
+    ptr = np.zeros(nfib + 1, dtype=np.int64)
+    idx = np.zeros(max(nin, 1), dtype=np.int64)
+    V = None if V is None else np.ascontiguousarray(V)
+    val = None if V is None else np.zeros(max(nin, 1), dtype=V.dtype)
+    q = lib().orc_coo_assemble(int(csc), dtype_code(V), combine, m, n, nin, _p(I), _p(J), _p(V),
+                               _p(ptr), _p(idx), _p(val))
+    if q < 0:
+        raise ValueError("coordinate out of range")
+    return ptr, idx[:q], (None if val is None else val[:q])

@@ -375,6 +375,137 @@ int orc_ewise_reduce(int dims, int at, int64_t m, int64_t n, const int64_t* pa,
   return 0;
 }
 
+/*
+ * fsparse(I, J, V, (m, n), combine) followed by the copy into
+ * Dense(SparseList(Element)) (csc = 1) or its row-major swizzle (csc = 0):
+ * the documented contract of src/interface/fsparse.jl:13-100 -- coordinates
+ * sorted with the last index most significant (column, then row), duplicates
+ * folded left to right in input order (`foldl(combine, V[run])`).  The sort
+ * is a stable merge sort on (fiber, coordinate, input position).  1-based
+ * coordinates in, 1-based ptr/idx out.  combine: 0 +, 1 |, 2 min, 3 max,
+ * 4 last (Julia Base semantics: wrapping integers, NaN-propagating float
+ * min/max with -0.0 < +0.0).  Returns the stored count, or -1 if a
+ * coordinate is out of range.
+ */
+static const int64_t* g_coo_key;
+static void coo_merge(int64_t* a, int64_t* tmp, int64_t n) {
+  if (n < 2) return;
+  const int64_t h = n / 2;
+  coo_merge(a, tmp, h);
+  coo_merge(a + h, tmp, n - h);
+  int64_t i = 0, j = h, k = 0;
+  while (i < h && j < n) tmp[k++] = g_coo_key[a[j]] < g_coo_key[a[i]] ? a[j++] : a[i++];
+  while (i < h) tmp[k++] = a[i++];
+  while (j < n) tmp[k++] = a[j++];
+  memcpy(a, tmp, (size_t)n * sizeof(int64_t));
+}
+
+static double coo_fold_double(int combine, double a, double b) {
+  switch (combine) {
+    case 0: return a + b;
+    case 2:
+      if (a != a) return a;
+      if (b != b) return b;
+      return (b < a || (b == a && signbit(b) && !signbit(a))) ? b : a;
+    case 3:
+      if (a != a) return a;
+      if (b != b) return b;
+      return (b > a || (b == a && !signbit(b) && signbit(a))) ? b : a;
+    default: return b;
+  }
+}
+static float coo_fold_float(int combine, float a, float b) {
+  switch (combine) {
+    case 0: return a + b;
+    case 2:
+      if (a != a) return a;
+      if (b != b) return b;
+      return (b < a || (b == a && signbit(b) && !signbit(a))) ? b : a;
+    case 3:
+      if (a != a) return a;
+      if (b != b) return b;
+      return (b > a || (b == a && !signbit(b) && signbit(a))) ? b : a;
+    default: return b;
+  }
+}
+static int32_t coo_fold_int32_t(int combine, int32_t a, int32_t b) {
+  switch (combine) {
+    case 0: return (int32_t)((uint32_t)a + (uint32_t)b);
+    case 2: return b < a ? b : a;
+    case 3: return b > a ? b : a;
+    default: return b;
+  }
+}
+static int64_t coo_fold_int64_t(int combine, int64_t a, int64_t b) {
+  switch (combine) {
+    case 0: return (int64_t)((uint64_t)a + (uint64_t)b);
+    case 2: return b < a ? b : a;
+    case 3: return b > a ? b : a;
+    default: return b;
+  }
+}
+static uint8_t coo_fold_uint8_t(int combine, uint8_t a, uint8_t b) {
+  switch (combine) {
+    case 0:
+    case 1: return (uint8_t)(a | b);
+    case 2: return b < a ? b : a;
+    case 3: return b > a ? b : a;
+    default: return b;
+  }
+}
+int64_t orc_coo_assemble(int csc, int vt, int combine, int64_t m, int64_t n, int64_t nin,
+                         const int64_t* I, const int64_t* J, const void* V, int64_t* out_ptr,
+                         int64_t* out_idx, void* out_val) {
+  const int64_t nfib = csc ? n : m, inner = csc ? m : n;
+  int64_t* key = (int64_t*)malloc((size_t)(nin > 0 ? nin : 1) * sizeof(int64_t));
+  int64_t* ord = (int64_t*)malloc((size_t)(nin > 0 ? nin : 1) * sizeof(int64_t));
+  int64_t* tmp = (int64_t*)malloc((size_t)(nin > 0 ? nin : 1) * sizeof(int64_t));
+  for (int64_t k = 0; k < nin; ++k) {
+    const int64_t i = I[k] - 1, j = J[k] - 1;
+    if (i < 0 || i >= m || j < 0 || j >= n) {
+      free(key);
+      free(ord);
+      free(tmp);
+      return -1;
+    }
+    key[k] = csc ? j * m + i : i * n + j;
+    ord[k] = k;
+  }
+  g_coo_key = key;
+  coo_merge(ord, tmp, nin);
+  int64_t q = 0, f = 0;
+  out_ptr[0] = 1;
+  for (int64_t k = 0; k < nin;) {
+    int64_t r = k + 1;
+    while (r < nin && key[ord[r]] == key[ord[k]]) ++r;
+    const int64_t fib = key[ord[k]] / inner;
+    while (f < fib) out_ptr[++f] = q + 1;
+    out_idx[q] = key[ord[k]] % inner + 1;
+#define FOLD(T)                                                      \
+  {                                                                  \
+    T v = ((const T*)V)[ord[k]];                                     \
+    for (int64_t t = k + 1; t < r; ++t) v = coo_fold_##T(combine, v, ((const T*)V)[ord[t]]); \
+    ((T*)out_val)[q] = v;                                            \
+  }
+    switch (vt) {
+      case T_F64: FOLD(double) break;
+      case T_F32: FOLD(float) break;
+      case T_I32: FOLD(int32_t) break;
+      case T_I64: FOLD(int64_t) break;
+      case T_BOOL: FOLD(uint8_t) break;
+      default: break; /* Pattern: no values */
+    }
+#undef FOLD
+    ++q;
+    k = r;
+  }
+  while (f < nfib) out_ptr[++f] = q + 1;
+  free(key);
+  free(ord);
+  free(tmp);
+  return q;
+}
+
 /* Threads available to the OpenMP runtime (1 without OpenMP). */
 int orc_max_threads(void) {
 #ifdef _OPENMP
