@@ -131,8 +131,9 @@ class ClockSampler:
 
 
 def dist_setup():
-    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
-            int(os.environ.get("LOCAL_RANK", "0")))
+    from finchgb.replicas import rank_env
+
+    return rank_env()
 
 
 def cpu_reference_pass(A, B, threads: int) -> float:
