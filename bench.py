@@ -547,7 +547,14 @@ def suite_sddmm() -> list[dict]:
     Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
     outd = torch.empty(A.nnz, dtype=torch.float32, device="cuda")
     nbytes = 4 * (m + 1) + 8 * A.nnz + 2 * 4 * m * 64 + 4 * A.nnz
-    ms = _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd), reps=10)
+    from finchgb.plan import Plan
+
+    schedules = {"one_pass_default": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd, slab=0), reps=10),
+                 "slab32_lanes8": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd, lanes=8, slab=32),
+                                            reps=10)}
+    plan = Plan.sddmm(Ad, Xd, Yd, outd, tune_reps=3)
+    schedules["plan"] = _timed_ms(plan.execute, reps=10)
+    ms = schedules["plan"]
     rows = 100_000
     p = A.ptr[: rows + 1]
     nnz_s = int(p[-1] - 1)
@@ -558,6 +565,8 @@ def suite_sddmm() -> list[dict]:
     return [{"suite": "sddmm_1M_k64", "metric": "sddmm_gbps_algorithmic",
              "value": round(nbytes / (ms / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "f32",
              "ms_per_call": round(ms, 4),
+             "schedules_ms": {k: round(v, 4) for k, v in schedules.items()},
+             "plan_choice": plan.info(),
              "config": {"workload": "zipf1.5 1Mx1M nnz 16M CSR, X/Y 1Mx64 N(0,1)"},
              "roofline": _roof(nbytes, ms),
              "cpu_baseline": {"value": round(nbytes / t_full / 1e9, 3), "unit": "GB/s",

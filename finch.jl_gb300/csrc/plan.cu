@@ -28,7 +28,7 @@ int spmv_with_group(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void*
                     void* y, int y_t, unsigned flags, int group, void* stream);
 int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
                int64_t ldy, int64_t k, void* out_val, int dtype, unsigned flags, int lanes,
-               int64_t chunk, void* stream);
+               int64_t chunk, void* stream, int64_t slab);
 
 struct Choice {
   int lanes = 0;
@@ -143,7 +143,8 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
                        c.lanes, 0, s);
     case FGB_PLAN_SDDMM:
       return sddmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, d.dtype,
-                        d.flags, c.lanes, c.path, s);
+                        d.flags, c.lanes, c.path, s,
+                        c.variant == 2 ? 128 / (d.dtype == FGB_F64 ? 8 : 4) : 0);
     default: return set_error(FGB_EINVAL, "fgb_plan: unknown op %d", d.op);
   }
 }
@@ -180,8 +181,10 @@ std::vector<Choice> candidates(const fgb_plan* p) {
             if (v == 0 || d.dtype == FGB_F32) out.push_back(Choice{32, path, np, v});
   } else {
     if (d.flags & FGB_FINCH_ORDER) return {Choice{0, 0}};
-    for (int l : {8, 16, 32})
+    for (int l : {4, 8, 16, 32})
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{l, chunk});
+    if (d.k * (d.dtype == FGB_F64 ? 8 : 4) > 128)  // column slabs of one 128-byte line
+      for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{d.dtype == FGB_F64 ? 16 : 8, chunk, 1, 2});
   }
   return out;
 }

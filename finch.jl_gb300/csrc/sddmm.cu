@@ -11,6 +11,12 @@
 // with xor-shuffles, and one lane writes out[e].  Y rows are gathered with
 // an evict-last L2 hint; A's idx/val and the output stream with evict-first.
 //
+// Column slabs: when Y is far larger than L2, k is cut into slabs of one
+// 128-byte line per row of Y, one launch per slab, so that a launch gathers
+// from ncols lines instead of ncols * k * esz / 128.  The first slab writes
+// the partial dot into out, middle slabs add to it, and the last one adds
+// its part and multiplies by A.val[e].
+//
 // FGB_FINCH_ORDER selects one thread per entry and a sequential dot over k
 // ascending, then the product with A.val[e].
 #include "fgb_internal.cuh"
@@ -58,7 +64,8 @@ __global__ void __launch_bounds__(256) sddmm_csr(int64_t nrows, int64_t nnz,
                                                  const T* __restrict__ val,
                                                  const T* __restrict__ X, int64_t ldx,
                                                  const T* __restrict__ Y, int64_t ldy, int64_t k,
-                                                 T* __restrict__ out, int base, int64_t chunk) {
+                                                 T* __restrict__ out, int base, int64_t chunk,
+                                                 int mode) {
   constexpr int GPW = 32 / L;  // groups per warp
   const int lane = threadIdx.x & 31;
   const int gl = lane & (L - 1);  // lane inside group
@@ -112,7 +119,11 @@ __global__ void __launch_bounds__(256) sddmm_csr(int64_t nrows, int64_t nnz,
       for (int u = 0; u < U; ++u) {
 #pragma unroll
         for (int m = L / 2; m >= 1; m >>= 1) dot[u] += __shfl_xor_sync(gmask, dot[u], m, L);
-        if (ok[u] && gl == 0) out[e[u]] = wmul(__ldg(val + e[u]), dot[u]);
+        if (ok[u] && gl == 0) {
+          // mode 0: the whole k; 1: first slab; 2: middle slab; 3: last slab
+          const T d = mode >= 2 ? out[e[u]] + dot[u] : dot[u];
+          out[e[u]] = (mode == 0 || mode == 3) ? wmul(__ldg(val + e[u]), d) : d;
+        }
       }
     }
   }
@@ -138,7 +149,7 @@ __global__ void sddmm_csr_serial(int64_t nrows, int64_t nnz, const PtrT* __restr
 template <class T, class PtrT>
 static int run(fgb_ctx* ctx, const fgb_sparse* A, const T* X, int64_t ldx, const T* Y,
                int64_t ldy, int64_t k, T* out, unsigned flags, int lanes, int64_t chunk,
-               cudaStream_t s) {
+               int64_t slab, cudaStream_t s) {
   const int64_t nf = n_fibers(A);
   const int64_t nnz = A->nnz;
   if (nnz == 0) return FGB_OK;
@@ -153,41 +164,50 @@ static int run(fgb_ctx* ctx, const fgb_sparse* A, const T* X, int64_t ldx, const
         nf, nnz, ptr, idx, val, X, ldx, Y, ldy, k, out, base, fm);
     return check_launch("sddmm_csr_serial");
   }
-  if (chunk <= 0) chunk = 256;
+  if (chunk <= 0) chunk = 128;
   const int64_t nchunks = (nnz + chunk - 1) / chunk;
   const int grid = grid_for(nchunks * 32, threads, ctx->num_sms, 8);
   constexpr int VN = sizeof(T) == 4 ? 4 : 1;
   const bool vec_ok = VN > 1 && k % VN == 0 && ldx % VN == 0 && ldy % VN == 0 &&
                       (uintptr_t)X % 16 == 0 && (uintptr_t)Y % 16 == 0;
-  if (lanes <= 0) {
-    const int64_t need = vec_ok ? (k + VN - 1) / VN : k;
-    lanes = need <= 4 ? 4 : need <= 8 ? 8 : need <= 16 ? 16 : 32;
+  if (slab <= 0 || slab >= k || (vec_ok && slab % VN)) slab = k;  // one pass
+  if (lanes <= 0) {  // at most 8 lanes per entry: more entries in flight per warp
+    const int64_t need = vec_ok ? (slab + VN - 1) / VN : slab;
+    lanes = need <= 4 ? 4 : 8;
   }
-#define FGB_SDDMM(LL, VV, UU)                                                            \
-  sddmm_csr<T, PtrT, LL, VV, UU><<<grid, threads, 0, s>>>(nf, nnz, ptr, idx, val, X, ldx, Y, \
-                                                          ldy, k, out, base, chunk)
-  if (vec_ok) {
-    switch (lanes) {
-      case 4: FGB_SDDMM(4, VN, 2); break;
-      case 8: FGB_SDDMM(8, VN, 2); break;
-      case 16: FGB_SDDMM(16, VN, 4); break;
-      default: FGB_SDDMM(32, VN, 4); break;
+  for (int64_t c0 = 0; c0 < k; c0 += slab) {
+    const int64_t kw = k - c0 < slab ? k - c0 : slab;
+    const int mode = slab >= k ? 0 : c0 == 0 ? 1 : c0 + slab >= k ? 3 : 2;
+    const T* Xs = X + c0;
+    const T* Ys = Y + c0;
+#define FGB_SDDMM(LL, VV, UU)                                                                   \
+  sddmm_csr<T, PtrT, LL, VV, UU><<<grid, threads, 0, s>>>(nf, nnz, ptr, idx, val, Xs, ldx, Ys, \
+                                                          ldy, kw, out, base, chunk, mode)
+    if (vec_ok) {
+      switch (lanes) {
+        case 4: FGB_SDDMM(4, VN, 2); break;
+        case 8: FGB_SDDMM(8, VN, 2); break;
+        case 16: FGB_SDDMM(16, VN, 4); break;
+        default: FGB_SDDMM(32, VN, 4); break;
+      }
+    } else {
+      switch (lanes) {
+        case 4: FGB_SDDMM(4, 1, 2); break;
+        case 8: FGB_SDDMM(8, 1, 2); break;
+        case 16: FGB_SDDMM(16, 1, 4); break;
+        default: FGB_SDDMM(32, 1, 4); break;
+      }
     }
-  } else {
-    switch (lanes) {
-      case 4: FGB_SDDMM(4, 1, 2); break;
-      case 8: FGB_SDDMM(8, 1, 2); break;
-      case 16: FGB_SDDMM(16, 1, 4); break;
-      default: FGB_SDDMM(32, 1, 4); break;
-    }
-  }
 #undef FGB_SDDMM
-  return check_launch("sddmm_csr");
+    const int rc = check_launch("sddmm_csr");
+    if (rc) return rc;
+  }
+  return FGB_OK;
 }
 
 int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
                int64_t ldy, int64_t k, void* out, int dtype, unsigned flags, int lanes,
-               int64_t chunk, void* stream) {
+               int64_t chunk, void* stream, int64_t slab) {
   if (!ctx) return set_error(FGB_EINVAL, "fgb_sddmm: null ctx");
   int rc = check_sparse(A, "fgb_sddmm: A", true);
   if (rc) return rc;
@@ -201,19 +221,24 @@ int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, co
   const int64_t ldxc = A->orient == FGB_CSR ? ldx : ldy;
   const int64_t ldyc = A->orient == FGB_CSR ? ldy : ldx;
   cudaStream_t s = pick_stream(ctx, stream);
+  if (slab < 0) {  // default: slabs of one 128-byte line when Y is far larger than L2
+    const int64_t esz = dtype == FGB_F64 ? 8 : 4;
+    const int64_t ny = A->orient == FGB_CSR ? A->ncols : A->nrows;
+    slab = ((double)ny * (double)k * (double)esz > 256.0 * 1024 * 1024) ? 128 / esz : 0;
+  }
   if (dtype == FGB_F32) {
     if (A->ptr_t == FGB_I32)
       return run<float, int32_t>(ctx, A, (const float*)Xc, ldxc, (const float*)Yc, ldyc, k,
-                                 (float*)out, flags, lanes, chunk, s);
+                                 (float*)out, flags, lanes, chunk, slab, s);
     return run<float, int64_t>(ctx, A, (const float*)Xc, ldxc, (const float*)Yc, ldyc, k,
-                               (float*)out, flags, lanes, chunk, s);
+                               (float*)out, flags, lanes, chunk, slab, s);
   }
   if (dtype == FGB_F64) {
     if (A->ptr_t == FGB_I32)
       return run<double, int32_t>(ctx, A, (const double*)Xc, ldxc, (const double*)Yc, ldyc, k,
-                                  (double*)out, flags, lanes, chunk, s);
+                                  (double*)out, flags, lanes, chunk, slab, s);
     return run<double, int64_t>(ctx, A, (const double*)Xc, ldxc, (const double*)Yc, ldyc, k,
-                                (double*)out, flags, lanes, chunk, s);
+                                (double*)out, flags, lanes, chunk, slab, s);
   }
   return set_error(FGB_EUNSUPPORTED, "fgb_sddmm: dtype %d", dtype);
 }
@@ -223,5 +248,17 @@ int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, co
 extern "C" int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
                          const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                          unsigned flags, void* stream) {
-  return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, 0, 0, stream);
+  return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, 0, 0, stream, -1);
+}
+
+extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
+                            const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
+                            unsigned flags, const fgb_sddmm_tuning* tune, void* stream) {
+  const int lanes = tune ? tune->lanes : 0;
+  if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: lanes must be 0, 4, 8, 16 or 32");
+  if (tune && (tune->chunk < 0 || tune->slab < -1))
+    return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: negative chunk or slab");
+  return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, lanes,
+                         tune ? tune->chunk : 0, stream, tune ? tune->slab : -1);
 }

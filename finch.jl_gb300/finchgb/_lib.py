@@ -43,6 +43,10 @@ class FgbSpmmTuning(ctypes.Structure):
     _fields_ = [("lanes", c_int32), ("variant", c_int32), ("path", c_int64)]
 
 
+class FgbSddmmTuning(ctypes.Structure):
+    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("chunk", c_int64), ("slab", c_int64)]
+
+
 class FgbCgOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("max_iter", c_int64), ("chunk", c_int32),
                 ("precision", c_int32), ("replace_every", c_int64)]
@@ -123,6 +127,8 @@ SIGNATURES: dict[str, tuple] = {
                                  c_void_p, c_int64, c_int, c_uint, c_void_p]),
     "fgb_sddmm": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
                           c_int64, c_void_p, c_int, c_uint, c_void_p]),
+    "fgb_sddmm_ex": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
+                             c_int64, c_void_p, c_int, c_uint, POINTER(FgbSddmmTuning), c_void_p]),
     "fgb_ewise_count": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
                                 POINTER(c_int64), c_void_p]),
     "fgb_ewise_fill": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,

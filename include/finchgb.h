@@ -268,6 +268,22 @@ FGB_API int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B, i
 FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
               int64_t ldy, int64_t k, void* out_val, int dtype, unsigned flags, void* stream);
 
+/* Schedule knobs of SDDMM (the autotuner's search space): lanes per stored
+ * entry (4, 8, 16 or 32), stored entries per warp chunk, and the column slab
+ * (k per launch; the dot is accumulated across launches; 0 = all of k, -1 =
+ * the default: one 128-byte line of Y per launch when Y is far larger than
+ * L2).  Zero lanes/chunk take the defaults. */
+typedef struct fgb_sddmm_tuning {
+  int32_t lanes;
+  int32_t reserved;
+  int64_t chunk;
+  int64_t slab;
+} fgb_sddmm_tuning;
+
+FGB_API int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
+                         const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
+                         unsigned flags, const fgb_sddmm_tuning* tune, void* stream);
+
 /* Elementwise ops of two same-shape CSR/CSC matrices (same orientation). */
 typedef enum {
   FGB_EW_MUL = 0, /* C = A .* B   (stored where both are stored) */

@@ -213,6 +213,12 @@ def test_sddmm(gpu_lib, k, dtype):
     # Finch order: sequential dot, then the product with A -- bit-exact
     out2 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), flags=L.FINCH_ORDER))
     assert np.array_equal(out2, oracle.sddmm_csr(r.nrows, r.ptr, r.idx, r.val, X, Y))
+    # column slabs (dots accumulated across launches) and explicit schedules
+    vn = 4 if dtype == np.float32 else 1
+    for slab in (vn * 4, 32 // (8 // np.dtype(dtype).itemsize), k):
+        for lanes in (4, 8, 32):
+            out3 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), lanes=lanes, chunk=200, slab=slab))
+            assert_close(out3, want, scale, dtype)
 
 
 def test_sddmm_csc_swaps_roles(gpu_lib):
