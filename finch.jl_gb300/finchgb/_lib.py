@@ -129,6 +129,10 @@ SIGNATURES: dict[str, tuple] = {
                           c_int64, c_void_p, c_int, c_uint, c_void_p]),
     "fgb_sddmm_ex": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_int64, c_void_p, c_int64,
                              c_int64, c_void_p, c_int, c_uint, POINTER(FgbSddmmTuning), c_void_p]),
+    "fgb_spgemm_symbolic": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
+                                    POINTER(c_int64), c_void_p]),
+    "fgb_spgemm_numeric": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_int, c_uint,
+                                   POINTER(FgbSparse), c_void_p]),
     "fgb_ewise_count": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,
                                 POINTER(c_int64), c_void_p]),
     "fgb_ewise_fill": (c_int, [c_void_p, c_int, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p,

@@ -267,6 +267,26 @@ def sddmm(A: DeviceSparse, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor |
     return out
 
 
+def spgemm(A: DeviceSparse, B: DeviceSparse, flags: int = 0) -> DeviceSparse:
+    """C = A * B (Gustavson, plus-times), same orientation and base as A."""
+    ctx = _ctx_for(A.idx)
+    d = A.idx.device
+    nf = A.nrows if A.orient == "csr" else B.ncols
+    c_ptr = torch.empty(nf + 1, dtype=torch.int64, device=d)
+    nnz = ctypes.c_int64()
+    da, db = A.desc(), B.desc()
+    L.call("fgb_spgemm_symbolic", ctx, ctypes.byref(da), ctypes.byref(db), c_ptr.data_ptr(),
+           ctypes.byref(nnz), stream_ptr())
+    k = nnz.value
+    c_idx = torch.empty(max(k, 1), dtype=torch.int32, device=d)
+    c_val = torch.empty(max(k, 1), dtype=A.val.dtype, device=d)
+    dc = L.FgbSparse(A.nrows, B.ncols, k, L.CSR if A.orient == "csr" else L.CSC, A.base, L.I64,
+                     L.I32, dtype_code(c_val), 0, c_ptr.data_ptr(), c_idx.data_ptr(), c_val.data_ptr())
+    L.call("fgb_spgemm_numeric", ctx, ctypes.byref(da), ctypes.byref(db), dtype_code(A.val), flags,
+           ctypes.byref(dc), stream_ptr())
+    return DeviceSparse(A.nrows, B.ncols, c_ptr, c_idx[:k], c_val[:k], A.orient, A.base)
+
+
 def ewise(op: int, A: DeviceSparse, B: DeviceSparse) -> DeviceSparse:
     """C = A .* B (op EW_MUL) or A .+ B (EW_ADD) of two same-shape matrices."""
     ctx = _ctx_for(A.idx)

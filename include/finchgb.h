@@ -284,6 +284,21 @@ FGB_API int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64
                          const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                          unsigned flags, const fgb_sddmm_tuning* tune, void* stream);
 
+/* SpGEMM C = A * B (plus-times), Gustavson's algorithm as Finch writes it
+ * (docs/examples/spgemm.jl:56-72, test/suites/kernel_tests.jl:89-129): every
+ * output accumulates its products in the order of the shared index k, so F64
+ * and F32 results equal the serial nest's for the same fused (default) or
+ * FGB_NO_FMA choice; touched coordinates are stored even where they sum to
+ * zero.  A and B share an orientation (CSR -> CSR, CSC -> CSC), a ptr type
+ * and int32 indices.  Two calls: the symbolic one writes C's ptr (int64,
+ * n_fibers + 1, in A's index base) and returns nnz(C); the caller allocates
+ * C's idx (int32) and values and the numeric one fills them, each fiber's
+ * coordinates ascending.  Both synchronous. */
+FGB_API int fgb_spgemm_symbolic(fgb_ctx* ctx, const fgb_sparse* A, const fgb_sparse* B,
+                                int64_t* c_ptr, int64_t* nnz_c, void* stream);
+FGB_API int fgb_spgemm_numeric(fgb_ctx* ctx, const fgb_sparse* A, const fgb_sparse* B, int dtype,
+                               unsigned flags, fgb_sparse* C, void* stream);
+
 /* Elementwise ops of two same-shape CSR/CSC matrices (same orientation). */
 typedef enum {
   FGB_EW_MUL = 0, /* C = A .* B   (stored where both are stored) */

@@ -65,6 +65,8 @@ def lib() -> ctypes.CDLL:
             L.orc_max_threads.argtypes = []
             L.orc_coo_assemble.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp, vp, vp, vp]
             L.orc_coo_assemble.restype = i64
+            L.orc_spgemm_csr.argtypes = [i32, i32, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+            L.orc_spgemm_csr.restype = i64
             _lib = L
     return _lib
 
@@ -191,3 +193,18 @@ def coo_assemble(m, n, I, J, V, csc=True, combine=0):
     if q < 0:
         raise ValueError("coordinate out of range")
     return ptr, idx[:q], (None if val is None else val[:q])
+
+
+def spgemm_csr(m, n, lp, li, lv, rp, ri, rv, fma=True):
+    """Gustavson's row-form SpGEMM of CSR buffers (1-based): (ptr, idx, val)
+    of C = L * R with m rows and n columns, sums in the order of k."""
+    lp, li, rp, ri = _i64(lp), _i64(li), _i64(rp), _i64(ri)
+    lv, rv = np.ascontiguousarray(lv), np.ascontiguousarray(rv)
+    ptr = np.zeros(m + 1, dtype=np.int64)
+    nnz = lib().orc_spgemm_csr(dtype_code(lv), int(fma), m, n, _p(lp), _p(li), _p(lv), _p(rp),
+                               _p(ri), _p(rv), _p(ptr), None, None)
+    idx = np.zeros(max(nnz, 1), dtype=np.int64)
+    val = np.zeros(max(nnz, 1), dtype=lv.dtype)
+    lib().orc_spgemm_csr(dtype_code(lv), int(fma), m, n, _p(lp), _p(li), _p(lv), _p(rp), _p(ri),
+                         _p(rv), _p(ptr), _p(idx), _p(val))
+    return ptr, idx[:nnz], val[:nnz]

@@ -506,6 +506,76 @@ int64_t orc_coo_assemble(int csc, int vt, int combine, int64_t m, int64_t n, int
   return q;
 }
 
+/*
+ * Gustavson's SpGEMM, the nest of docs/examples/spgemm.jl:56-72 in its row
+ * form on CSR buffers: for every row r, w .= 0; for k in L[r,:] (stored
+ * order), for c in R[k,:]: w[c] += L[r,k] * R[k,c]; then the touched
+ * coordinates of w, ascending, are the row of C (stored even when they sum
+ * to zero).  Finch's column form on CSC operands is this nest on the
+ * transposed problem.  F64 (vt 0) or F32 (vt 1) values, fused (`fma`) or
+ * not.  Pass out_idx = NULL to count only.  Returns nnz(C).
+ */
+int64_t orc_spgemm_csr(int vt, int fma, int64_t m, int64_t n, const int64_t* lp, const int64_t* li,
+                       const void* lv, const int64_t* rp, const int64_t* ri, const void* rv,
+                       int64_t* out_ptr, int64_t* out_idx, void* out_val) {
+  double* wd = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+  float* wf = (float*)calloc((size_t)(n > 0 ? n : 1), sizeof(float));
+  unsigned char* seen = (unsigned char*)calloc((size_t)(n > 0 ? n : 1), 1);
+  int64_t* list = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  int64_t q = 0;
+  out_ptr[0] = 1;
+  for (int64_t r = 0; r < m; ++r) {
+    int64_t cnt = 0;
+    for (int64_t a = lp[r]; a < lp[r + 1]; ++a) {
+      const int64_t k = li[a - 1] - 1;
+      for (int64_t b = rp[k]; b < rp[k + 1]; ++b) {
+        const int64_t c = ri[b - 1] - 1;
+        if (!seen[c]) {
+          seen[c] = 1;
+          list[cnt++] = c;
+          wd[c] = 0.0;
+          wf[c] = 0.0f;
+        }
+        if (out_idx) {
+          if (vt == T_F64) {
+            const double x = ((const double*)lv)[a - 1], y = ((const double*)rv)[b - 1];
+            wd[c] = fma ? __builtin_fma(y, x, wd[c]) : wd[c] + y * x;
+          } else {
+            const float x = ((const float*)lv)[a - 1], y = ((const float*)rv)[b - 1];
+            wf[c] = fma ? __builtin_fmaf(y, x, wf[c]) : wf[c] + y * x;
+          }
+        }
+      }
+    }
+    /* ascending coordinates: counting over the touched list */
+    for (int64_t t = 1; t < cnt; ++t) {
+      const int64_t v = list[t];
+      int64_t u = t - 1;
+      while (u >= 0 && list[u] > v) {
+        list[u + 1] = list[u];
+        --u;
+      }
+      list[u + 1] = v;
+    }
+    for (int64_t t = 0; t < cnt; ++t) {
+      const int64_t c = list[t];
+      if (out_idx) {
+        out_idx[q] = c + 1;
+        if (vt == T_F64) ((double*)out_val)[q] = wd[c];
+        else ((float*)out_val)[q] = wf[c];
+      }
+      seen[c] = 0;
+      ++q;
+    }
+    out_ptr[r + 1] = q + 1;
+  }
+  free(wd);
+  free(wf);
+  free(seen);
+  free(list);
+  return q;
+}
+
 /* Threads available to the OpenMP runtime (1 without OpenMP). */
 int orc_max_threads(void) {
 #ifdef _OPENMP
