@@ -885,11 +885,45 @@ def suite_coo() -> list[dict]:
                               "sample": "first 2M triplets, fsparse contract (oracle stable merge sort + fold)"}}]
 
 
+def suite_spgemm() -> list[dict]:
+    """C = A * A for the 2048^2 5-point Poisson matrix (FP64, CSR), Gustavson."""
+    import torch
+
+    import oracle
+    from finchgb import device as dev
+    from finchgb.workloads import poisson2d
+
+    P = poisson2d(2048)
+    A = dev.DeviceSparse.from_host(P.nrows, P.ncols, P.ptr, P.idx, P.val, orient="csr")
+    C = dev.spgemm(A, A)
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dev.spgemm(A, A)  # synchronous: symbolic, allocation, numeric, row sort
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    products = int(np.sum(np.diff(P.ptr)[P.idx - 1] * 1))  # sum over entries of |row k|
+    nbytes = 2 * (12 * P.nnz + 8 * (P.nrows + 1)) + 12 * C.nnz + 8 * (P.nrows + 1)
+    rows = 200_000
+    t = _cpu_time(lambda: oracle.spgemm_csr(rows, P.ncols, P.ptr[: rows + 1], P.idx, P.val, P.ptr,
+                                            P.idx, P.val), min_seconds=2.0, max_reps=3)
+    t_full = t * P.nrows / rows
+    return [{"suite": "spgemm_poisson2048_squared", "metric": "spgemm_products_per_s", "unit": "Gproducts/s",
+             "value": round(products / (ms / 1e3) / 1e9, 3), "ms_per_call": round(ms, 3),
+             "products": products, "nnz_A": int(P.nnz), "nnz_C": int(C.nnz), "dtype": "f64",
+             "config": {"workload": "2048^2 5-point Poisson CSR (FP64) times itself"},
+             "timing": "host wall time of the synchronous symbolic + numeric calls",
+             "roofline": _roof(nbytes, ms),
+             "cpu_baseline": {"value": round(products / t_full / 1e9, 4), "unit": "Gproducts/s",
+                              "cores": 1, "kind": "port",
+                              "sample": "rows 1..200000 (Gustavson nest, oracle), scaled by rows"}}]
+
+
 def run_suite(args):
     from finchgb import build
 
     build.build()
-    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo):
+    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm):
         if args.suite_only and fn.__name__ not in args.suite_only.split(","):
             continue
         try:

@@ -17,7 +17,8 @@
 // accumulates its products in k order without atomics, exactly Gustavson's
 // order: bit-identical to the serial nest for the same fused/unfused
 // choice.  Touched keys are stored even if their sum is zero (like the
-// workspace).  A segmented sort then orders every row's columns.
+// workspace).  A warp writes each pair at its rank among the row's keys, so
+// small rows come out ordered; a segmented sort orders the large rows.
 #include <cub/cub.cuh>
 
 #include "fgb_internal.cuh"
@@ -128,7 +129,16 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
     for (int64_t s = tid; s < cap; s += nthreads) {
       const int32_t c = keys[s];
       if (c != SG_EMPTY) {
-        const int o = atomicAdd(cnt, 1);
+        int o;
+        if (warp) {  // small table: the rank among the row's keys is the sorted position
+          o = 0;
+          for (int64_t t = 0; t < cap; ++t) {
+            const int32_t d = keys[t];
+            o += (d != SG_EMPTY && d < c) ? 1 : 0;
+          }
+        } else {  // large rows: unsorted here, ordered by a segmented sort afterwards
+          o = atomicAdd(cnt, 1);
+        }
         out_idx[out_pos + o] = c + out_base;
         out_val[out_pos + o] = vals[s];
       }
@@ -150,9 +160,12 @@ __global__ void __launch_bounds__(SG_WARPS * 32) sg_warp_k(
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nw = (int64_t)gridDim.x * SG_WARPS;
   for (int64_t r = blockIdx.x * (int64_t)SG_WARPS + w; r < m; r += nw) {
-    if (ub[r] > SG_WARP_UB) continue;  // warp-uniform
+    const int64_t u = ub[r];
+    if (u > SG_WARP_UB) continue;  // warp-uniform
+    int64_t cap = 32;  // a table sized to the row: at least twice its bound
+    while (cap < 2 * u) cap <<= 1;
     sg_row<T, PtrT, SYMB>(r, lane, 32, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[w],
-                          SYMB ? nullptr : &s_vals[SYMB ? 0 : w][0], SG_WARP_SLOTS, fm, &s_cnt[w],
+                          SYMB ? nullptr : &s_vals[SYMB ? 0 : w][0], cap, fm, &s_cnt[w],
                           out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, true);
     if (SYMB && lane == 0) cnt_out[r] = s_cnt[w];
   }
@@ -174,6 +187,18 @@ __global__ void __launch_bounds__(SG_BLOCK) sg_block_k(
                           gkeys + off, SYMB ? nullptr : gvals + off, cap, fm, &s_cnt, out_base,
                           out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, false);
     if (SYMB && threadIdx.x == 0) cnt_out[r] = s_cnt;
+  }
+}
+
+// Segment bounds for the final sort: the block-tier rows only (warp-tier
+// rows are written in order already and become empty segments).
+__global__ void sg_segs_k(int64_t m, const int64_t* __restrict__ ub, const int64_t* __restrict__ cptr,
+                          int base, int64_t* __restrict__ sb, int64_t* __restrict__ se) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const bool big = ub[r] > SG_WARP_UB;
+    sb[r] = cptr[r] - base;
+    se[r] = big ? cptr[r + 1] - base : cptr[r] - base;
   }
 }
 
@@ -353,34 +378,41 @@ extern "C" int fgb_spgemm_numeric(fgb_ctx* ctx, const fgb_sparse* A, const fgb_s
   }
 #undef SG_NUM
   cudaError_t e = cudaGetLastError();
-  // order every row's columns (keys compared with the base added: same order)
-  if (e == cudaSuccess && C->nnz > 0) {
-    int64_t* seg = nullptr;  // 0-based row offsets
+  // order the large rows' columns (keys compared with the base added: same order)
+  int64_t n_big = 0;
+  if (e == cudaSuccess && C->nnz > 0) e = cudaMemcpyAsync(&n_big, S.goff + P.m, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && C->nnz > 0 && n_big > 0) {
+    int64_t* seg = nullptr;  // begin offsets, then end offsets (0-based)
     int32_t* k2 = nullptr;
     void* v2 = nullptr;
     void* tmp = nullptr;
     size_t tb = 0;
     const int nseg = (int)P.m;
     const int nnz = (int)C->nnz;
-    e = cudaMallocAsync((void**)&seg, 8 * (P.m + 1), s);
+    e = cudaMallocAsync((void**)&seg, 16 * (P.m + 1), s);
+    int64_t* seg_end = seg + (P.m + 1);
     if (e == cudaSuccess) {
-      sg_rebase_k<<<grid_for(P.m + 1, 256, ctx->num_sms), 256, 0, s>>>(P.m + 1, cptr, ob, seg);
+      sg_segs_k<<<grid_for(P.m, 256, ctx->num_sms), 256, 0, s>>>(P.m, S.ub, cptr, ob, seg, seg_end);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&k2, 4 * (size_t)nnz, s);
     if (e == cudaSuccess) e = cudaMallocAsync(&v2, esz * (size_t)nnz, s);
+    // the sort writes only items inside segments: the small rows keep these copies
+    if (e == cudaSuccess) e = cudaMemcpyAsync(k2, cidx, 4 * (size_t)nnz, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v2, C->val, esz * (size_t)nnz, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) {
       if (dtype == FGB_F64)
-        cub::DeviceSegmentedSort::SortPairs(nullptr, tb, cidx, k2, (const double*)C->val, (double*)v2, nnz, nseg, seg, seg + 1, s);
+        cub::DeviceSegmentedSort::SortPairs(nullptr, tb, cidx, k2, (const double*)C->val, (double*)v2, nnz, nseg, seg, seg_end, s);
       else
-        cub::DeviceSegmentedSort::SortPairs(nullptr, tb, cidx, k2, (const float*)C->val, (float*)v2, nnz, nseg, seg, seg + 1, s);
+        cub::DeviceSegmentedSort::SortPairs(nullptr, tb, cidx, k2, (const float*)C->val, (float*)v2, nnz, nseg, seg, seg_end, s);
       e = cudaMallocAsync(&tmp, tb ? tb : 1, s);
     }
     if (e == cudaSuccess) {
       if (dtype == FGB_F64)
-        e = cub::DeviceSegmentedSort::SortPairs(tmp, tb, cidx, k2, (const double*)C->val, (double*)v2, nnz, nseg, seg, seg + 1, s);
+        e = cub::DeviceSegmentedSort::SortPairs(tmp, tb, cidx, k2, (const double*)C->val, (double*)v2, nnz, nseg, seg, seg_end, s);
       else
-        e = cub::DeviceSegmentedSort::SortPairs(tmp, tb, cidx, k2, (const float*)C->val, (float*)v2, nnz, nseg, seg, seg + 1, s);
+        e = cub::DeviceSegmentedSort::SortPairs(tmp, tb, cidx, k2, (const float*)C->val, (float*)v2, nnz, nseg, seg, seg_end, s);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(cidx, k2, 4 * (size_t)nnz, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(const_cast<void*>(C->val), v2, esz * (size_t)nnz, cudaMemcpyDeviceToDevice, s);
