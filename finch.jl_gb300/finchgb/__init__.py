@@ -3,6 +3,7 @@
 Finch-facing API (mirrors Finch.jl names):
   levels     Dense, SparseList, SparseCOO, Element, Pattern
   tensors    Tensor, swizzle, csr, fsparse, fsprand, transfer, gpu
+  fileio     fread, fwrite (.bspnpy, .mtx/.ttx, .tns)
   front ends einsum (@einsum), lazy/compute, finch (@finch programs),
              tensordot, reduce, permutedims, broadcast, minimum, maximum
   scheduler  GB300Scheduler, set_scheduler, with_scheduler, Scalar
@@ -13,6 +14,7 @@ Lower layers:
 """
 from . import _lib
 from ._lib import FinchGBError
+from .fileio import FinchExtensionError, fread, fwrite
 from .device import DeviceSparse, context, ewise, ewise_reduce, sddmm, spmm, spmv
 from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, reduce, tensordot
 from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, default_scheduler,
@@ -25,6 +27,6 @@ __all__ = [
     "ewise", "ewise_reduce", "LazyTensor", "lazy", "compute", "einsum", "finch", "tensordot",
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",
     "default_scheduler", "get_scheduler", "set_scheduler", "with_scheduler", "GPU", "Dense",
-    "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsparse", "fsprand",
+    "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsparse", "fsprand", "fread", "fwrite", "FinchExtensionError",
     "gpu", "swizzle", "transfer", "_lib",
 ]

@@ -107,9 +107,14 @@ def main(ref: Path) -> None:
                       "dims2": _after("reduce(+, A, dims = 2)"),
                       "all": _floats(next(p for p in parts if p.startswith("reduce(+, A, dims = (:))")).splitlines()[1])[0]}
 
+    # 6. fwrite of Trec4 read from its .mtx: the canonical TensorMarket text
+    #    (test/suites/fileio_tests.jl:164-168 checks it against this fixture)
+    kats["trec4_ttx"] = {"file": "test/reference64/fileio/Trec4.ttx",
+                         "text": (ref / "test/reference64/fileio/Trec4.ttx").read_text()}
+
     (HERE / "finch_kats.json").write_text(json.dumps(out, indent=1))
 
-    # 6. MatrixMarket matrices used by Finch's kernel tests (kernel_tests.jl)
+    # 7. MatrixMarket matrices used by Finch's kernel tests (kernel_tests.jl)
     for rel in ["HB/west0132", "LPnetlib/lpi_itest6", "LPnetlib/lp_blend", "JGD_Kocay/Trec4"]:
         lines = [ln for ln in (ref / "test/data" / f"{rel}.mtx").read_text().splitlines()
                  if ln and not ln.startswith("%")]
