@@ -142,6 +142,16 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
       return spmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype, d.flags,
                        c.lanes, 0, s);
     case FGB_PLAN_SDDMM:
+      if (c.variant == 3) {  // virtual rows (schedule built outside capture)
+        auto it = p->vrows.find(c.path);
+        if (it == p->vrows.end()) {
+          VrowSchedule v;
+          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s);
+          if (rc) return rc;
+          it = p->vrows.emplace(c.path, v).first;
+        }
+        return sddmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, s);
+      }
       return sddmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, d.dtype,
                         d.flags, c.lanes, c.path, s,
                         c.variant == 2 ? 128 / (d.dtype == FGB_F64 ? 8 : 4) : 0);
@@ -185,6 +195,9 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{l, chunk});
     if (d.k * (d.dtype == FGB_F64 ? 8 : 4) > 128)  // column slabs of one 128-byte line
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{d.dtype == FGB_F64 ? 16 : 8, chunk, 1, 2});
+    if (d.dtype == FGB_F32 && p->A.orient == FGB_CSR && p->A.val_t == FGB_F32 && d.k <= 128 &&
+        d.k % 4 == 0 && d.ld_in0 % 4 == 0 && d.ld_in1 % 4 == 0 && p->A.nnz <= INT32_MAX)
+      for (int64_t t : {64, 128, 256}) out.push_back(Choice{0, t, 1, 3});  // virtual rows
   }
   return out;
 }
@@ -299,7 +312,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   }
   p->choice = best;
   for (auto it = p->vrows.begin(); it != p->vrows.end();) {  // and the chosen schedule
-    if (best.variant != 2 || it->first != best.path) {
+    if ((best.variant != 2 && best.variant != 3) || it->first != best.path) {
       vrow_free(&it->second);
       it = p->vrows.erase(it);
     } else {

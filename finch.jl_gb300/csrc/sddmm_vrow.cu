@@ -1,0 +1,96 @@
+// SDDMM over the virtual-row schedule of the slab SpMM (FP32, CSR, k <= 128,
+// k a multiple of 4).
+//
+// out[e] = A.val[e] * <X[i,:], Y[j,:]>.  A sub-group of L lanes (4 columns
+// of k per lane) takes one virtual row -- at most T stored entries of one
+// row -- so the row's slice of X is loaded once into registers and every
+// entry only gathers its row of Y.  NB entries are in flight per sub-group;
+// each dot product is reduced over the L lanes with xor-shuffles (a fixed
+// tree: deterministic).  Virtual rows are sorted by length class, so the
+// sub-groups of a warp run similar trip counts.
+#include "spmm_common.cuh"
+
+namespace fgb {
+
+constexpr int SV_THREADS = 256;
+
+template <int L, int NB>
+__global__ void __launch_bounds__(SV_THREADS, 4) sddmm_vrow_k(
+    int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx, const float* __restrict__ val,
+    const float* __restrict__ X, int64_t ldx, const float* __restrict__ Y, int64_t ldy, int64_t k,
+    float* __restrict__ out, int base) {
+  const int lane = threadIdx.x & 31, sl = lane % L;
+  const unsigned gmask = group_mask<L>();
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / L;
+  const int64_t col = (int64_t)sl * 4;
+  const bool active = col < k;
+  const uint64_t pol_stream = policy_evict_first();
+  const uint64_t pol_keep = policy_evict_last();
+  for (int64_t v = gid; v < nv; v += ngroups) {
+    const int4 rec = __ldg(vr + v);  // row, first entry, length, (slot: unused here)
+    float4 xr = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) xr = __ldg(reinterpret_cast<const float4*>(X + (int64_t)rec.x * ldx + col));
+    for (int t = 0; t < rec.z; t += NB) {
+      float d[NB];
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        d[u] = 0.f;
+        if (t + u < rec.z && active) {
+          const int j = __ldg(idx + rec.y + t + u) - base;
+          const float4 y = ld_gather_f32x4(Y + (int64_t)j * ldy + col, pol_keep);
+          d[u] = __fmaf_rn(xr.x, y.x, __fmaf_rn(xr.y, y.y, __fmaf_rn(xr.z, y.z, xr.w * y.w)));
+        }
+      }
+#pragma unroll
+      for (int m = L / 2; m >= 1; m >>= 1)
+#pragma unroll
+        for (int u = 0; u < NB; ++u) d[u] += __shfl_xor_sync(gmask, d[u], m, L);
+      if (sl < NB && t + sl < rec.z) {  // lane u of the sub-group stores entry t + u
+        float mine = d[0];
+#pragma unroll
+        for (int u = 1; u < NB; ++u)
+          if (sl == u) mine = d[u];
+        const int64_t e = (int64_t)rec.y + t + sl;
+        __stcs(out + e, __fmul_rn(ld_stream_f32(val + e, pol_stream), mine));
+      }
+    }
+  }
+}
+
+template <int L>
+static int launch_sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* X,
+                             int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
+                             cudaStream_t s) {
+  constexpr int NB = L >= 4 ? 4 : L;
+  static int occ = -1;  // per process: one device model
+  if (occ < 0) {
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_k<L, NB>, SV_THREADS, 0);
+    occ = o > 0 ? o : 1;
+  }
+  const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
+  sddmm_vrow_k<L, NB><<<grid, SV_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val,
+                                                  X, ldx, Y, ldy, k, out, A->index_base);
+  FGB_CUDA_TRY(cudaGetLastError());
+  return FGB_OK;
+}
+
+int sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* X, int64_t ldx,
+               const void* Y, int64_t ldy, int64_t k, void* out, cudaStream_t s) {
+  if (A->orient != FGB_CSR || A->val_t != FGB_F32 || A->idx_t != FGB_I32)
+    return set_error(FGB_EUNSUPPORTED, "sddmm vrow: CSR with F32 values and int32 indices only");
+  if (k <= 0 || k > 128 || k % 4 || ldx % 4 || ldy % 4 || (uintptr_t)X % 16 || (uintptr_t)Y % 16)
+    return set_error(FGB_EUNSUPPORTED, "sddmm vrow: needs k in (0, 128], a multiple of 4, and 16-byte rows");
+  const float* x = (const float*)X;
+  const float* y = (const float*)Y;
+  float* o = (float*)out;
+  const int64_t need = k / 4;
+  if (need <= 4) return launch_sddmm_vrow<4>(ctx, v, A, x, ldx, y, ldy, k, o, s);
+  if (need <= 8) return launch_sddmm_vrow<8>(ctx, v, A, x, ldx, y, ldy, k, o, s);
+  if (need <= 16) return launch_sddmm_vrow<16>(ctx, v, A, x, ldx, y, ldy, k, o, s);
+  return launch_sddmm_vrow<32>(ctx, v, A, x, ldx, y, ldy, k, o, s);
+}
+
+}  // namespace fgb

@@ -44,7 +44,7 @@ class FgbSpmmTuning(ctypes.Structure):
 
 
 class FgbSddmmTuning(ctypes.Structure):
-    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("chunk", c_int64), ("slab", c_int64)]
+    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("chunk", c_int64), ("slab", c_int64)]
 
 
 class FgbCgOptions(ctypes.Structure):

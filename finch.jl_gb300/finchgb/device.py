@@ -254,13 +254,15 @@ class Panels:
 
 
 def sddmm(A: DeviceSparse, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
-          flags: int = 0, lanes: int = 0, chunk: int = 0, slab: int = -1) -> torch.Tensor:
+          flags: int = 0, lanes: int = 0, chunk: int = 0, slab: int = -1,
+          variant: int = 0) -> torch.Tensor:
     """out[e] = A.val[e] * <X[i,:], Y[j,:]> over A's stored entries
-    (lanes/chunk/slab override the schedule; slab 0 = all of k per launch)."""
+    (lanes/chunk/slab/variant override the schedule; slab 0 = all of k per
+    launch; variant 1 = virtual rows of at most `chunk` entries)."""
     if out is None:
         out = torch.empty(A.nnz, dtype=X.dtype, device=X.device)
     d = A.desc()
-    tune = L.FgbSddmmTuning(lanes, 0, chunk, slab)
+    tune = L.FgbSddmmTuning(lanes, variant, chunk, slab)
     L.call("fgb_sddmm_ex", _ctx_for(X), ctypes.byref(d), _dptr(X), X.stride(0), _dptr(Y),
            Y.stride(0), X.shape[1], _dptr(out), dtype_code(X), flags, ctypes.byref(tune),
            stream_ptr())

@@ -268,14 +268,17 @@ FGB_API int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B, i
 FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, const void* Y,
               int64_t ldy, int64_t k, void* out_val, int dtype, unsigned flags, void* stream);
 
-/* Schedule knobs of SDDMM (the autotuner's search space): lanes per stored
- * entry (4, 8, 16 or 32), stored entries per warp chunk, and the column slab
- * (k per launch; the dot is accumulated across launches; 0 = all of k, -1 =
- * the default: one 128-byte line of Y per launch when Y is far larger than
- * L2).  Zero lanes/chunk take the defaults. */
+/* Schedule knobs of SDDMM (the autotuner's search space).  variant 0: warps
+ * own chunks of `chunk` stored entries, `lanes` lanes (4, 8, 16 or 32) per
+ * entry, and `slab` columns of k per launch (the dot accumulated across
+ * launches; 0 = all of k, -1 = the default: one 128-byte line of Y per launch
+ * when Y is far larger than L2).  variant 1 (F32 CSR, k <= 128 and a multiple
+ * of 4): sub-groups own virtual rows of at most `chunk` entries, sorted by
+ * length, holding the row's slice of X in registers.  Zero lanes/chunk take
+ * the defaults. */
 typedef struct fgb_sddmm_tuning {
   int32_t lanes;
-  int32_t reserved;
+  int32_t variant;
   int64_t chunk;
   int64_t slab;
 } fgb_sddmm_tuning;

@@ -219,6 +219,15 @@ def test_sddmm(gpu_lib, k, dtype):
         for lanes in (4, 8, 32):
             out3 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), lanes=lanes, chunk=200, slab=slab))
             assert_close(out3, want, scale, dtype)
+    # virtual rows (X's row held in registers): F32, k a multiple of 4 up to 128
+    if dtype == np.float32 and k % 4 == 0:
+        for T in (8, 64, 200):
+            out4 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1))
+            assert_close(out4, want, scale, dtype)
+            assert np.array_equal(out4, to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1)))
+    else:
+        with pytest.raises(L.FinchGBError):
+            dev.sddmm(A, to_dev(X), to_dev(Y), chunk=64, variant=1)
 
 
 def test_sddmm_csc_swaps_roles(gpu_lib):
