@@ -9,8 +9,8 @@
 // problem C^T = B^T A^T, whose CSR buffers are A's and B's CSC buffers.
 //
 // Per output row: an upper bound ub = sum of |R[k,:]| over the row's k picks
-// a tier -- a warp with a hash table in shared memory (ub <= 256), or a
-// block with a hash table in global scratch.  The symbolic pass inserts the
+// a tier -- 8 lanes (ub <= 64) or a warp (ub <= 256) with a hash table in
+// shared memory, or a block with a hash table in global scratch.  The symbolic pass inserts the
 // column keys and counts them (C's ptr); the numeric pass walks the row's k
 // in storage order, one k at a time (a barrier between them), with the
 // lanes spread over R[k,:] -- every column occurs once per k, so each output
@@ -28,6 +28,7 @@ namespace fgb {
 
 constexpr int SG_WARP_SLOTS = 512;  // hash slots per warp (ub <= SG_WARP_UB)
 constexpr int SG_WARP_UB = 256;
+constexpr int SG_SMALL_UB = 64;      // rows up to this bound take 8 lanes (128 slots)
 constexpr int SG_WARPS = 4;          // warps per block of the warp tier
 constexpr int SG_BLOCK = 256;        // threads of the block tier
 constexpr int32_t SG_EMPTY = -1;
@@ -100,9 +101,11 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
                        const PtrT* __restrict__ rp, const int* __restrict__ ri,
                        const T* __restrict__ rv, int rbase, int32_t* keys, T* vals, int64_t cap,
                        int fm, int* cnt, int out_base, int32_t* __restrict__ out_idx,
-                       T* __restrict__ out_val, int64_t out_pos, bool warp) {
+                       T* __restrict__ out_val, int64_t out_pos, unsigned smask) {
+  // smask: the lanes of a (sub-)warp group; 0 for a whole block
+  const bool warp = smask != 0;
   auto sync = [&]() {
-    if (warp) __syncwarp(); else __syncthreads();
+    if (warp) __syncwarp(smask); else __syncthreads();
   };
   for (int64_t s = tid; s < cap; s += nthreads) keys[s] = SG_EMPTY;
   if (tid == 0) *cnt = 0;
@@ -147,27 +150,32 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
   sync();
 }
 
-template <class T, class PtrT, bool SYMB>
+// Rows whose bound lies in (LO, HI] with G lanes per row (32 / G rows per
+// warp), each group with a table of 16 * G slots in shared memory.
+template <class T, class PtrT, bool SYMB, int G>
 __global__ void __launch_bounds__(SG_WARPS * 32) sg_warp_k(
-    int64_t m, const int64_t* __restrict__ ub, const PtrT* __restrict__ lp, const int* __restrict__ li,
-    const T* __restrict__ lv, int lbase, const PtrT* __restrict__ rp, const int* __restrict__ ri,
-    const T* __restrict__ rv, int rbase, int fm, int64_t* __restrict__ cnt_out,
-    const int64_t* __restrict__ cptr, int out_base, int32_t* __restrict__ out_idx,
-    T* __restrict__ out_val) {
-  __shared__ int32_t s_keys[SG_WARPS][SG_WARP_SLOTS];
-  __shared__ T s_vals[SYMB ? 1 : SG_WARPS][SYMB ? 1 : SG_WARP_SLOTS];
-  __shared__ int s_cnt[SG_WARPS];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t nw = (int64_t)gridDim.x * SG_WARPS;
-  for (int64_t r = blockIdx.x * (int64_t)SG_WARPS + w; r < m; r += nw) {
+    int64_t m, const int64_t* __restrict__ ub, int64_t lo, int64_t hi, const PtrT* __restrict__ lp,
+    const int* __restrict__ li, const T* __restrict__ lv, int lbase, const PtrT* __restrict__ rp,
+    const int* __restrict__ ri, const T* __restrict__ rv, int rbase, int fm,
+    int64_t* __restrict__ cnt_out, const int64_t* __restrict__ cptr, int out_base,
+    int32_t* __restrict__ out_idx, T* __restrict__ out_val) {
+  constexpr int NG = SG_WARPS * 32 / G;      // groups per block
+  constexpr int SLOTS = SG_WARP_SLOTS * G / 32;
+  __shared__ int32_t s_keys[NG][SLOTS];
+  __shared__ T s_vals[SYMB ? 1 : NG][SYMB ? 1 : SLOTS];
+  __shared__ int s_cnt[NG];
+  const int grp = threadIdx.x / G, gl = threadIdx.x % G;
+  const unsigned gmask = group_mask<G>();
+  const int64_t ngr = (int64_t)gridDim.x * NG;
+  for (int64_t r = blockIdx.x * (int64_t)NG + grp; r < m; r += ngr) {
     const int64_t u = ub[r];
-    if (u > SG_WARP_UB) continue;  // warp-uniform
-    int64_t cap = 32;  // a table sized to the row: at least twice its bound
+    if (u <= lo || u > hi) continue;  // group-uniform
+    int64_t cap = 16;  // a table sized to the row: at least twice its bound
     while (cap < 2 * u) cap <<= 1;
-    sg_row<T, PtrT, SYMB>(r, lane, 32, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[w],
-                          SYMB ? nullptr : &s_vals[SYMB ? 0 : w][0], cap, fm, &s_cnt[w],
-                          out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, true);
-    if (SYMB && lane == 0) cnt_out[r] = s_cnt[w];
+    sg_row<T, PtrT, SYMB>(r, gl, G, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[grp],
+                          SYMB ? nullptr : &s_vals[SYMB ? 0 : grp][0], cap, fm, &s_cnt[grp],
+                          out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, gmask);
+    if (SYMB && gl == 0) cnt_out[r] = s_cnt[grp];
   }
 }
 
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(SG_BLOCK) sg_block_k(
     const int64_t off = goff[r], cap = goff[r + 1] - off;
     sg_row<T, PtrT, SYMB>(r, threadIdx.x, SG_BLOCK, lp, li, lv, lbase, rp, ri, rv, rbase,
                           gkeys + off, SYMB ? nullptr : gvals + off, cap, fm, &s_cnt, out_base,
-                          out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, false);
+                          out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, 0u);
     if (SYMB && threadIdx.x == 0) cnt_out[r] = s_cnt;
   }
 }
@@ -276,11 +284,17 @@ template <class T, class PtrT, bool SYMB>
 static void sg_launch(fgb_ctx* ctx, const SgProblem& P, const SgScratch& S, int fm, const int64_t* cptr,
                       int out_base, int32_t* out_idx, T* out_val, cudaStream_t s) {
   const fgb_sparse *L = P.L, *R = P.R;
-  const int gw = grid_for(P.m * 32, SG_WARPS * 32, ctx->num_sms, 16);
-  sg_warp_k<T, PtrT, SYMB><<<gw, SG_WARPS * 32, 0, s>>>(
-      P.m, S.ub, (const PtrT*)L->ptr, (const int*)L->idx, (const T*)L->val, L->index_base,
-      (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val, R->index_base, fm, S.cnt, cptr,
-      out_base, out_idx, out_val);
+  // small rows: 8 lanes each (bound <= 64); medium: a warp each (<= 256)
+  const int g8 = grid_for(P.m * 8, SG_WARPS * 32, ctx->num_sms, 16);
+  sg_warp_k<T, PtrT, SYMB, 8><<<g8, SG_WARPS * 32, 0, s>>>(
+      P.m, S.ub, -1, SG_SMALL_UB, (const PtrT*)L->ptr, (const int*)L->idx, (const T*)L->val,
+      L->index_base, (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val, R->index_base, fm,
+      S.cnt, cptr, out_base, out_idx, out_val);
+  const int g32 = grid_for(P.m * 32, SG_WARPS * 32, ctx->num_sms, 16);
+  sg_warp_k<T, PtrT, SYMB, 32><<<g32, SG_WARPS * 32, 0, s>>>(
+      P.m, S.ub, SG_SMALL_UB, SG_WARP_UB, (const PtrT*)L->ptr, (const int*)L->idx, (const T*)L->val,
+      L->index_base, (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val, R->index_base, fm,
+      S.cnt, cptr, out_base, out_idx, out_val);
   sg_block_k<T, PtrT, SYMB><<<ctx->num_sms * 4, SG_BLOCK, 0, s>>>(
       P.m, S.ub, S.goff, S.gkeys, (T*)S.gvals, (const PtrT*)L->ptr, (const int*)L->idx,
       (const T*)L->val, L->index_base, (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val,
