@@ -164,18 +164,33 @@ __global__ void __launch_bounds__(SG_WARPS * 32) sg_warp_k(
   __shared__ int32_t s_keys[NG][SLOTS];
   __shared__ T s_vals[SYMB ? 1 : NG][SYMB ? 1 : SLOTS];
   __shared__ int s_cnt[NG];
+  __shared__ int64_t s_rows[SG_WARPS * 32];  // this tile's rows of the tier
+  __shared__ int s_n;
   const int grp = threadIdx.x / G, gl = threadIdx.x % G;
   const unsigned gmask = group_mask<G>();
-  const int64_t ngr = (int64_t)gridDim.x * NG;
-  for (int64_t r = blockIdx.x * (int64_t)NG + grp; r < m; r += ngr) {
-    const int64_t u = ub[r];
-    if (u <= lo || u > hi) continue;  // group-uniform
-    int64_t cap = 16;  // a table sized to the row: at least twice its bound
-    while (cap < 2 * u) cap <<= 1;
-    sg_row<T, PtrT, SYMB>(r, gl, G, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[grp],
-                          SYMB ? nullptr : &s_vals[SYMB ? 0 : grp][0], cap, fm, &s_cnt[grp],
-                          out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, gmask);
-    if (SYMB && gl == 0) cnt_out[r] = s_cnt[grp];
+  // tiles of one row per thread: one coalesced look at the bounds, then the
+  // groups take the tile's rows of this tier
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const int64_t rr = base + threadIdx.x;
+    if (rr < m) {
+      const int64_t u = ub[rr];
+      if (u > lo && u <= hi) s_rows[atomicAdd(&s_n, 1)] = rr;
+    }
+    __syncthreads();
+    const int n = s_n;
+    for (int t = grp; t < n; t += NG) {
+      const int64_t r = s_rows[t];
+      const int64_t u = ub[r];
+      int64_t cap = 16;  // a table sized to the row: at least twice its bound
+      while (cap < 2 * u) cap <<= 1;
+      sg_row<T, PtrT, SYMB>(r, gl, G, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[grp],
+                            SYMB ? nullptr : &s_vals[SYMB ? 0 : grp][0], cap, fm, &s_cnt[grp],
+                            out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, gmask);
+      if (SYMB && gl == 0) cnt_out[r] = s_cnt[grp];
+    }
+    __syncthreads();  // s_rows is refilled for the next tile
   }
 }
 
@@ -188,13 +203,24 @@ __global__ void __launch_bounds__(SG_BLOCK) sg_block_k(
     int64_t* __restrict__ cnt_out, const int64_t* __restrict__ cptr, int out_base,
     int32_t* __restrict__ out_idx, T* __restrict__ out_val) {
   __shared__ int s_cnt;
-  for (int64_t r = blockIdx.x; r < m; r += gridDim.x) {
-    if (ub[r] <= SG_WARP_UB) continue;  // block-uniform
-    const int64_t off = goff[r], cap = goff[r + 1] - off;
-    sg_row<T, PtrT, SYMB>(r, threadIdx.x, SG_BLOCK, lp, li, lv, lbase, rp, ri, rv, rbase,
-                          gkeys + off, SYMB ? nullptr : gvals + off, cap, fm, &s_cnt, out_base,
-                          out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, 0u);
-    if (SYMB && threadIdx.x == 0) cnt_out[r] = s_cnt;
+  __shared__ int64_t s_rows[SG_BLOCK];
+  __shared__ int s_n;
+  for (int64_t base = blockIdx.x * (int64_t)SG_BLOCK; base < m; base += (int64_t)gridDim.x * SG_BLOCK) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const int64_t rr = base + threadIdx.x;
+    if (rr < m && ub[rr] > SG_WARP_UB) s_rows[atomicAdd(&s_n, 1)] = rr;
+    __syncthreads();
+    const int n = s_n;
+    for (int t = 0; t < n; ++t) {  // block-uniform
+      const int64_t r = s_rows[t];
+      const int64_t off = goff[r], cap = goff[r + 1] - off;
+      sg_row<T, PtrT, SYMB>(r, threadIdx.x, SG_BLOCK, lp, li, lv, lbase, rp, ri, rv, rbase,
+                            gkeys + off, SYMB ? nullptr : gvals + off, cap, fm, &s_cnt, out_base,
+                            out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, 0u);
+      if (SYMB && threadIdx.x == 0) cnt_out[r] = s_cnt;
+    }
+    __syncthreads();
   }
 }
 
@@ -285,12 +311,12 @@ static void sg_launch(fgb_ctx* ctx, const SgProblem& P, const SgScratch& S, int 
                       int out_base, int32_t* out_idx, T* out_val, cudaStream_t s) {
   const fgb_sparse *L = P.L, *R = P.R;
   // small rows: 8 lanes each (bound <= 64); medium: a warp each (<= 256)
-  const int g8 = grid_for(P.m * 8, SG_WARPS * 32, ctx->num_sms, 16);
+  const int g8 = grid_for(P.m, SG_WARPS * 32, ctx->num_sms, 16);
   sg_warp_k<T, PtrT, SYMB, 8><<<g8, SG_WARPS * 32, 0, s>>>(
       P.m, S.ub, -1, SG_SMALL_UB, (const PtrT*)L->ptr, (const int*)L->idx, (const T*)L->val,
       L->index_base, (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val, R->index_base, fm,
       S.cnt, cptr, out_base, out_idx, out_val);
-  const int g32 = grid_for(P.m * 32, SG_WARPS * 32, ctx->num_sms, 16);
+  const int g32 = grid_for(P.m, SG_WARPS * 32, ctx->num_sms, 16);
   sg_warp_k<T, PtrT, SYMB, 32><<<g32, SG_WARPS * 32, 0, s>>>(
       P.m, S.ub, SG_SMALL_UB, SG_WARP_UB, (const PtrT*)L->ptr, (const int*)L->idx, (const T*)L->val,
       L->index_base, (const PtrT*)R->ptr, (const int*)R->idx, (const T*)R->val, R->index_base, fm,
