@@ -150,7 +150,8 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           if (rc) return rc;
           it = p->vrows.emplace(c.path, v).first;
         }
-        return sddmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, s);
+        return sddmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, s,
+                          c.lanes > 0 ? 4 * c.lanes : 0);
       }
       return sddmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, d.dtype,
                         d.flags, c.lanes, c.path, s,
@@ -197,7 +198,10 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{d.dtype == FGB_F64 ? 16 : 8, chunk, 1, 2});
     if (d.dtype == FGB_F32 && p->A.orient == FGB_CSR && p->A.val_t == FGB_F32 && d.k <= 128 &&
         d.k % 4 == 0 && d.ld_in0 % 4 == 0 && d.ld_in1 % 4 == 0 && p->A.nnz <= INT32_MAX)
-      for (int64_t t : {64, 128, 256}) out.push_back(Choice{0, t, 1, 3});  // virtual rows
+      for (int64_t t : {64, 128, 256}) {  // virtual rows, all of k or 32-column slabs
+        out.push_back(Choice{0, t, 1, 3});
+        if (d.k > 32) out.push_back(Choice{8, t, 1, 3});
+      }
   }
   return out;
 }

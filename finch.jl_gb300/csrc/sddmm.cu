@@ -271,7 +271,7 @@ extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, in
     fgb::VrowSchedule v;
     rc = fgb::vrow_build(ctx, A, tune->chunk > 0 ? (int)std::min<int64_t>(tune->chunk, 4096) : 128, &v, s);
     if (rc) return rc;
-    rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s);
+    rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s, tune->slab > 0 ? tune->slab : 0);
     cudaError_t e = cudaStreamSynchronize(s);
     fgb::vrow_free(&v);
     if (rc == FGB_OK && e != cudaSuccess) rc = fgb::set_error(FGB_ECUDA, "fgb_sddmm_ex: %s", cudaGetErrorString(e));

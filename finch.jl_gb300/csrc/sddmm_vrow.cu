@@ -7,7 +7,10 @@
 // entry only gathers its row of Y.  NB entries are in flight per sub-group;
 // each dot product is reduced over the L lanes with xor-shuffles (a fixed
 // tree: deterministic).  Virtual rows are sorted by length class, so the
-// sub-groups of a warp run similar trip counts.
+// sub-groups of a warp run similar trip counts.  Optionally k is cut into
+// column slabs of one 128-byte line of Y, one launch each (fewer L2 lines per
+// launch); the dot then accumulates in `out` across launches and the last
+// launch multiplies by A's value.
 #include "spmm_common.cuh"
 
 namespace fgb {
@@ -18,7 +21,7 @@ template <int L, int NB>
 __global__ void __launch_bounds__(SV_THREADS, 4) sddmm_vrow_k(
     int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx, const float* __restrict__ val,
     const float* __restrict__ X, int64_t ldx, const float* __restrict__ Y, int64_t ldy, int64_t k,
-    float* __restrict__ out, int base) {
+    float* __restrict__ out, int base, int mode) {
   const int lane = threadIdx.x & 31, sl = lane % L;
   const unsigned gmask = group_mask<L>();
   const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
@@ -52,7 +55,9 @@ __global__ void __launch_bounds__(SV_THREADS, 4) sddmm_vrow_k(
         for (int u = 1; u < NB; ++u)
           if (sl == u) mine = d[u];
         const int64_t e = (int64_t)rec.y + t + sl;
-        __stcs(out + e, __fmul_rn(ld_stream_f32(val + e, pol_stream), mine));
+        // mode 0: all of k; 1: first slab; 2: middle slab; 3: last slab
+        const float dsum = mode >= 2 ? out[e] + mine : mine;
+        out[e] = (mode == 0 || mode == 3) ? __fmul_rn(ld_stream_f32(val + e, pol_stream), dsum) : dsum;
       }
     }
   }
@@ -61,7 +66,7 @@ __global__ void __launch_bounds__(SV_THREADS, 4) sddmm_vrow_k(
 template <int L>
 static int launch_sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* X,
                              int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
-                             cudaStream_t s) {
+                             int mode, cudaStream_t s) {
   constexpr int NB = L >= 4 ? 4 : L;
   static int occ = -1;  // per process: one device model
   if (occ < 0) {
@@ -72,13 +77,13 @@ static int launch_sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_spar
   const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   sddmm_vrow_k<L, NB><<<grid, SV_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val,
-                                                  X, ldx, Y, ldy, k, out, A->index_base);
+                                                  X, ldx, Y, ldy, k, out, A->index_base, mode);
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
 }
 
 int sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* X, int64_t ldx,
-               const void* Y, int64_t ldy, int64_t k, void* out, cudaStream_t s) {
+               const void* Y, int64_t ldy, int64_t k, void* out, cudaStream_t s, int64_t slab) {
   if (A->orient != FGB_CSR || A->val_t != FGB_F32 || A->idx_t != FGB_I32)
     return set_error(FGB_EUNSUPPORTED, "sddmm vrow: CSR with F32 values and int32 indices only");
   if (k <= 0 || k > 128 || k % 4 || ldx % 4 || ldy % 4 || (uintptr_t)X % 16 || (uintptr_t)Y % 16)
@@ -86,11 +91,19 @@ int sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const v
   const float* x = (const float*)X;
   const float* y = (const float*)Y;
   float* o = (float*)out;
-  const int64_t need = k / 4;
-  if (need <= 4) return launch_sddmm_vrow<4>(ctx, v, A, x, ldx, y, ldy, k, o, s);
-  if (need <= 8) return launch_sddmm_vrow<8>(ctx, v, A, x, ldx, y, ldy, k, o, s);
-  if (need <= 16) return launch_sddmm_vrow<16>(ctx, v, A, x, ldx, y, ldy, k, o, s);
-  return launch_sddmm_vrow<32>(ctx, v, A, x, ldx, y, ldy, k, o, s);
+  if (slab <= 0 || slab >= k || slab % 4) slab = k;
+  for (int64_t c0 = 0; c0 < k; c0 += slab) {
+    const int64_t kw = k - c0 < slab ? k - c0 : slab;
+    const int mode = slab >= k ? 0 : c0 == 0 ? 1 : c0 + slab >= k ? 3 : 2;
+    const int64_t need = (slab + 3) / 4;
+    int rc;
+    if (need <= 4) rc = launch_sddmm_vrow<4>(ctx, v, A, x + c0, ldx, y + c0, ldy, kw, o, mode, s);
+    else if (need <= 8) rc = launch_sddmm_vrow<8>(ctx, v, A, x + c0, ldx, y + c0, ldy, kw, o, mode, s);
+    else if (need <= 16) rc = launch_sddmm_vrow<16>(ctx, v, A, x + c0, ldx, y + c0, ldy, kw, o, mode, s);
+    else rc = launch_sddmm_vrow<32>(ctx, v, A, x + c0, ldx, y + c0, ldy, kw, o, mode, s);
+    if (rc) return rc;
+  }
+  return FGB_OK;
 }
 
 }  // namespace fgb

@@ -274,7 +274,8 @@ FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t 
  * launches; 0 = all of k, -1 = the default: one 128-byte line of Y per launch
  * when Y is far larger than L2).  variant 1 (F32 CSR, k <= 128 and a multiple
  * of 4): sub-groups own virtual rows of at most `chunk` entries, sorted by
- * length, holding the row's slice of X in registers.  Zero lanes/chunk take
+ * length, holding the row's slice of X in registers; `slab` > 0 (a multiple
+ * of 4) cuts k into launches of that many columns.  Zero lanes/chunk take
  * the defaults. */
 typedef struct fgb_sddmm_tuning {
   int32_t lanes;

@@ -224,6 +224,8 @@ def test_sddmm(gpu_lib, k, dtype):
         for T in (8, 64, 200):
             out4 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1))
             assert_close(out4, want, scale, dtype)
+            out5 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1, slab=32))
+            assert_close(out5, want, scale, dtype)
             assert np.array_equal(out4, to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1)))
     else:
         with pytest.raises(L.FinchGBError):
