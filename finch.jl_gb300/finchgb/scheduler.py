@@ -203,6 +203,10 @@ class GB300Scheduler:
                         flags |= L.FINCH_ORDER
                         if A.orient == "csc":
                             A = _csr_copy(a.tns, A)
+                    elif A.orient == "csc" and _reused(a.tns):
+                        # a CSC operand used again (an iterative program): pull over
+                        # a CSR copy built once -- no atomics, deterministic sums
+                        A = _csr_copy(a.tns, A)
                     y = None
                     if out is not None:
                         y = dense_operand(out, (i,), (i,))
@@ -414,6 +418,14 @@ class GB300Scheduler:
         b = vals[1] if vals[1] is not None else _scalar_tensor(m.core.args[1].value, like.dtype)
         self.last_kernel = "fgb_scalar_op"
         return Scalar(dev.scalar_op(ops[m.core.op], a, b, None if out is None else out.t))
+
+
+def _reused(t) -> bool:
+    """Counts SpMV uses of a tensor; true from its second use on."""
+    body = t.body if isinstance(t, SwizzleArray) else t
+    n = getattr(body, "_gb_uses", 0) + 1
+    body._gb_uses = n
+    return n >= 2
 
 
 def _csr_copy(t, A: dev.DeviceSparse) -> dev.DeviceSparse:

@@ -124,6 +124,7 @@ def test_lazy_spmm_sddmm_reduce(gpu_lib):
 
 
 def test_bellman_ford_in_einsum(gpu_lib):
+    from finchgb.scheduler import get_scheduler
     from finchgb.workloads import random_graph
 
     rng = np.random.default_rng(4)
@@ -132,12 +133,16 @@ def test_bellman_ford_in_einsum(gpu_lib):
     A = F.Tensor.from_buffers(F.Dense(F.SparseList(F.Element(np.int32(2**31 - 1), np.int32))), g)
     x = vec(np.where(np.arange(n) == 0, 0, 2**30).astype(np.int32))
     xh = x.todense().copy()
+    kernels = []
     for _ in range(10):
         y = F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x)
+        kernels.append(get_scheduler().last_kernel)
         x = F.einsum("x[i] = min(x[i], y[i])", x=x, y=y)
         yh = oracle.spmv_csc(oracle.SR_MINP, n, n, g.ptr, g.idx, g.val, xh)
         xh = np.minimum(xh, yh)
     assert np.array_equal(x.todense(), xh)
+    # the CSC operand is pushed once, then pulled through its CSR copy
+    assert kernels[0].endswith(",csc]") and all(k.endswith(",csr]") for k in kernels[1:])
 
 
 def test_cg_in_einsum_small(gpu_lib):
