@@ -247,7 +247,7 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   CgBuffers bufs;
   double* hist_h = nullptr;
   int64_t hist_cap = 0;
-  const int grid = grid_for(n, CG_THREADS, ctx->num_sms, 4);
+  const int grid = grid_for(n, CG_THREADS, ctx->num_sms, 8);  // full occupancy: streaming kernels
   const bool i32 = A64->ptr_t == FGB_I32;  // ptr width of the FP64 matrix
   auto t0 = std::chrono::steady_clock::now();
   auto fail = [&](int code, const char* what, cudaError_t e) {
