@@ -421,6 +421,19 @@ def run_gpu(args):
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
                         "algorithmic_bytes_per_launch": nbytes,
                         "avg_launch_ms": round(avg_ms, 4)}
+    # The slab kernel gathers a 4*lanes-column piece of one B row per stored
+    # entry and slab: nnz * NK * 4 bytes per step, from a working set of one
+    # slab of B.  Its ceiling is the random-gather rate at that width and
+    # working set, measured here on the same device.
+    if variant == 2:
+        gbytes = 16 * plan_lanes
+        ceiling = dev.gather_ceiling(A_h.ncols * gbytes, gbytes)
+        gathered = A_h.nnz * NK * 4
+        g_achieved = gathered / (avg_ms / 1e3) / 1e9
+        line["gather_ceiling"] = {"gathered_bytes_per_step": gathered, "gather_bytes": gbytes,
+                                  "working_set_bytes": A_h.ncols * gbytes,
+                                  "achieved": round(g_achieved, 1), "ceiling": round(ceiling, 1),
+                                  "unit": "GB/s", "frac": round(g_achieved / ceiling, 4)}
     line["cpu_baseline"] = None
     if rank == 0 and not args.skip_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A_h, B_h, nbytes)
@@ -603,11 +616,6 @@ def suite_semiring() -> list[dict]:
     ms20 = _timed_ms(lambda: rounds(20), reps=3, warm=1)
     x_push = rounds(20)
     per_round_bytes = 8 * g.nnz + 4 * (n + 1) + 3 * 4 * n + 2 * 4 * n
-    f0 = torch.zeros(n, dtype=torch.uint8, device="cuda")
-    f0[0] = 1
-    yb = torch.empty_like(f0)
-    ms_or = _timed_ms(lambda: dev.spmv(Ap, f0, yb, semiring=L.OR_AND), reps=20)
-    or_bytes = 4 * g.nnz + 4 * (n + 1) + 2 * n
     # pull over a CSR copy built once on the device (rows = targets: no atomics)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -631,8 +639,41 @@ def suite_semiring() -> list[dict]:
 
     ms20_pull = _timed_ms(lambda: rounds_pull(20), reps=3, warm=1)
     same = bool(torch.equal(rounds_pull(20), x_push))
-    plan_or = Plan.spmv(Arp, f0, yb, semiring=L.OR_AND)
-    ms_or_pull = _timed_ms(plan_or.execute, reps=20)
+    # or-and reachability, y = A x over (|, &), for a one-vertex frontier and a
+    # frontier of a quarter of the vertices.  The push skips columns whose
+    # x[j] is false and the pull stops a row at its first true product, so
+    # each line's bytes are the ones that frontier requires: push = y fill,
+    # x scan, ptr and entries of the true columns (+ their y writes); pull =
+    # the whole matrix, x and y (a row's entries share one 32-byte sector).
+    deg = np.diff(g.ptr)
+    or_bytes = 4 * g.nnz + 4 * (n + 1) + 2 * n
+    frontiers = {"one_vertex": np.zeros(n, dtype=np.uint8),
+                 "quarter": (rng.random(n) < 0.25).astype(np.uint8)}
+    frontiers["one_vertex"][0] = 1
+    or_lines = []
+    for fname, fh in frontiers.items():
+        fx = torch.from_numpy(fh).cuda()
+        y_push, y_pull = torch.empty_like(fx), torch.empty_like(fx)
+        ms_push = _timed_ms(lambda: dev.spmv(Ap, fx, y_push, semiring=L.OR_AND), reps=20)
+        plan_or = Plan.spmv(Arp, fx, y_pull, semiring=L.OR_AND)
+        ms_pull = _timed_ms(plan_or.execute, reps=20)
+        active = fh.astype(bool)
+        e_active = int(deg[active].sum())
+        push_bytes = 2 * n + 8 * int(active.sum()) + 5 * e_active
+        same_or = bool(torch.equal(y_push, y_pull))
+        common = {"suite": "reachability_or_and_4M", "metric": "or_and_spmv_gbps", "unit": "GB/s",
+                  "dtype": "bool", "frontier": fname, "frontier_vertices": int(active.sum()),
+                  "equal_push_pull": same_or}
+        or_lines.append({**common, "variant": "csc_push",
+                         "value": round(push_bytes / (ms_push / 1e3) / 1e9, 1),
+                         "ms_per_call": round(ms_push, 4), "entries_touched": e_active,
+                         "config": {"workload": "same graph, Pattern level, CSC (columns = sources)"},
+                         "roofline": _roof(push_bytes, ms_push)})
+        or_lines.append({**common, "variant": "csr_pull",
+                         "value": round(or_bytes / (ms_pull / 1e3) / 1e9, 1),
+                         "ms_per_call": round(ms_pull, 4), "lanes_per_row": plan_or.info()["lanes"],
+                         "config": {"workload": "same graph, Pattern level, CSR copy"},
+                         "roofline": _roof(or_bytes, ms_pull)})
     threads = oracle.max_threads()
     xh = np.full(n, sentinel, dtype=np.int32)
     xh[0] = 0
@@ -653,16 +694,7 @@ def suite_semiring() -> list[dict]:
              "one_time_csr_copy_ms": round(ms_transpose, 3), "equal_to_push": same,
              "lanes_per_row": plan_mp.info()["lanes"],
              "config": {"workload": "same graph; CSR copy built once on the device"},
-             "roofline": _roof(20 * per_round_bytes, ms20_pull)},
-            {"suite": "reachability_or_and_4M", "metric": "or_and_spmv_gbps",
-             "value": round(or_bytes / (ms_or / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "bool",
-             "ms_per_call": round(ms_or, 4), "config": {"workload": "same graph, Pattern level"},
-             "roofline": _roof(or_bytes, ms_or)},
-            {"suite": "reachability_or_and_4M", "variant": "csr_pull", "metric": "or_and_spmv_gbps",
-             "value": round(or_bytes / (ms_or_pull / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "bool",
-             "ms_per_call": round(ms_or_pull, 4), "lanes_per_row": plan_or.info()["lanes"],
-             "config": {"workload": "same graph, Pattern level, CSR copy"},
-             "roofline": _roof(or_bytes, ms_or_pull)}]
+             "roofline": _roof(20 * per_round_bytes, ms20_pull)}] + or_lines
 
 
 def suite_cg() -> list[dict]:

@@ -13,6 +13,12 @@
 // applies y[i] <<(+)>>= A[i,j] (*) x[j] for every stored i with an atomic
 // update.  For exact semirings (integer +, min, max, |) the atomics commute,
 // so results are exact; float sums are exact up to summation order.
+//
+// OR-AND works on Bool (0 or 1) bytes, where `true` absorbs under | and
+// `false` annihilates under &: the push skips the columns whose x[j] is
+// false and the pull stops a lane's scan at its first true product.  The
+// result is the full nest's, bit for bit; a sparse frontier touches only its
+// own columns' entries.
 #include "fgb_internal.cuh"
 #include "semiring.cuh"
 
@@ -37,6 +43,7 @@ __global__ void __launch_bounds__(256) spmv_csr_pull(int64_t nrows, const PtrT* 
       const int j = __ldg(idx + p) - base;
       const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
       acc = S::step(acc, a, __ldg(x + j), fm);
+      if (SR == SR_OA && acc) break;  // Bool: true absorbs every later product
     }
     if (G > 1) {
 #pragma unroll
@@ -59,14 +66,77 @@ __global__ void __launch_bounds__(256) spmv_csc_push(int64_t ncols, const PtrT* 
   const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
   const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
   for (int64_t col = group; col < ncols; col += ngroups) {
+    const A xj = __ldg(x + col);
+    if (SR == SR_OA && !xj) continue;  // Bool: a & false adds nothing to any y[i]
     const int64_t p0 = ld_ptr(ptr, col) - base;
     const int64_t p1 = ld_ptr(ptr, col + 1) - base;
     if (p0 >= p1) continue;
-    const A xj = __ldg(x + col);
     for (int64_t p = p0 + lane; p < p1; p += G) {
       const int i = __ldg(idx + p) - base;
       const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
       AtomicAdd<SR, A>::apply(y + i, S::mul(a, xj));
+    }
+  }
+}
+
+// OR-AND push, warp-cooperative.  Each lane reads x for one column of a
+// 32-column tile (four tiles in flight per lane); the warp takes an exclusive
+// scan of the true columns' entry counts and spreads those entries over its
+// 32 lanes, each finding its column by a binary search of the scan held in
+// registers.  A false column costs one byte of x; the warp's lanes stay busy
+// whatever the frontier's density.
+template <class VT, class PtrT, bool PATTERN>
+__global__ void __launch_bounds__(256) spmv_csc_push_oa(int64_t ncols, const PtrT* __restrict__ ptr,
+                                                        const int* __restrict__ idx,
+                                                        const VT* __restrict__ val,
+                                                        const uint8_t* __restrict__ x,
+                                                        uint8_t* __restrict__ y, int base) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int U = 4;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c0 = warp * 32 * U; c0 < ncols; c0 += nwarps * 32 * U) {
+    uint8_t xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t col = c0 + 32 * u + lane;
+      xv[u] = col < ncols ? __ldg(x + col) : uint8_t(0);
+    }
+#pragma unroll 1
+    for (int u = 0; u < U; ++u) {
+      const int64_t col = c0 + 32 * u + lane;
+      if (!__any_sync(FULL, xv[u] != 0)) continue;
+      int64_t p0 = 0, deg = 0;
+      if (xv[u]) {
+        p0 = ld_ptr(ptr, col) - base;
+        deg = ld_ptr(ptr, col + 1) - base - p0;
+      }
+      int64_t incl = deg;  // inclusive scan of the entry counts over the warp
+#pragma unroll
+      for (int m = 1; m < 32; m <<= 1) {
+        const int64_t t = __shfl_up_sync(FULL, incl, m);
+        if (lane >= m) incl += t;
+      }
+      const int64_t excl = incl - deg;
+      const int64_t total = __shfl_sync(FULL, incl, 31);
+      for (int64_t k = 0; k < total; k += 32) {
+        const int64_t e = k + lane;
+        // owner: the largest lane whose scan start is <= e (it has entries)
+        int l = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int64_t s = __shfl_sync(FULL, excl, l + step);
+          if (s <= e) l += step;
+        }
+        const int64_t pp = __shfl_sync(FULL, p0, l) + (e - __shfl_sync(FULL, excl, l));
+        const uint8_t xj = __shfl_sync(FULL, xv[u], l);
+        if (e < total) {
+          const int i = __ldg(idx + pp) - base;
+          const uint8_t a = PATTERN ? uint8_t(1) : val[pp];
+          if (a & xj) *(volatile uint8_t*)(y + i) = 1;
+        }
+      }
     }
   }
 }
@@ -127,6 +197,14 @@ static int launch_typed(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void*
     if (rc) return rc;
   }
   if (nf == 0) return FGB_OK;
+  if constexpr (SR == SR_OA) {
+    if (t_group_override <= 0) {  // the plan may still time the lane-group kernels
+      const int grid = grid_for((nf + 127) / 128 * 32, threads, ctx->num_sms, 8);
+      spmv_csc_push_oa<VT, PtrT, PATTERN><<<grid, threads, 0, s>>>(nf, ptr, idx, val, (const uint8_t*)x,
+                                                                  (uint8_t*)y, base);
+      return check_launch("spmv_csc_push_oa");
+    }
+  }
   int G = t_group_override > 0 ? (t_group_override <= 1 ? 1 : t_group_override <= 8 ? 8 : 32)
                                : (avg <= 4.0 ? 1 : (avg <= 16.0 ? 8 : 32));
   int grid = grid_for(nf * G, threads, ctx->num_sms, 8);

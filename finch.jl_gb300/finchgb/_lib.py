@@ -96,9 +96,10 @@ class FgbSparse(ctypes.Structure):
                 ("val", c_void_p)]
 
 
-# name -> (restype, argtypes); every symbol include/finchgb.h declares.
+# name -> (restype, argtypes); every symbol include/*.h declares.
 SIGNATURES: dict[str, tuple] = {
     "fgb_version": (c_int, []),
+    "fgb_gather_ceiling": (c_int, [c_void_p, c_int64, c_int32, c_int64, POINTER(c_double), c_void_p]),
     "fgb_last_error": (c_char_p, []),
     "fgb_ctx_create": (c_int, [c_int, POINTER(c_void_p)]),
     "fgb_ctx_destroy": (c_int, [c_void_p]),

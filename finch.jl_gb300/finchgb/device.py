@@ -56,6 +56,16 @@ def _dptr(t: torch.Tensor | None) -> int | None:
     return None if t is None or t.numel() == 0 else t.data_ptr()
 
 
+def gather_ceiling(working_set_bytes: int, gather_bytes: int, gathers: int = 1 << 24) -> float:
+    """GB/s at which random gathers of `gather_bytes` contiguous bytes are served
+    from a device working set of `working_set_bytes` (fgb_gather_ceiling): the
+    limit that binds the kernels gathering dense rows."""
+    out = ctypes.c_double()
+    L.call("fgb_gather_ceiling", context(), int(working_set_bytes), int(gather_bytes), int(gathers),
+           ctypes.byref(out), stream_ptr())
+    return out.value
+
+
 @dataclass
 class DeviceSparse:
     """A 2-D SparseList matrix in HBM.

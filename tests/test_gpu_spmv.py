@@ -120,6 +120,45 @@ def test_or_and(gpu_lib, orient, pattern):
     assert np.array_equal(y, want)
 
 
+@pytest.mark.parametrize("orient", ["csc", "csr"])
+@pytest.mark.parametrize("frontier", ["none", "one", "sparse", "half", "all"])
+@pytest.mark.parametrize("pattern", [True, False])
+def test_or_and_short_circuits(gpu_lib, orient, frontier, pattern):
+    """The push skips false columns and the pull stops at a row's first true
+    product: the result is still the full nest's for every frontier density,
+    lane count (heuristic, Finch's serial order, every plan candidate),
+    accumulation into a preset y, and Bool values holding explicit falses."""
+    from finchgb.plan import Plan
+
+    rng = np.random.default_rng(29)
+    n = 5000
+    b = random_graph(rng, n, 9.0, pattern=True)
+    if not pattern:
+        b.val = rng.random(b.nnz) < 0.8
+    if orient == "csr":
+        b = csr_of(b)
+    x = {"none": np.zeros(n, bool), "one": np.arange(n) == 17, "sparse": rng.random(n) < 0.01,
+         "half": rng.random(n) < 0.5, "all": np.ones(n, bool)}[frontier].astype(np.uint8)
+    want = oracle_spmv(oracle.SR_OA, b, x)
+    A, xd = upload(b), to_dev(x)
+    assert np.array_equal(to_host(dev.spmv(A, xd, semiring=L.OR_AND)), want)
+    y0 = (rng.random(n) < 0.3).astype(np.uint8)
+    y = to_dev(y0)
+    dev.spmv(A, xd, y, semiring=L.OR_AND, flags=L.ACCUMULATE)
+    assert np.array_equal(to_host(y), want | y0)
+    if orient == "csr":
+        y1 = torch.empty(n, dtype=torch.uint8, device="cuda")
+        dev.spmv(A, xd, y1, semiring=L.OR_AND, flags=L.FINCH_ORDER)
+        assert np.array_equal(to_host(y1), want)
+        y2 = to_dev(y0)
+        dev.spmv(A, xd, y2, semiring=L.OR_AND, flags=L.FINCH_ORDER | L.ACCUMULATE)
+        assert np.array_equal(to_host(y2), want | y0)
+    yp = torch.empty(n, dtype=torch.uint8, device="cuda")
+    plan = Plan.spmv(A, xd, yp, semiring=L.OR_AND, tune_reps=1)
+    plan.execute()
+    assert np.array_equal(to_host(yp), want)
+
+
 def test_minplus_bellman_ford_rounds(gpu_lib):
     """20 relaxation rounds y .= inf; y[i] <<min>>= A[i,j] + x[j]; x = min(x, y)."""
     rng = np.random.default_rng(3)
