@@ -257,11 +257,11 @@ def run_gpu(args):
     variant = info["variant"] if plan is not None else fixed_variant
     plan_lanes = info["lanes"] if plan is not None else lanes
     slabs = -(-NK // (4 * plan_lanes))
-    if plan is None and variant == 2:  # schedule built per call: counted as its kernels
+    if plan is None and variant in (2, 3):  # schedule built per call: counted as its kernels
         launches_per_step = 10 + slabs
     elif plan is None:
         launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
-    elif variant == 2:  # one launch per column slab + the partial-sum fix-up
+    elif variant in (2, 3):  # one launch per column slab + the partial-sum fix-up
         launches_per_step = slabs + 1
     else:  # per panel: the slab launches + fix-up (item boundaries precomputed)
         launches_per_step = npanels * (slabs + 1)
@@ -416,6 +416,7 @@ def run_gpu(args):
                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": traffic, "traffic_source": traffic_src,
                         "kernel": (f"spmm_vrow_k x{slabs} column slabs + vrow_fixup_k" if variant == 2 else
+                                   f"spmm_vrow_async_k x{slabs} column slabs + vrow_fixup_k" if variant == 3 else
                                    f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
                                    if plan is not None and npanels > 1 else
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
@@ -425,7 +426,7 @@ def run_gpu(args):
     # entry and slab: nnz * NK * 4 bytes per step, from a working set of one
     # slab of B.  Its ceiling is the random-gather rate at that width and
     # working set, measured here on the same device.
-    if variant == 2:
+    if variant in (2, 3):
         gbytes = 16 * plan_lanes
         ceiling = dev.gather_ceiling(A_h.ncols * gbytes, gbytes)
         gathered = A_h.nnz * NK * 4

@@ -114,7 +114,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
         return fgb_panels_spmm(p->ctx, it->second, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                                d.flags, &t, s);
       }
-      if (c.variant == 2) {
+      if (c.variant == 2 || c.variant == 3) {
         auto it = p->vrows.find(c.path);
         if (it == p->vrows.end()) {  // built outside capture (the timing pass comes first)
           VrowSchedule v;
@@ -133,7 +133,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           p->partial_bytes = need;
         }
         return spmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out,
-                         (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s);
+                         (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s, c.variant == 3);
       }
       if (c.path > 0)
         return spmm_merge(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
@@ -184,7 +184,8 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t path : {256, 512, 1024, 2048}) out.push_back(Choice{32, path, 1, 1});
     if (d.dtype == FGB_F32 && p->A.val_t == FGB_F32 && p->A.nrows <= INT32_MAX)
       for (int l : {2, 4, 8})  // column slabs over length-sorted virtual rows
-        for (int64_t t : {32, 64, 128}) out.push_back(Choice{l, t, 1, 2});
+        for (int64_t t : {32, 64, 128})
+          for (int v : {2, 3}) out.push_back(Choice{l, t, 1, v});  // register / cp.async gathers
     // column panels keep each panel's slice of B in L2 (worth it when B is not)
     const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);
     if (b_bytes > 32.0 * 1024 * 1024 && !(d.flags & FGB_ACCUMULATE))
@@ -234,7 +235,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   if (p->d.op == FGB_PLAN_SPMM) {
     const size_t esz = p->d.dtype == FGB_F64 ? 8 : 4;
     for (const Choice& c : cands)
-      if (c.path > 0 && c.variant != 2)
+      if (c.path > 0 && c.variant < 2)  // the merge-path schedules
         p->scratch_bytes = std::max(p->scratch_bytes,
                                     spmm_merge_scratch_bytes(p->A.nrows, p->A.nnz, p->d.k, esz, c.path));
     if (p->scratch_bytes) {

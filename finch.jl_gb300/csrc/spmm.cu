@@ -228,9 +228,9 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
   if ((A->ncols > 0 && nk > 0 && !B) || (A->nrows > 0 && nk > 0 && !C))
     return set_error(FGB_EINVAL, "fgb_spmm: null B or C");
   cudaStream_t s = pick_stream(ctx, stream);
-  if (variant == 2) {  // virtual-row column slabs: schedule built for this call
+  if (variant == 2 || variant == 3) {  // virtual-row column slabs: schedule built for this call
     if (A->orient != FGB_CSR || dtype != FGB_F32 || (flags & FGB_FINCH_ORDER))
-      return set_error(FGB_EUNSUPPORTED, "fgb_spmm: variant 2 needs CSR, F32 and no FGB_FINCH_ORDER");
+      return set_error(FGB_EUNSUPPORTED, "fgb_spmm: variants 2 and 3 need CSR, F32 and no FGB_FINCH_ORDER");
     if (A->nrows == 0 || nk == 0) return FGB_OK;
     VrowSchedule v;
     rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s);
@@ -242,7 +242,8 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
       vrow_free(&v);
       return set_error(FGB_ENOMEM, "fgb_spmm: partial sums (%zu bytes)", pb);
     }
-    rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0, slab, part, s);
+    rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0, slab, part, s,
+                   variant == 3);
     cudaError_t e = cudaStreamSynchronize(s);  // before the schedule is freed
     cudaFree(part);
     vrow_free(&v);
@@ -272,7 +273,7 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
   int lanes = tune ? tune->lanes : 0;
   int64_t path = tune ? tune->path : 0;
   const int variant = tune ? tune->variant : 0;
-  if (variant < 0 || variant > 2) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1 or 2");
+  if (variant < 0 || variant > 3) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1, 2 or 3");
   if (variant == 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant 2 takes lanes 2, 4 or 8");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)

@@ -149,6 +149,90 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
   }
 }
 
+// The same launch with the gathers staged in shared memory by cp.async
+// instead of held in registers: a lane's NB float4 gathers land in its own
+// slots, so no registers wait on memory, more warps fit per SM and more
+// gathers are in flight per SM for the same NB.  Accumulation order is the
+// register kernel's, so results are identical.
+__device__ __forceinline__ void cp_async16_keep(void* smem, const void* gmem, uint64_t pol) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int L, int NB, int MINB>
+__global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
+    int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx,
+    const float* __restrict__ val, const float* __restrict__ B, int64_t ldb, float* __restrict__ C,
+    int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, float* __restrict__ partial) {
+  constexpr int PER = NB / L;
+  static_assert(PER * L == NB, "batch must be a multiple of the sub-group");
+  extern __shared__ float4 vr_stage[];  // [NB][VR_THREADS]: slot u of thread t at u * VR_THREADS + t
+  const int lane = threadIdx.x & 31, sl = lane % L;
+  const unsigned gmask = group_mask<L>();
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / L;
+  const int64_t col = c0 + (int64_t)sl * 4;
+  const bool active = col < nk;
+  const float* Bc = B + col;
+  float4* slot = vr_stage + threadIdx.x;
+  const uint64_t pol_stream = policy_evict_first();
+  const uint64_t pol_keep = policy_evict_last();
+  for (int64_t v = gid; v < nv; v += ngroups) {
+    const int4 rec = __ldg(vr + v);
+    const int len = rec.z;
+    const int* ix = idx + rec.y;
+    const float* vx = val + rec.y;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int t = 0; t < len; t += NB) {
+      int j[PER];
+      float a[PER];
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int p = t + sl + L * q;
+        j[q] = 0;
+        a[q] = 0.f;
+        if (p < len) {
+          j[q] = ld_stream_i32(ix + p, pol_stream) - base;
+          a[q] = ld_stream_f32(vx + p, pol_stream);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        const int jj = __shfl_sync(gmask, j[u / L], u % L, L);
+        if (t + u < len && active) cp_async16_keep(slot + u * VR_THREADS, Bc + (int64_t)jj * ldb, pol_keep);
+      }
+      cp_async_wait_all();
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        const float aa = __shfl_sync(gmask, a[u / L], u % L, L);
+        if (t + u < len && active) {
+          const float4 b = slot[u * VR_THREADS];
+          acc.x = __fmaf_rn(aa, b.x, acc.x);
+          acc.y = __fmaf_rn(aa, b.y, acc.y);
+          acc.z = __fmaf_rn(aa, b.z, acc.z);
+          acc.w = __fmaf_rn(aa, b.w, acc.w);
+        }
+      }
+    }
+    if (!active) continue;
+    if (rec.w < 0) {
+      float* dst = C + (int64_t)rec.x * ldc + col;
+      if (accumulate) {
+        const float4 o = *reinterpret_cast<const float4*>(dst);
+        acc.x += o.x;
+        acc.y += o.y;
+        acc.z += o.z;
+        acc.w += o.w;
+      }
+      st_stream_f32x4(dst, acc, pol_stream);
+    } else {
+      *reinterpret_cast<float4*>(partial + (int64_t)rec.w * nk + col) = acc;
+    }
+  }
+}
+
 // Adds each long row's partial sums to that row of C: one warp per row (the
 // warp of its first slot), slots summed in order, 4 columns per lane.
 __global__ void vrow_fixup_k(int64_t nl, int64_t nk, const int64_t* __restrict__ part_row,
@@ -315,22 +399,27 @@ void vrow_free(VrowSchedule* v) {
   if (v) *v = VrowSchedule{};
 }
 
-template <int L, int NB, int MINB>
+template <int L, int NB, int MINB, bool ASYNC>
 static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* B,
                        int64_t ldb, int64_t nk, float* C, int64_t ldc, int accumulate, float* partial,
                        cudaStream_t s) {
+  auto kern = [] {
+    if constexpr (ASYNC) return spmm_vrow_async_k<L, NB, MINB>;
+    else return spmm_vrow_k<L, NB, MINB>;
+  }();
+  const size_t smem = ASYNC ? sizeof(float4) * NB * VR_THREADS : 0;
   static int occ = -1;  // per process: one device model
   if (occ < 0) {
+    if (ASYNC) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int o = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmm_vrow_k<L, NB, MINB>, VR_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, VR_THREADS, smem);
     occ = o > 0 ? o : 1;
   }
   const int64_t need = (v.nv * L + VR_THREADS - 1) / VR_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
-    spmm_vrow_k<L, NB, MINB><<<grid, VR_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx,
-                                                        (const float*)A->val, B, ldb, C, ldc, c0, nk,
-                                                        A->index_base, accumulate, partial);
+    kern<<<grid, VR_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val, B, ldb, C, ldc,
+                                        c0, nk, A->index_base, accumulate, partial);
   if (v.nl > 0)
     vrow_fixup_k<<<grid_for(v.nl * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nl, nk, v.part_row, partial,
                                                                          C, ldc);
@@ -344,7 +433,7 @@ size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk) {
 
 int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
               int64_t nk, void* C, int64_t ldc, int accumulate, int slab, void* partial,
-              cudaStream_t s) {
+              cudaStream_t s, bool async_gather) {
   if (A->val_t != FGB_F32 || A->idx_t != FGB_I32)
     return set_error(FGB_EUNSUPPORTED, "spmm vrow: F32 values and int32 indices only");
   if (nk % 4 || ldb % 4 || ldc % 4 || (uintptr_t)B % 16 || (uintptr_t)C % 16)
@@ -353,9 +442,15 @@ int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const vo
   const float* b = (const float*)B;
   float* c = (float*)C;
   float* part = (float*)partial;
-  if (slab == 8) return launch_vrow<2, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  if (slab == 16) return launch_vrow<4, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  if (slab == 32) return launch_vrow<8, 8, 4>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  if (async_gather) {  // 32 KB of gather slots per block: 6 blocks (48 warps) per SM
+    if (slab == 8) return launch_vrow<2, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+    if (slab == 16) return launch_vrow<4, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+    if (slab == 32) return launch_vrow<8, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  } else {
+    if (slab == 8) return launch_vrow<2, 8, 4, false>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+    if (slab == 16) return launch_vrow<4, 8, 4, false>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+    if (slab == 32) return launch_vrow<8, 8, 4, false>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
+  }
   return set_error(FGB_EINVAL, "spmm vrow: slab %d not in {8, 16, 32}", slab);
 }
 

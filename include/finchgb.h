@@ -226,12 +226,14 @@ FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
  * lanes * vector-width, one launch per slab, so the gathered slab of B stays
  * L2-resident.  Zero fields take the defaults. */
 typedef struct fgb_spmm_tuning {
-  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variant 2: 2, 4 or 8) */
+  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variants 2 and 3: 2, 4 or 8) */
   int32_t variant; /* 0: B rows gathered into registers; 1: B rows staged into a
                       shared-memory ring by TMA tile::gather4 (fp32); 2: rows
                       cut into virtual rows of at most `path` entries, sorted
-                      by length, one launch per column slab of 4 * lanes (fp32) */
-  int64_t path;    /* merge-path item length (variant 2: virtual-row length) */
+                      by length, one launch per column slab of 4 * lanes (fp32);
+                      3: variant 2 with the gathers staged in shared memory by
+                      cp.async (more warps per SM; identical results) */
+  int64_t path;    /* merge-path item length (variants 2, 3: virtual-row length) */
 } fgb_spmm_tuning;
 
 /* fgb_spmm with an explicit schedule (NULL = defaults).  The result does not
@@ -418,7 +420,7 @@ typedef struct fgb_plan_info {
   int32_t candidates;        /* schedules in the search space */
   int32_t from_cache;        /* 1 if the choice came from the tuning cache */
   int32_t panels;            /* SpMM: column panels of the chosen schedule (1 = none) */
-  int32_t variant;           /* SpMM: 0 register gathers, 1 TMA stage ring */
+  int32_t variant;           /* SpMM: fgb_spmm_tuning.variant; SDDMM: 3 virtual rows */
 } fgb_plan_info;
 
 /* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use

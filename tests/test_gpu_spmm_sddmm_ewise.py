@@ -140,16 +140,20 @@ def test_spmm_virtual_rows(gpu_lib, nk):
     want = oracle.spmm_csr(r.nrows, r.ncols, r.ptr, r.idx, r.val, B, nthreads=oracle.max_threads())
     scale = spmm_scale(r, B)
     Bd = to_dev(B)
-    for lanes in (4, 8):
+    for lanes in (2, 4, 8):
         for T in (8, 64, 200):
             C1 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=2))
             assert_close(C1, want, scale, np.float32)
             C2 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=2))
             assert np.array_equal(C1, C2)
+            # gathers staged in shared memory by cp.async: the same sums, bit for bit
+            C4 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=3))
+            assert np.array_equal(C4, C1)
     A64 = dev.DeviceSparse(A.nrows, A.ncols, torch.from_numpy(r.ptr.astype(np.int64)).cuda(), A.idx,
                            A.val, "csr", 1)
     C3 = to_host(dev.spmm(A64, Bd, lanes=4, path=64, variant=2))
     assert np.array_equal(C3, to_host(dev.spmm(A, Bd, lanes=4, path=64, variant=2)))
+    assert np.array_equal(C3, to_host(dev.spmm(A64, Bd, lanes=4, path=64, variant=3)))
 
 
 def test_spmm_virtual_rows_accumulate_strides_empty(gpu_lib):
@@ -171,6 +175,9 @@ def test_spmm_virtual_rows_accumulate_strides_empty(gpu_lib):
     got = to_host(Cd)
     assert_close(got[:, :48], want, spmm_scale(r, B48) + np.abs(C0[:, :48]), np.float32)
     assert np.array_equal(got[:, 48:], C0[:, 48:])  # untouched beyond nk
+    Cd3 = to_dev(C0)
+    dev.spmm(A, to_dev(Bfull)[:, :48], Cd3[:, :48], flags=L.ACCUMULATE, lanes=8, path=16, variant=3)
+    assert np.array_equal(to_host(Cd3), got)
     empty = upload(csr_from_dense(np.zeros((40, 30), dtype=np.float32)))
     Ce = dev.spmm(empty, to_dev(rng.standard_normal((30, 16)).astype(np.float32)), variant=2)
     assert not to_host(Ce).any()
