@@ -161,25 +161,29 @@ __device__ __forceinline__ void cp_async16_keep(void* smem, const void* gmem, ui
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <int L, int NB, int MINB>
+// ALL: every lane's 4 columns lie inside nk (nk a multiple of 4L), so no
+// lane is masked.  A full batch (NB entries left) runs without per-entry
+// predicates; ldb fits 32 bits, so a gather address is one 32x32->64
+// multiply-add.
+template <int L, int NB, int MINB, bool ALL>
 __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
     int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx,
-    const float* __restrict__ val, const float* __restrict__ B, int64_t ldb, float* __restrict__ C,
+    const float* __restrict__ val, const float* __restrict__ B, int ldb, float* __restrict__ C,
     int64_t ldc, int64_t c0, int64_t nk, int base, int accumulate, float* __restrict__ partial) {
   constexpr int PER = NB / L;
   static_assert(PER * L == NB, "batch must be a multiple of the sub-group");
   extern __shared__ float4 vr_stage[];  // [NB][VR_THREADS]: slot u of thread t at u * VR_THREADS + t
   const int lane = threadIdx.x & 31, sl = lane % L;
   const unsigned gmask = group_mask<L>();
-  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
-  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / L;
+  const int gid = (int)((blockIdx.x * blockDim.x + threadIdx.x) / L);  // nv < 2^31 (vrow_build)
+  const int ngroups = (int)((gridDim.x * blockDim.x) / L);
   const int64_t col = c0 + (int64_t)sl * 4;
-  const bool active = col < nk;
+  const bool active = ALL || col < nk;
   const float* Bc = B + col;
   float4* slot = vr_stage + threadIdx.x;
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
-  for (int64_t v = gid; v < nv; v += ngroups) {
+  for (int v = gid; v < nv; v += ngroups) {
     const int4 rec = __ldg(vr + v);
     const int len = rec.z;
     const int* ix = idx + rec.y;
@@ -197,6 +201,24 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
           j[q] = ld_stream_i32(ix + p, pol_stream) - base;
           a[q] = ld_stream_f32(vx + p, pol_stream);
         }
+      }
+      if (t + NB <= len && active) {  // full batch
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          const int jj = __shfl_sync(gmask, j[u / L], u % L, L);
+          cp_async16_keep(slot + u * VR_THREADS, Bc + (int64_t)jj * ldb, pol_keep);
+        }
+        cp_async_wait_all();
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          const float aa = __shfl_sync(gmask, a[u / L], u % L, L);
+          const float4 b = slot[u * VR_THREADS];
+          acc.x = __fmaf_rn(aa, b.x, acc.x);
+          acc.y = __fmaf_rn(aa, b.y, acc.y);
+          acc.z = __fmaf_rn(aa, b.z, acc.z);
+          acc.w = __fmaf_rn(aa, b.w, acc.w);
+        }
+        continue;
       }
 #pragma unroll
       for (int u = 0; u < NB; ++u) {
@@ -399,14 +421,19 @@ void vrow_free(VrowSchedule* v) {
   if (v) *v = VrowSchedule{};
 }
 
-template <int L, int NB, int MINB, bool ASYNC>
+template <int L, int NB, int MINB, bool ASYNC, bool ALL = false>
 static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* B,
                        int64_t ldb, int64_t nk, float* C, int64_t ldc, int accumulate, float* partial,
                        cudaStream_t s) {
+  if constexpr (ASYNC) {
+    if (!ALL && nk % (4 * L) == 0)  // no masked lanes: the unmasked build
+      return launch_vrow<L, NB, MINB, true, true>(ctx, v, A, B, ldb, nk, C, ldc, accumulate, partial, s);
+  }
   auto kern = [] {
-    if constexpr (ASYNC) return spmm_vrow_async_k<L, NB, MINB>;
+    if constexpr (ASYNC) return spmm_vrow_async_k<L, NB, MINB, ALL>;
     else return spmm_vrow_k<L, NB, MINB>;
   }();
+  using LdT = std::conditional_t<ASYNC, int, int64_t>;
   const size_t smem = ASYNC ? sizeof(float4) * NB * VR_THREADS : 0;
   static int occ = -1;  // per process: one device model
   if (occ < 0) {
@@ -418,8 +445,8 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
   const int64_t need = (v.nv * L + VR_THREADS - 1) / VR_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
-    kern<<<grid, VR_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val, B, ldb, C, ldc,
-                                        c0, nk, A->index_base, accumulate, partial);
+    kern<<<grid, VR_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val, B, (LdT)ldb, C,
+                                        ldc, c0, nk, A->index_base, accumulate, partial);
   if (v.nl > 0)
     vrow_fixup_k<<<grid_for(v.nl * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nl, nk, v.part_row, partial,
                                                                          C, ldc);
@@ -442,6 +469,8 @@ int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const vo
   const float* b = (const float*)B;
   float* c = (float*)C;
   float* part = (float*)partial;
+  if (async_gather && ldb > INT32_MAX)
+    return set_error(FGB_EUNSUPPORTED, "spmm vrow: cp.async gathers need a leading dimension below 2^31");
   if (async_gather) {  // 32 KB of gather slots per block: 6 blocks (48 warps) per SM
     if (slab == 8) return launch_vrow<2, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
     if (slab == 16) return launch_vrow<4, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
