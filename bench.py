@@ -576,13 +576,24 @@ def suite_sddmm() -> list[dict]:
     t = _cpu_time(lambda: oracle.sddmm_csr(rows, p, A.idx[:nnz_s], A.val[:nnz_s], X[:rows], Y,
                                            nthreads=threads), min_seconds=3.0)
     t_full = t * A.nnz / max(nnz_s, 1)
+    # virtual-row plans gather one slab of a Y row per stored entry and slab
+    info = plan.info()
+    gather = None
+    if info["variant"] in (3, 4):
+        gbytes = 16 * info["lanes"] if info["lanes"] > 0 else 4 * 64
+        gathered = A.nnz * 64 * 4
+        ceiling = dev.gather_ceiling(m * gbytes, gbytes)
+        g_ach = gathered / (ms / 1e3) / 1e9
+        gather = {"gathered_bytes_per_call": gathered, "gather_bytes": gbytes,
+                  "working_set_bytes": m * gbytes, "achieved": round(g_ach, 1),
+                  "ceiling": round(ceiling, 1), "unit": "GB/s", "frac": round(g_ach / ceiling, 4)}
     return [{"suite": "sddmm_1M_k64", "metric": "sddmm_gbps_algorithmic",
              "value": round(nbytes / (ms / 1e3) / 1e9, 1), "unit": "GB/s", "dtype": "f32",
              "ms_per_call": round(ms, 4),
              "schedules_ms": {k: round(v, 4) for k, v in schedules.items()},
-             "plan_choice": plan.info(),
+             "plan_choice": info,
              "config": {"workload": "zipf1.5 1Mx1M nnz 16M CSR, X/Y 1Mx64 N(0,1)"},
-             "roofline": _roof(nbytes, ms),
+             "roofline": _roof(nbytes, ms), "gather_ceiling": gather,
              "cpu_baseline": {"value": round(nbytes / t_full / 1e9, 3), "unit": "GB/s",
                               "cores": threads, "kind": "port",
                               "sample": f"rows 1..{rows}, time scaled by stored entries"}}]

@@ -142,7 +142,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
       return spmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype, d.flags,
                        c.lanes, 0, s);
     case FGB_PLAN_SDDMM:
-      if (c.variant == 3) {  // virtual rows (schedule built outside capture)
+      if (c.variant == 3 || c.variant == 4) {  // virtual rows (schedule built outside capture); 4: cp.async gathers
         auto it = p->vrows.find(c.path);
         if (it == p->vrows.end()) {
           VrowSchedule v;
@@ -151,7 +151,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           it = p->vrows.emplace(c.path, v).first;
         }
         return sddmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, s,
-                          c.lanes > 0 ? 4 * c.lanes : 0);
+                          c.lanes > 0 ? 4 * c.lanes : 0, c.variant == 4);
       }
       return sddmm_impl(p->ctx, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, d.dtype,
                         d.flags, c.lanes, c.path, s,
@@ -201,10 +201,11 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{d.dtype == FGB_F64 ? 16 : 8, chunk, 1, 2});
     if (d.dtype == FGB_F32 && p->A.orient == FGB_CSR && p->A.val_t == FGB_F32 && d.k <= 128 &&
         d.k % 4 == 0 && d.ld_in0 % 4 == 0 && d.ld_in1 % 4 == 0 && p->A.nnz <= INT32_MAX)
-      for (int64_t t : {64, 128, 256}) {  // virtual rows, all of k or 32-column slabs
-        out.push_back(Choice{0, t, 1, 3});
-        if (d.k > 32) out.push_back(Choice{8, t, 1, 3});
-      }
+      for (int64_t t : {64, 128, 256})  // virtual rows, all of k or 32-column slabs
+        for (int v : {3, 4}) {            // register / cp.async gathers
+          out.push_back(Choice{0, t, 1, v});
+          if (d.k > 32) out.push_back(Choice{8, t, 1, v});
+        }
   }
   return out;
 }
@@ -319,7 +320,9 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   }
   p->choice = best;
   for (auto it = p->vrows.begin(); it != p->vrows.end();) {  // and the chosen schedule
-    if ((best.variant != 2 && best.variant != 3) || it->first != best.path) {
+    const bool vrow_choice = p->d.op == FGB_PLAN_SPMM ? (best.variant == 2 || best.variant == 3)
+                                                       : (best.variant == 3 || best.variant == 4);
+    if (!vrow_choice || it->first != best.path) {
       vrow_free(&it->second);
       it = p->vrows.erase(it);
     } else {

@@ -260,24 +260,25 @@ extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, in
     return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: lanes must be 0, 4, 8, 16 or 32");
   if (tune && (tune->chunk < 0 || tune->slab < -1))
     return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: negative chunk or slab");
-  if (tune && tune->variant == 1) {  // virtual rows: schedule built for this call
+  if (tune && (tune->variant == 1 || tune->variant == 2)) {  // virtual rows: schedule built for this call
     if (!ctx) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: null ctx");
     int rc = fgb::check_sparse(A, "fgb_sddmm_ex: A", true);
     if (rc) return rc;
     if (dtype != FGB_F32 || A->val_t != FGB_F32 || (flags & FGB_FINCH_ORDER))
-      return fgb::set_error(FGB_EUNSUPPORTED, "fgb_sddmm_ex: variant 1 needs F32 and no FGB_FINCH_ORDER");
+      return fgb::set_error(FGB_EUNSUPPORTED, "fgb_sddmm_ex: variants 1 and 2 need F32 and no FGB_FINCH_ORDER");
     if (A->nnz == 0) return FGB_OK;
     cudaStream_t s = fgb::pick_stream(ctx, stream);
     fgb::VrowSchedule v;
     rc = fgb::vrow_build(ctx, A, tune->chunk > 0 ? (int)std::min<int64_t>(tune->chunk, 4096) : 128, &v, s);
     if (rc) return rc;
-    rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s, tune->slab > 0 ? tune->slab : 0);
+    rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s, tune->slab > 0 ? tune->slab : 0,
+                         tune->variant == 2);
     cudaError_t e = cudaStreamSynchronize(s);
     fgb::vrow_free(&v);
     if (rc == FGB_OK && e != cudaSuccess) rc = fgb::set_error(FGB_ECUDA, "fgb_sddmm_ex: %s", cudaGetErrorString(e));
     return rc;
   }
-  if (tune && tune->variant != 0) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: variant must be 0 or 1");
+  if (tune && tune->variant != 0) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: variant must be 0, 1 or 2");
   return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, lanes,
                          tune ? tune->chunk : 0, stream, tune ? tune->slab : -1);
 }

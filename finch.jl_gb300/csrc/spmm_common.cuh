@@ -45,8 +45,10 @@ int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const vo
 
 // SDDMM over the same virtual rows (sddmm_vrow.cu): F32 CSR, k <= 128, k % 4 == 0.
 // slab: columns of k per launch (0 = all of k), a multiple of 4.
+// async_gather: gathers of Y staged in shared memory by cp.async.
 int sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* X, int64_t ldx,
-               const void* Y, int64_t ldy, int64_t k, void* out, cudaStream_t s, int64_t slab = 0);
+               const void* Y, int64_t ldy, int64_t k, void* out, cudaStream_t s, int64_t slab = 0,
+               bool async_gather = false);
 
 // Stage-ring (TMA gather4) kernels over planned merge-path items (spmm_tma.cu).
 int spmm_tma_items(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk,

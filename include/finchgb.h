@@ -277,8 +277,9 @@ FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t 
  * when Y is far larger than L2).  variant 1 (F32 CSR, k <= 128 and a multiple
  * of 4): sub-groups own virtual rows of at most `chunk` entries, sorted by
  * length, holding the row's slice of X in registers; `slab` > 0 (a multiple
- * of 4) cuts k into launches of that many columns.  Zero lanes/chunk take
- * the defaults. */
+ * of 4) cuts k into launches of that many columns.  variant 2: variant 1
+ * with the gathers of Y staged in shared memory by cp.async (identical
+ * results).  Zero lanes/chunk take the defaults. */
 typedef struct fgb_sddmm_tuning {
   int32_t lanes;
   int32_t variant;
@@ -420,7 +421,8 @@ typedef struct fgb_plan_info {
   int32_t candidates;        /* schedules in the search space */
   int32_t from_cache;        /* 1 if the choice came from the tuning cache */
   int32_t panels;            /* SpMM: column panels of the chosen schedule (1 = none) */
-  int32_t variant;           /* SpMM: fgb_spmm_tuning.variant; SDDMM: 3 virtual rows */
+  int32_t variant;           /* SpMM: fgb_spmm_tuning.variant; SDDMM: 3 virtual rows, 4 the same
+                                with cp.async gathers */
 } fgb_plan_info;
 
 /* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use

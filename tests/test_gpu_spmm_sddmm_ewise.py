@@ -234,9 +234,15 @@ def test_sddmm(gpu_lib, k, dtype):
             out5 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1, slab=32))
             assert_close(out5, want, scale, dtype)
             assert np.array_equal(out4, to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=1)))
+            # gathers of Y staged in shared memory by cp.async: identical results
+            assert np.array_equal(out4, to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=2)))
+            out6 = to_host(dev.sddmm(A, to_dev(X), to_dev(Y), chunk=T, variant=2, slab=32))
+            assert np.array_equal(out5, out6)
     else:
         with pytest.raises(L.FinchGBError):
             dev.sddmm(A, to_dev(X), to_dev(Y), chunk=64, variant=1)
+        with pytest.raises(L.FinchGBError):
+            dev.sddmm(A, to_dev(X), to_dev(Y), chunk=64, variant=2)
 
 
 def test_sddmm_csc_swaps_roles(gpu_lib):
