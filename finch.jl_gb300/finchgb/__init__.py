@@ -21,6 +21,7 @@ from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, def
                         einsum, finch, get_scheduler, set_scheduler, with_scheduler)
 from .tensors import (GPU, Dense, Element, Pattern, SparseCOO, SparseList, SwizzleArray, Tensor,
                       csr, fsparse, fsprand, gpu, swizzle, transfer)
+from .galley import GalleyScheduler, galley_scheduler
 
 __all__ = [
     "FinchGBError", "FinchGBUnsupported", "DeviceSparse", "context", "spmv", "spmm", "sddmm",
@@ -28,5 +29,5 @@ __all__ = [
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",
     "default_scheduler", "get_scheduler", "set_scheduler", "with_scheduler", "GPU", "Dense",
     "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsparse", "fsprand", "fread", "fwrite", "FinchExtensionError",
-    "gpu", "swizzle", "transfer", "_lib",
+    "gpu", "swizzle", "transfer", "_lib", "GalleyScheduler", "galley_scheduler",
 ]

@@ -296,6 +296,10 @@ def spgemm(A: DeviceSparse, B: DeviceSparse, flags: int = 0) -> DeviceSparse:
                      L.I32, dtype_code(c_val), 0, c_ptr.data_ptr(), c_idx.data_ptr(), c_val.data_ptr())
     L.call("fgb_spgemm_numeric", ctx, ctypes.byref(da), ctypes.byref(db), dtype_code(A.val), flags,
            ctypes.byref(dc), stream_ptr())
+    if k < 2**31 - 1:  # the upload layout: 32-bit ptr below 2^31 entries
+        p32 = torch.empty(nf + 1, dtype=torch.int32, device=d)
+        L.call("fgb_narrow_index", ctx, c_ptr.data_ptr(), p32.data_ptr(), nf + 1, 0, stream_ptr())
+        c_ptr = p32
     return DeviceSparse(A.nrows, B.ncols, c_ptr, c_idx[:k], c_val[:k], A.orient, A.base)
 
 

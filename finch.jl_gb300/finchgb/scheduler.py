@@ -173,7 +173,7 @@ class GB300Scheduler:
 
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
-        for rule in (self._spmv, self._spmm, self._sddmm, self._ewise, self._ewise_reduce,
+        for rule in (self._spmv, self._spmm, self._spgemm, self._sddmm, self._ewise, self._ewise_reduce,
                      self._dot, self._dense_map, self._scalar):
             r = rule(m, out, accumulate)
             if r is not None:
@@ -238,6 +238,30 @@ class GB300Scheduler:
                 C = dev.spmm(A, B, C, flags=flags)
                 return dense_from_device(C)
         return None
+
+    # -- C[i,k] += A[i,j] * B[j,k] with both sparse: a sparse result (Gustavson)
+    def _spgemm(self, m: Match, out, accumulate):
+        if m.agg != "+" or len(m.outs) != 2 or len(m.red) != 1 or out is not None:
+            return None
+        args = _args(m.core, "*")
+        if not args or len(args) != 2:
+            return None
+        (i, k), (j,) = m.outs, m.red
+        a, b = args
+        if not all(isinstance(t, Access) and _is_sparse(t.tns) for t in (a, b)):
+            return None
+        if set(a.idxs) != {i, j}:
+            a, b = b, a
+        if set(a.idxs) != {i, j} or set(b.idxs) != {j, k}:
+            return None
+        A = sparse_operand(a.tns, a.idxs, (i, j))
+        B = sparse_operand(b.tns, b.idxs, (j, k))
+        if A.val is None or B.val is None:
+            return None
+        if B.orient != A.orient:
+            B = _other_orientation(b.tns, B)
+        self.last_kernel = "fgb_spgemm"
+        return sparse_from_device(dev.spgemm(A, B))
 
     # -- C[i,j] = A[i,j] * sum_k X[i,k] * Y[j,k]
     def _sddmm(self, m: Match, out, accumulate):

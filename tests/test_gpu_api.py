@@ -175,6 +175,15 @@ def test_cg_in_einsum_small(gpu_lib):
 
 
 def test_unsupported_plan_raises(gpu_lib):
-    A = csc(np.eye(4))
+    D = F.Tensor(F.Dense(F.Dense(F.Element(0.0))), np.eye(4))
     with pytest.raises(F.FinchGBUnsupported):
-        F.einsum("C[i,j] += A[i,k] * B[k,j]", A=A, B=csc(np.eye(4)))  # SpGEMM
+        F.einsum("C[i,j] += A[i,k] * B[k,j]", A=D, B=D)  # dense GEMM: no kernel here
+
+
+def test_einsum_sparse_times_sparse_is_spgemm(gpu_lib):
+    rng = np.random.default_rng(21)
+    Ad = np.where(rng.random((30, 20)) < 0.2, rng.integers(1, 5, (30, 20)), 0).astype(np.float64)
+    Bd = np.where(rng.random((20, 25)) < 0.2, rng.integers(1, 5, (20, 25)), 0).astype(np.float64)
+    C = F.einsum("C[i,j] += A[i,k] * B[k,j]", A=csc(Ad), B=csc(Bd))
+    assert F.get_scheduler().last_kernel == "fgb_spgemm"
+    assert np.array_equal(C.todense(), Ad @ Bd)
