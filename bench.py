@@ -686,6 +686,20 @@ def suite_semiring() -> list[dict]:
                          "ms_per_call": round(ms_pull, 4), "lanes_per_row": plan_or.info()["lanes"],
                          "config": {"workload": "same graph, Pattern level, CSR copy"},
                          "roofline": _roof(or_bytes, ms_pull)})
+    # The pull SpMVs gather one x value per stored entry (a 32-byte sector
+    # request each) from an L2-resident x: their ceiling is the device's
+    # random-gather request rate over x's working set.
+    def gather_line(gathers_per_call, ms_call, x_bytes):
+        rate = dev.gather_ceiling(x_bytes, 4) / 4  # gathers per second (GB/s of 4-byte words / 4)
+        achieved = gathers_per_call / (ms_call / 1e3)
+        return {"gathers_per_call": int(gathers_per_call), "achieved_g_per_s": round(achieved / 1e9, 1),
+                "ceiling_g_per_s": round(rate, 1), "working_set_bytes": int(x_bytes),
+                "frac": round(achieved / 1e9 / rate, 4)}
+
+    mp_gather = gather_line(g.nnz, ms20_pull / 20, 4 * n)
+    for line in or_lines:
+        if line["variant"] == "csr_pull":
+            line["gather_ceiling"] = gather_line(g.nnz, line["ms_per_call"], n)
     threads = oracle.max_threads()
     xh = np.full(n, sentinel, dtype=np.int32)
     xh[0] = 0
@@ -706,7 +720,7 @@ def suite_semiring() -> list[dict]:
              "one_time_csr_copy_ms": round(ms_transpose, 3), "equal_to_push": same,
              "lanes_per_row": plan_mp.info()["lanes"],
              "config": {"workload": "same graph; CSR copy built once on the device"},
-             "roofline": _roof(20 * per_round_bytes, ms20_pull)}] + or_lines
+             "roofline": _roof(20 * per_round_bytes, ms20_pull), "gather_ceiling": mp_gather}] + or_lines
 
 
 def suite_cg() -> list[dict]:

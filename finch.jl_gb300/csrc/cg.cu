@@ -29,6 +29,11 @@
 namespace fgb {
 
 constexpr int CG_THREADS = 256;
+constexpr int CG_ILP = 4;  // elements per thread in flight in the streaming updates
+// The updates run one block of 1024 threads per SM, each thread with CG_ILP
+// elements in flight (up to 64 registers): few partials, one load per thread
+// in each block's fold of the previous kernel's partials.
+constexpr int CG_UPD_THREADS = 1024;
 
 template <class T>
 __device__ __forceinline__ T cg_block_sum(T v, T* sh) {
@@ -71,27 +76,42 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
     int base, const double* __restrict__ p, double* __restrict__ q, double* __restrict__ part) {
   __shared__ double sh[33];
   double dot = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k0 = ld_ptr(ptr, i) - base, k1 = ld_ptr(ptr, i + 1) - base;
-    ACC acc = ACC(0);
-    for (int64_t k = k0; k < k1; ++k) {
-      const int j = __ldg(idx + k) - base;
-      if constexpr (sizeof(ACC) == 4)
-        acc = __fmaf_rn(cg_val(val, k), (float)__ldg(p + j), acc);
-      else
-        acc = __fma_rn((double)__ldg((const double*)val + k), __ldg(p + j), acc);
+  auto term = [&](int64_t k, ACC acc) -> ACC {
+    const int j = __ldg(idx + k) - base;
+    if constexpr (sizeof(ACC) == 4)
+      return __fmaf_rn(cg_val(val, k), (float)__ldg(p + j), acc);
+    else
+      return __fma_rn((double)__ldg((const double*)val + k), __ldg(p + j), acc);
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // two rows (i, i + stride) per thread in flight; rows and their products
+  // in the plain loop's order, so q and the partial are bit-identical
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+    const int64_t i2 = i + stride;
+    const bool two = i2 < n;
+    const int64_t a0 = ld_ptr(ptr, i) - base, a1 = ld_ptr(ptr, i + 1) - base;
+    const int64_t b0 = two ? ld_ptr(ptr, i2) - base : 0, b1 = two ? ld_ptr(ptr, i2 + 1) - base : 0;
+    ACC acc_a = ACC(0), acc_b = ACC(0);
+    const int64_t la = a1 - a0, lb = b1 - b0;
+    for (int64_t t = 0; t < (la > lb ? la : lb); ++t) {
+      if (t < la) acc_a = term(a0 + t, acc_a);
+      if (t < lb) acc_b = term(b0 + t, acc_b);
     }
-    const double qi = (double)acc;
-    q[i] = qi;
-    dot = __fma_rn(__ldg(p + i), qi, dot);
+    const double qa = (double)acc_a;
+    q[i] = qa;
+    dot = __fma_rn(__ldg(p + i), qa, dot);
+    if (two) {
+      const double qb = (double)acc_b;
+      q[i2] = qb;
+      dot = __fma_rn(__ldg(p + i2), qb, dot);
+    }
   }
   dot = cg_block_sum(dot, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = dot;
 }
 
 // alpha = rr[slot] / (p.q);  x += alpha p;  r -= alpha q;  partials of r.r
-__global__ void __launch_bounds__(CG_THREADS) cg_update_xr(
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xr(
     int64_t n, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
     const double* __restrict__ q, const double* __restrict__ part_pq, int nparts,
     const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
@@ -100,8 +120,28 @@ __global__ void __launch_bounds__(CG_THREADS) cg_update_xr(
   // a vanished curvature (p.q == 0) only happens once r is exactly zero
   const double alpha = pq != 0.0 ? rr[slot] / pq : 0.0;
   double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // CG_ILP elements per thread in flight: all loads first, then the updates
+  // in the same element order as the plain loop (bit-identical partials)
+  for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
+    double pv[CG_ILP], qv[CG_ILP], xv[CG_ILP], rv[CG_ILP];
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      pv[u] = p[i + u * stride];
+      qv[u] = q[i + u * stride];
+      xv[u] = x[i + u * stride];
+      rv[u] = r[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      x[i + u * stride] = __fma_rn(alpha, pv[u], xv[u]);
+      const double ri = __fma_rn(-alpha, qv[u], rv[u]);
+      r[i + u * stride] = ri;
+      acc = __fma_rn(ri, ri, acc);
+    }
+  }
+  for (; i < n; i += stride) {
     x[i] = __fma_rn(alpha, p[i], x[i]);
     const double ri = __fma_rn(-alpha, q[i], r[i]);
     r[i] = ri;
@@ -112,16 +152,26 @@ __global__ void __launch_bounds__(CG_THREADS) cg_update_xr(
 }
 
 // rr' = fold(r.r partials);  p = r + (rr' / rr[slot_in]) p;  rr[slot_out] = rr'
-__global__ void __launch_bounds__(CG_THREADS) cg_update_p(
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_p(
     int64_t n, const double* __restrict__ r, double* __restrict__ p,
     const double* __restrict__ part_rr, int nparts, double* __restrict__ rr, int slot_in,
     int slot_out, double* __restrict__ hist, int64_t it) {
   __shared__ double sh[33];
   const double rr_new = fold_parts(part_rr, nparts, sh);
   const double beta = rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = __fma_rn(beta, p[i], r[i]);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
+    double pv[CG_ILP], rv[CG_ILP];
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      pv[u] = p[i + u * stride];
+      rv[u] = r[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) p[i + u * stride] = __fma_rn(beta, pv[u], rv[u]);
+  }
+  for (; i < n; i += stride) p[i] = __fma_rn(beta, p[i], r[i]);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     rr[slot_out] = rr_new;
     hist[it] = rr_new;
@@ -175,6 +225,26 @@ struct CgBuffers {
   double *r = nullptr, *p = nullptr, *q = nullptr, *part_a = nullptr, *part_b = nullptr,
          *part_c = nullptr, *rr = nullptr, *bb = nullptr, *hist = nullptr;
 };
+
+// The SpMV's own grid: at most `grid` blocks and no more than fit the SMs at
+// once (its two rows per thread take more registers than the updates).
+template <class VT, class ACC, class PtrT>
+static int dot_grid_t(int grid, int sms) {
+  static int occ = -1;  // per process: one device model
+  if (occ < 0) {
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cg_spmv_dot<VT, ACC, PtrT>, CG_THREADS, 0);
+    occ = o > 0 ? o : 1;
+  }
+  return std::max(1, std::min(grid, occ * sms));
+}
+
+template <class PtrT>
+static int spmv_dot_grid(int precision, int grid, int sms) {
+  if (precision == FGB_F64) return dot_grid_t<double, double, PtrT>(grid, sms);
+  if (precision == FGB_BF16) return dot_grid_t<__nv_bfloat16, float, PtrT>(grid, sms);
+  return dot_grid_t<float, float, PtrT>(grid, sms);
+}
 
 template <class PtrT>
 static void launch_spmv_dot(const fgb_sparse* A, int precision, int grid, const double* p,
@@ -287,12 +357,17 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     }
     // one chunk of iterations, captured once (slots alternate; chunk is even)
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { fail(FGB_ECUDA, "capture", e); break; }
+    const int grid_upd = grid_for(n, CG_UPD_THREADS, ctx->num_sms, 1);  // <= grid partial slots
+    const int grid_dot = Ait->ptr_t == FGB_I32 ? spmv_dot_grid<int32_t>(precision, grid, ctx->num_sms)
+                                               : spmv_dot_grid<int64_t>(precision, grid, ctx->num_sms);
     for (int t = 0; t < chunk; ++t) {
       const int si = t & 1, so = si ^ 1;
-      if (Ait->ptr_t == FGB_I32) launch_spmv_dot<int32_t>(Ait, precision, grid, bufs.p, bufs.q, bufs.part_a, s);
-      else launch_spmv_dot<int64_t>(Ait, precision, grid, bufs.p, bufs.q, bufs.part_a, s);
-      cg_update_xr<<<grid, CG_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.q, bufs.part_a, grid, bufs.rr, si, bufs.part_b);
-      cg_update_p<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p, bufs.part_b, grid, bufs.rr, si, so, bufs.hist, t);
+      if (Ait->ptr_t == FGB_I32) launch_spmv_dot<int32_t>(Ait, precision, grid_dot, bufs.p, bufs.q, bufs.part_a, s);
+      else launch_spmv_dot<int64_t>(Ait, precision, grid_dot, bufs.p, bufs.q, bufs.part_a, s);
+      cg_update_xr<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
+                                              bufs.part_b);
+      cg_update_p<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.p, bufs.part_b, grid_upd, bufs.rr, si, so,
+                                                     bufs.hist, t);
     }
     e = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);

@@ -17,10 +17,11 @@ extern "C" {
 #endif
 
 /* Random-gather ceiling: times `gathers` loads of `gather_bytes` contiguous
- * bytes each (16, 32, 64, 128, 256 or 512; aligned to their size) at
+ * bytes each (4, 8, 16, 32, 64, 128, 256 or 512; aligned to their size) at
  * uniformly random places of a device buffer of `working_set_bytes`, issued
  * the way the gather kernels issue them (16 bytes per lane, 8 loads in flight
- * per lane, L2 evict_last).  `*gbs` receives gathered bytes / device time in
+ * per lane, L2 evict_last; 4- and 8-byte gathers one per lane, as the x
+ * gathers of a pull SpMV).  `*gbs` receives gathered bytes / device time in
  * GB/s (CUDA events on `stream`, after warm-up).  Synchronous; allocates and
  * frees its buffer on `stream`.  EINVAL for a width outside the list, a
  * working set smaller than 64 gathers or `gathers` <= 0. */

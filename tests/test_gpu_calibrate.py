@@ -17,12 +17,12 @@ def test_gather_ceiling_orders_working_sets():
     assert small > 0.9 * large
 
 
-@pytest.mark.parametrize("width", [16, 64, 512])
+@pytest.mark.parametrize("width", [4, 8, 16, 64, 512])
 def test_gather_ceiling_widths(width):
     assert dev.gather_ceiling(64 << 20, width, gathers=1 << 20) > 0
 
 
-@pytest.mark.parametrize("width,ws,gathers", [(24, 1 << 20, 1024), (1024, 1 << 20, 1024),
+@pytest.mark.parametrize("width,ws,gathers", [(24, 1 << 20, 1024), (1024, 1 << 20, 1024), (2, 1 << 20, 1024),
                                               (128, 1024, 1024), (128, 1 << 20, 0)])
 def test_gather_ceiling_rejects(width, ws, gathers):
     with pytest.raises(L.FinchGBError) as e:
