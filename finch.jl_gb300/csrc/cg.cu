@@ -230,12 +230,11 @@ struct CgBuffers {
 // once (its two rows per thread take more registers than the updates).
 template <class VT, class ACC, class PtrT>
 static int dot_grid_t(int grid, int sms) {
-  static int occ = -1;  // per process: one device model
-  if (occ < 0) {
+  static const int occ = [] {  // once per process (one device model); thread-safe
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cg_spmv_dot<VT, ACC, PtrT>, CG_THREADS, 0);
-    occ = o > 0 ? o : 1;
-  }
+    return o > 0 ? o : 1;
+  }();
   return std::max(1, std::min(grid, occ * sms));
 }
 

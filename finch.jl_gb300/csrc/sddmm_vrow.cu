@@ -137,13 +137,12 @@ static int launch_sddmm_vrow_async(fgb_ctx* ctx, const VrowSchedule& v, const fg
                                    int mode, cudaStream_t s) {
   constexpr int NB = L >= 8 ? 8 : L;
   constexpr size_t smem = sizeof(float4) * NB * SV_THREADS;
-  static int occ = -1;  // per process: one device model
-  if (occ < 0) {
+  static const int occ = [] {  // once per process (one device model); thread-safe
     cudaFuncSetAttribute(sddmm_vrow_async_k<L, NB, 6>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_async_k<L, NB, 6>, SV_THREADS, smem);
-    occ = o > 0 ? o : 1;
-  }
+    return o > 0 ? o : 1;
+  }();
   const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   sddmm_vrow_async_k<L, NB, 6><<<grid, SV_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx,
@@ -158,12 +157,11 @@ static int launch_sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_spar
                              int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
                              int mode, cudaStream_t s) {
   constexpr int NB = L >= 4 ? 4 : L;
-  static int occ = -1;  // per process: one device model
-  if (occ < 0) {
+  static const int occ = [] {  // once per process (one device model); thread-safe
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_k<L, NB>, SV_THREADS, 0);
-    occ = o > 0 ? o : 1;
-  }
+    return o > 0 ? o : 1;
+  }();
   const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   sddmm_vrow_k<L, NB><<<grid, SV_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val,

@@ -435,13 +435,12 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
   }();
   using LdT = std::conditional_t<ASYNC, int, int64_t>;
   const size_t smem = ASYNC ? sizeof(float4) * NB * VR_THREADS : 0;
-  static int occ = -1;  // per process: one device model
-  if (occ < 0) {
+  static const int occ = [&] {  // once per process (one device model); thread-safe
     if (ASYNC) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, VR_THREADS, smem);
-    occ = o > 0 ? o : 1;
-  }
+    return o > 0 ? o : 1;
+  }();
   const int64_t need = (v.nv * L + VR_THREADS - 1) / VR_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
