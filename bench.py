@@ -26,7 +26,6 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
-import os
 import statistics
 import subprocess
 import sys

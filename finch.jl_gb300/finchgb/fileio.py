@@ -19,7 +19,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .tensors import (GPU, Dense, Element, Pattern, SparseCOO, SparseList, SwizzleArray, Tensor,
+from .tensors import (GPU, Dense, Element, Pattern, SparseList, SwizzleArray, Tensor,
                       fsparse, swizzle, transfer)
 from .workloads import SparseBuffers
 

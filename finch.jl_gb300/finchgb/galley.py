@@ -35,14 +35,13 @@ array.
 """
 from __future__ import annotations
 
-import itertools
 import math
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import _lib as L
-from .logic import Access, Aggregate, Literal, MapJoin, Node, Reorder, flatten, indices_of
+from .logic import Access, Aggregate, MapJoin, Node, Reorder, flatten, indices_of
 from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, _csr_copy, _is_dense, _is_sparse,
                         _other_orientation)
 from .tensors import SwizzleArray, swizzle
