@@ -84,6 +84,18 @@ int fgb_ctx_create(int device, fgb_ctx** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+  // The library's scratch comes from this process's default stream-ordered
+  // pool of the device.  With the default release threshold (0) the pool
+  // unmaps freed blocks at every synchronisation and the next call maps them
+  // again; keeping up to FGB_POOL_KEEP_BYTES mapped makes repeated calls
+  // (COO assembly, SpGEMM, schedules built per call) reuse their scratch.
+  cudaMemPool_t pool = nullptr;
+  if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, device);
+  if (e == cudaSuccess) {
+    uint64_t keep = FGB_POOL_KEEP_BYTES, cur = 0;
+    e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur);
+    if (e == cudaSuccess && cur < keep) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (e != cudaSuccess) {
     delete c;
     return set_error(FGB_ECUDA, "fgb_ctx_create: %s", cudaGetErrorString(e));

@@ -122,9 +122,13 @@ FGB_API int fgb_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 FGB_API const char* fgb_last_error(void);
 
-/* Create a context on `device`: records SM count, creates a stream.
- * Replaces the CPU device of src/architecture.jl (AbstractDevice/CPU,
- * architecture.jl:1-60) as the place Finch runs the matched nests. */
+/* Create a context on `device`: records SM count, creates a stream, and
+ * lets this process's default stream-ordered memory pool of the device keep
+ * up to FGB_POOL_KEEP_BYTES of freed scratch mapped for reuse (it never
+ * lowers a larger threshold the caller set).  Replaces the CPU device of
+ * src/architecture.jl (AbstractDevice/CPU, architecture.jl:1-60) as the place
+ * Finch runs the matched nests. */
+#define FGB_POOL_KEEP_BYTES (8ull << 30)
 FGB_API int fgb_ctx_create(int device, fgb_ctx** out);
 FGB_API int fgb_ctx_destroy(fgb_ctx* ctx);
 /* The context's stream (a cudaStream_t). */
