@@ -254,8 +254,12 @@ def run_gpu(args):
         info = plan.info()
         npanels = info["panels"]
     variant = info["variant"] if plan is not None else fixed_variant
-    plan_lanes = info["lanes"] if plan is not None else lanes
+    # lanes 0 in a fixed schedule is the library's own default; for this
+    # workload that is the 32-column slab schedule (8 lanes)
+    plan_lanes = info["lanes"] if plan is not None else (lanes if lanes > 0 else 8)
     slabs = -(-NK // (4 * plan_lanes))
+    if plan is None and lanes == 0 and path == 0 and variant == 0:
+        variant = 3  # the library's default for a B far larger than L2
     if plan is None and variant in (2, 3):  # schedule built per call: counted as its kernels
         launches_per_step = 10 + slabs
     elif plan is None:

@@ -269,13 +269,12 @@ extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, in
     if (A->nnz == 0) return FGB_OK;
     cudaStream_t s = fgb::pick_stream(ctx, stream);
     fgb::VrowSchedule v;
-    rc = fgb::vrow_build(ctx, A, tune->chunk > 0 ? (int)std::min<int64_t>(tune->chunk, 4096) : 128, &v, s);
+    rc = fgb::vrow_build(ctx, A, tune->chunk > 0 ? (int)std::min<int64_t>(tune->chunk, 4096) : 128, &v, s,
+                         true);
     if (rc) return rc;
     rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s, tune->slab > 0 ? tune->slab : 0,
                          tune->variant == 2);
-    cudaError_t e = cudaStreamSynchronize(s);
-    fgb::vrow_free(&v);
-    if (rc == FGB_OK && e != cudaSuccess) rc = fgb::set_error(FGB_ECUDA, "fgb_sddmm_ex: %s", cudaGetErrorString(e));
+    fgb::vrow_free(&v, s);  // stream-ordered, behind the launches
     return rc;
   }
   if (tune && tune->variant != 0) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: variant must be 0, 1 or 2");

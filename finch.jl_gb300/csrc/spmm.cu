@@ -157,18 +157,17 @@ static int default_lanes(int64_t nk, int vn, int64_t b_bytes) {
   return lanes;
 }
 
-// Default merge-path tuning: the column slab keeps the gathered slab of B
-// within about half of L2 (one slab when B already fits), items of 256
-// path steps.
+// Default merge-path tuning: lanes enough for all of nk (up to 32, i.e.
+// whole 512-byte rows of fp32 B per gather), items of 256 path steps.
+// Narrower column slabs do not shrink B's L2 footprint on row-major B --
+// a 64-byte slice still occupies a whole 128-byte line -- and they re-read
+// A once per slab: on the 1M x 1M Zipf matrix with k = 128, 4 lanes (16
+// columns) take 6.0 ms and 32 lanes 2.1 ms.
 static void default_merge_tuning(const fgb_sparse* A, int64_t nk, size_t esz, int* lanes,
                                  int64_t* path) {
+  (void)A;
   const int vn = esz == 4 ? 4 : 2;
-  const double b_bytes = (double)A->ncols * (double)nk * (double)esz;
-  const double budget = 64.0 * 1024 * 1024;
-  int64_t slab = nk;
-  while (slab > vn * 4 && (double)A->ncols * slab * esz > budget) slab /= 2;
-  (void)b_bytes;
-  int64_t need = (slab + vn - 1) / vn;
+  const int64_t need = (nk + vn - 1) / vn;
   int l = 4;
   while (l < need && l < 32) l *= 2;
   if (*lanes <= 0) *lanes = l;
@@ -228,26 +227,39 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
   if ((A->ncols > 0 && nk > 0 && !B) || (A->nrows > 0 && nk > 0 && !C))
     return set_error(FGB_EINVAL, "fgb_spmm: null B or C");
   cudaStream_t s = pick_stream(ctx, stream);
+  // No schedule given: a B far larger than L2 with many stored entries takes
+  // the virtual-row slab schedule with cp.async gathers (32-column slabs,
+  // 128-entry virtual rows; on the 1M x 1M Zipf matrix with k = 128, 1.23 ms
+  // per call with its schedule built, against 2.1 ms for the best merge path).
+  if (variant == 0 && lanes <= 0 && path <= 0 && A->orient == FGB_CSR && dtype == FGB_F32 &&
+      A->val_t == FGB_F32 && A->idx_t == FGB_I32 && !(flags & FGB_FINCH_ORDER) && nk >= 32 && nk % 4 == 0 &&
+      ldb % 4 == 0 && ldc % 4 == 0 && ldb <= INT32_MAX && (uintptr_t)B % 16 == 0 && (uintptr_t)C % 16 == 0 &&
+      A->nrows <= INT32_MAX && A->nnz >= (1 << 20) && A->nnz <= INT32_MAX &&
+      (double)A->ncols * (double)nk * 4.0 > 64.0 * 1024 * 1024) {
+    variant = 3;
+    lanes = 8;
+    path = 128;
+  }
   if (variant == 2 || variant == 3) {  // virtual-row column slabs: schedule built for this call
     if (A->orient != FGB_CSR || dtype != FGB_F32 || (flags & FGB_FINCH_ORDER))
       return set_error(FGB_EUNSUPPORTED, "fgb_spmm: variants 2 and 3 need CSR, F32 and no FGB_FINCH_ORDER");
     if (A->nrows == 0 || nk == 0) return FGB_OK;
+    // the schedule and partial sums come from the stream-ordered pool and go
+    // back to it behind the launches (no device-wide synchronisation)
     VrowSchedule v;
-    rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s);
+    rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s, true);
     if (rc) return rc;
     void* part = nullptr;
     const int slab = 4 * (lanes > 0 ? lanes : 4);
     const size_t pb = spmm_vrow_scratch_bytes(v, nk);
-    if (pb && cudaMalloc(&part, pb) != cudaSuccess) {
-      vrow_free(&v);
+    if (pb && cudaMallocAsync(&part, pb, s) != cudaSuccess) {
+      vrow_free(&v, s);
       return set_error(FGB_ENOMEM, "fgb_spmm: partial sums (%zu bytes)", pb);
     }
     rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0, slab, part, s,
                    variant == 3);
-    cudaError_t e = cudaStreamSynchronize(s);  // before the schedule is freed
-    cudaFree(part);
-    vrow_free(&v);
-    if (rc == FGB_OK && e != cudaSuccess) rc = set_error(FGB_ECUDA, "fgb_spmm: %s", cudaGetErrorString(e));
+    if (part) cudaFreeAsync(part, s);
+    vrow_free(&v, s);
     return rc;
   }
   if (dtype == FGB_F32) {

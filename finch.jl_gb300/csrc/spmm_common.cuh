@@ -32,9 +32,14 @@ struct VrowSchedule {
                            // slot (-1: writes C)
   int64_t* part_row = nullptr;  // per partial slot: its row (slots of a row in order)
   void* mem = nullptr;
+  bool pooled = false;  // mem from the stream-ordered pool (a schedule for one call)
 };
-int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s);
-void vrow_free(VrowSchedule* v);
+// pooled: allocate the schedule from the stream-ordered pool, to be freed by
+// vrow_free on a stream (a schedule built for one call); else cudaMalloc
+// (a plan's).  Stream-ordered: the schedule is ready for launches on s.
+int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s,
+               bool pooled = false);
+void vrow_free(VrowSchedule* v, cudaStream_t s = nullptr);
 // partial: the long rows' partial sums (spmm_vrow_scratch_bytes).
 size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk);
 // slab: 8, 16 or 32 columns per launch.  async_gather: gathers staged in

@@ -306,32 +306,43 @@ __global__ void vrow_fixup_k(int64_t nl, int64_t nk, const int64_t* __restrict__
 static inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 template <class PtrT>
-static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s) {
+static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s,
+                        bool pooled) {
   const int64_t nrows = A->nrows;
   const PtrT* ptr = (const PtrT*)A->ptr;
   const int grid = grid_for(nrows, 256, ctx->num_sms);
+  // Temporaries come from the stream-ordered pool (kept mapped across calls);
+  // the schedule itself too when `pooled` (a schedule built for one call).
   int64_t *cnt_v = nullptr, *cnt_l = nullptr, *voff = nullptr, *loff = nullptr;
   void* cub_tmp = nullptr;
+  char* tmp = nullptr;
+  char* mem = nullptr;
   size_t cub_bytes = 0, b2 = 0;
   cudaError_t e = cudaSuccess;
+  auto release = [&](bool keep_schedule) {
+    for (void* q : {(void*)cnt_v, (void*)cnt_l, (void*)voff, (void*)loff, cub_tmp, (void*)tmp})
+      if (q) cudaFreeAsync(q, s);
+    if (!keep_schedule && mem) {
+      if (pooled) cudaFreeAsync(mem, s);
+      else cudaFree(mem);
+      *out = VrowSchedule{};
+    }
+  };
   auto fail = [&](const char* what) {
-    cudaFree(cnt_v);
-    cudaFree(cnt_l);
-    cudaFree(voff);
-    cudaFree(loff);
-    cudaFree(cub_tmp);
+    release(false);
     return set_error(e == cudaErrorMemoryAllocation ? FGB_ENOMEM : FGB_ECUDA, "vrow schedule: %s: %s",
                      what, cudaGetErrorString(e));
   };
-  if ((e = cudaMalloc(&cnt_v, sizeof(int64_t) * (nrows + 1))) != cudaSuccess) return fail("alloc");
-  if ((e = cudaMalloc(&cnt_l, sizeof(int64_t) * (nrows + 1))) != cudaSuccess) return fail("alloc");
-  if ((e = cudaMalloc(&voff, sizeof(int64_t) * (nrows + 1))) != cudaSuccess) return fail("alloc");
-  if ((e = cudaMalloc(&loff, sizeof(int64_t) * (nrows + 1))) != cudaSuccess) return fail("alloc");
+  const size_t rows_bytes = sizeof(int64_t) * (nrows + 1);
+  if ((e = cudaMallocAsync((void**)&cnt_v, rows_bytes, s)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMallocAsync((void**)&cnt_l, rows_bytes, s)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMallocAsync((void**)&voff, rows_bytes, s)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMallocAsync((void**)&loff, rows_bytes, s)) != cudaSuccess) return fail("alloc");
   cudaMemsetAsync(cnt_v + nrows, 0, sizeof(int64_t), s);
   cudaMemsetAsync(cnt_l + nrows, 0, sizeof(int64_t), s);
   vrow_count_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, T, cnt_v, cnt_l);
   cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, cnt_v, voff, nrows + 1, s);
-  if ((e = cudaMalloc(&cub_tmp, cub_bytes)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMallocAsync(&cub_tmp, cub_bytes, s)) != cudaSuccess) return fail("alloc");
   if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt_v, voff, nrows + 1, s)) != cudaSuccess)
     return fail("scan");
   if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt_l, loff, nrows + 1, s)) != cudaSuccess)
@@ -342,31 +353,22 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail("count");
   const int64_t nv = tot[0], nl = tot[1];
   if (nv > INT32_MAX || nl > INT32_MAX) {
-    e = cudaSuccess;
-    cudaFree(cnt_v);
-    cudaFree(cnt_l);
-    cudaFree(voff);
-    cudaFree(loff);
-    cudaFree(cub_tmp);
+    release(false);
     return set_error(FGB_EUNSUPPORTED, "vrow schedule: too many virtual rows");
   }
-  // persistent: the sorted records and part_row; temporary: keys, order, unsorted records
+  // the schedule: sorted records and part_row; temporaries: keys, order, unsorted records
   const size_t keep = a256(16 * nv) + a256(8 * (nl > 0 ? nl : 1));
-  char* mem = nullptr;
-  if ((e = cudaMalloc(&mem, keep)) != cudaSuccess) return fail("alloc");
+  e = pooled ? cudaMallocAsync((void**)&mem, keep, s) : cudaMalloc((void**)&mem, keep);
+  if (e != cudaSuccess) return fail("alloc");
   out->vr = (int4*)mem;
   out->part_row = (int64_t*)(mem + a256(16 * nv));
   out->mem = mem;
+  out->pooled = pooled;
   out->nv = nv;
   out->nl = nl;
   out->T = T;
-  char* tmp = nullptr;
   const size_t tmp_bytes = a256(nv) * 2 + a256(4 * nv) * 2 + a256(16 * nv);
-  if ((e = cudaMalloc(&tmp, tmp_bytes)) != cudaSuccess) {
-    cudaFree(mem);
-    out->mem = nullptr;
-    return fail("alloc");
-  }
+  if ((e = cudaMallocAsync((void**)&tmp, tmp_bytes, s)) != cudaSuccess) return fail("alloc");
   uint8_t* key = (uint8_t*)tmp;
   uint8_t* key2 = (uint8_t*)(tmp + a256(nv));
   int32_t* ord = (int32_t*)(tmp + 2 * a256(nv));
@@ -377,47 +379,36 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   b2 = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, 4, s);
   if (b2 > cub_bytes) {
-    cudaFree(cub_tmp);
+    cudaFreeAsync(cub_tmp, s);
     cub_tmp = nullptr;
-    if ((e = cudaMalloc(&cub_tmp, b2)) != cudaSuccess) {
-      cudaFree(tmp);
-      cudaFree(mem);
-      out->mem = nullptr;
-      return fail("alloc");
-    }
+    if ((e = cudaMallocAsync(&cub_tmp, b2, s)) != cudaSuccess) return fail("alloc");
     cub_bytes = b2;
   }
   e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, key, key2, ord, ord2, (int)nv, 0, 4, s);
   if (e == cudaSuccess) {
     vrow_gather_k<<<grid_for(nv, 256, ctx->num_sms), 256, 0, s>>>(nv, ord2, unsorted, out->vr);
-    e = cudaStreamSynchronize(s);
+    e = cudaGetLastError();
   }
-  cudaFree(tmp);
-  if (e != cudaSuccess) {
-    cudaFree(mem);
-    out->mem = nullptr;
-    return fail("sort");
-  }
-  cudaFree(cnt_v);
-  cudaFree(cnt_l);
-  cudaFree(voff);
-  cudaFree(loff);
-  cudaFree(cub_tmp);
+  if (e != cudaSuccess) return fail("sort");
+  release(true);  // stream-ordered: the schedule is ready for the next launch on s
   return FGB_OK;
 }
 
-int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s) {
+int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s, bool pooled) {
   *out = VrowSchedule{};
   if (A->orient != FGB_CSR) return set_error(FGB_EUNSUPPORTED, "vrow schedule: CSR only");
   if (T < 8 || T > 4096) return set_error(FGB_EINVAL, "vrow schedule: chunk %d outside [8, 4096]", T);
   if (A->nrows > INT32_MAX || A->nnz > INT32_MAX)
     return set_error(FGB_EUNSUPPORTED, "vrow schedule: needs fewer than 2^31 rows and entries");
-  return A->ptr_t == FGB_I32 ? vrow_build_t<int32_t>(ctx, A, T, out, s)
-                             : vrow_build_t<int64_t>(ctx, A, T, out, s);
+  return A->ptr_t == FGB_I32 ? vrow_build_t<int32_t>(ctx, A, T, out, s, pooled)
+                             : vrow_build_t<int64_t>(ctx, A, T, out, s, pooled);
 }
 
-void vrow_free(VrowSchedule* v) {
-  if (v && v->mem) cudaFree(v->mem);
+void vrow_free(VrowSchedule* v, cudaStream_t s) {
+  if (v && v->mem) {
+    if (v->pooled) cudaFreeAsync(v->mem, s);
+    else cudaFree(v->mem);
+  }
   if (v) *v = VrowSchedule{};
 }
 
