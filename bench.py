@@ -566,7 +566,8 @@ def suite_sddmm() -> list[dict]:
     nbytes = 4 * (m + 1) + 8 * A.nnz + 2 * 4 * m * 64 + 4 * A.nnz
     from finchgb.plan import Plan
 
-    schedules = {"one_pass_default": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd, slab=0), reps=10),
+    schedules = {"library_default_per_call": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd), reps=10),
+                 "one_pass_default": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd, slab=0), reps=10),
                  "slab32_lanes8": _timed_ms(lambda: dev.sddmm(Ad, Xd, Yd, outd, lanes=8, slab=32),
                                             reps=10)}
     plan = Plan.sddmm(Ad, Xd, Yd, outd, tune_reps=3)

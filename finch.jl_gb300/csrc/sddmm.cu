@@ -246,16 +246,35 @@ int sddmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx, co
 
 }  // namespace fgb
 
+namespace fgb {
+// No schedule given: a Y far larger than L2 with many stored entries takes the
+// virtual rows with cp.async gathers in 32-column slabs, built for the call
+// (the plan autotuner's choice for the 1M x 1M Zipf matrix with k = 64).
+static bool sddmm_default_vrow(const fgb_sparse* A, const void* X, int64_t ldx, const void* Y, int64_t ldy,
+                               int64_t k, int dtype, unsigned flags) {
+  return A && A->orient == FGB_CSR && A->val_t == FGB_F32 && A->idx_t == FGB_I32 && dtype == FGB_F32 &&
+         !(flags & FGB_FINCH_ORDER) && k > 0 && k <= 128 && k % 4 == 0 && ldx % 4 == 0 && ldy % 4 == 0 &&
+         ldy <= INT32_MAX && (uintptr_t)X % 16 == 0 && (uintptr_t)Y % 16 == 0 && A->nrows <= INT32_MAX &&
+         A->nnz >= (1 << 20) && A->nnz <= INT32_MAX && (double)A->ncols * (double)k * 4.0 > 64.0 * 1024 * 1024;
+}
+}  // namespace fgb
+
 extern "C" int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
                          const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                          unsigned flags, void* stream) {
+  if (fgb::sddmm_default_vrow(A, X, ldx, Y, ldy, k, dtype, flags)) {
+    const fgb_sddmm_tuning t{0, 2, 256, k > 32 ? 32 : 0};
+    return fgb_sddmm_ex(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, &t, stream);
+  }
   return fgb::sddmm_impl(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, 0, 0, stream, -1);
 }
 
 extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
                             const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                             unsigned flags, const fgb_sddmm_tuning* tune, void* stream) {
-  const int lanes = tune ? tune->lanes : 0;
+  if (!tune || (tune->lanes == 0 && tune->variant == 0 && tune->chunk == 0 && tune->slab == -1))
+    return fgb_sddmm(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, stream);  // no schedule given
+  const int lanes = tune->lanes;
   if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: lanes must be 0, 4, 8, 16 or 32");
   if (tune && (tune->chunk < 0 || tune->slab < -1))

@@ -283,7 +283,8 @@ FGB_API int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t 
  * length, holding the row's slice of X in registers; `slab` > 0 (a multiple
  * of 4) cuts k into launches of that many columns.  variant 2: variant 1
  * with the gathers of Y staged in shared memory by cp.async (identical
- * results).  Zero lanes/chunk take the defaults. */
+ * results).  Zero lanes/chunk take the defaults; NULL, or all fields at their
+ * defaults (0, 0, 0, -1), is fgb_sddmm: the library picks the schedule. */
 typedef struct fgb_sddmm_tuning {
   int32_t lanes;
   int32_t variant;
