@@ -260,12 +260,14 @@ def run_gpu(args):
     slabs = -(-NK // (4 * plan_lanes))
     if plan is None and lanes == 0 and path == 0 and variant == 0:
         variant = 3  # the library's default for a B far larger than L2
-    if plan is None and variant in (2, 3):  # schedule built per call: counted as its kernels
-        launches_per_step = 10 + slabs
+    if plan is None and variant in (2, 3):
+        # schedule built per call: count, 5 scans (2 kernels each), fill, a
+        # 3-kernel radix sort and the gather, then the slabs and 2 fix-up passes
+        launches_per_step = 16 + slabs + 2
     elif plan is None:
         launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
-    elif variant in (2, 3):  # one launch per column slab + the partial-sum fix-up
-        launches_per_step = slabs + 1
+    elif variant in (2, 3):  # one launch per column slab + the two partial-sum fix-up passes
+        launches_per_step = slabs + 2
     else:  # per panel: the slab launches + fix-up (item boundaries precomputed)
         launches_per_step = npanels * (slabs + 1)
 
@@ -418,8 +420,8 @@ def run_gpu(args):
                         "unit": "GB/s", "frac": round(achieved / peak, 4),
                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": traffic, "traffic_source": traffic_src,
-                        "kernel": (f"spmm_vrow_k x{slabs} column slabs + vrow_fixup_k" if variant == 2 else
-                                   f"spmm_vrow_async_k x{slabs} column slabs + vrow_fixup_k" if variant == 3 else
+                        "kernel": (f"spmm_vrow_k x{slabs} column slabs + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 2 else
+                                   f"spmm_vrow_async_k x{slabs} column slabs + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 3 else
                                    f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
                                    if plan is not None and npanels > 1 else
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),

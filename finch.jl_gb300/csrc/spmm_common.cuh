@@ -30,7 +30,13 @@ struct VrowSchedule {
   int T = 0;
   int4* vr = nullptr;      // per virtual row (sorted): row, first entry, length, partial
                            // slot (-1: writes C)
-  int64_t* part_row = nullptr;  // per partial slot: its row (slots of a row in order)
+  // fix-up of the partial sums: segments of at most 16 slots of one row
+  // {row, first slot, slots, segment-sum slot (-1: add to C directly)}, and the
+  // long rows {row, first segment-sum slot, segments, 0} whose segment sums a
+  // second pass adds to C in order
+  int64_t nseg = 0, nlong = 0, nss = 0;
+  int4* seg = nullptr;
+  int4* lrow = nullptr;
   void* mem = nullptr;
   bool pooled = false;  // mem from the stream-ordered pool (a schedule for one call)
 };

@@ -28,16 +28,27 @@ namespace fgb {
 
 constexpr int VR_BATCH = 8;
 constexpr int VR_THREADS = 256;
+constexpr int VR_SEG = 16;  // partial-sum slots per fix-up segment
 
+// Per row: virtual rows, partial-sum slots, fix-up segments (a row's slots in
+// runs of at most VR_SEG), whether it is a long row (more than one segment:
+// its segment sums are combined by a second pass) and its segment sums.
 template <class PtrT>
 __global__ void vrow_count_k(int64_t nrows, const PtrT* __restrict__ ptr, int T,
-                             int64_t* __restrict__ nv, int64_t* __restrict__ nl) {
+                             int64_t* __restrict__ nv, int64_t* __restrict__ nl,
+                             int64_t* __restrict__ nseg, int64_t* __restrict__ nlong,
+                             int64_t* __restrict__ nss) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
        r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t len = ld_ptr(ptr, r + 1) - ld_ptr(ptr, r);
     const int64_t nch = len <= T ? 1 : (len + T - 1) / T;
+    const int64_t slots = nch - 1;
+    const int64_t segs = (slots + VR_SEG - 1) / VR_SEG;
     nv[r] = nch;
-    nl[r] = nch - 1;
+    nl[r] = slots;
+    nseg[r] = segs;
+    nlong[r] = segs > 1 ? 1 : 0;
+    nss[r] = segs > 1 ? segs : 0;
   }
 }
 
@@ -47,11 +58,16 @@ __device__ __forceinline__ uint8_t vrow_class(int64_t len) {
   return (uint8_t)(15 - b);
 }
 
+// The virtual rows of every row (unsorted, with their length-class keys) and
+// its fix-up records.  soff/goff/ssoff: exclusive scans of the segments, the
+// long rows and the segment sums (vrow_count_k).
 template <class PtrT>
 __global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int base, int T,
                             const int64_t* __restrict__ voff, const int64_t* __restrict__ loff,
-                            uint8_t* __restrict__ key, int32_t* __restrict__ ord,
-                            int4* __restrict__ unsorted, int64_t* __restrict__ part_row) {
+                            const int64_t* __restrict__ soff, const int64_t* __restrict__ goff,
+                            const int64_t* __restrict__ ssoff, uint8_t* __restrict__ key,
+                            int32_t* __restrict__ ord, int4* __restrict__ unsorted,
+                            int4* __restrict__ seg, int4* __restrict__ lrow) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
        r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b0 = ld_ptr(ptr, r) - base;
@@ -64,7 +80,18 @@ __global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int bas
       key[v] = vrow_class(clen);
       ord[v] = (int32_t)v;
       unsorted[v] = make_int4((int)r, (int)(b0 + c * T), (int)clen, c == 0 ? -1 : (int)(l0 + c - 1));
-      if (c > 0) part_row[l0 + c - 1] = r;
+    }
+    const int64_t slots = nch - 1, s0 = soff[r], segs = soff[r + 1] - s0;
+    if (segs == 1) {
+      seg[s0] = make_int4((int)r, (int)l0, (int)slots, -1);
+    } else if (segs > 1) {
+      const int64_t ss0 = ssoff[r];
+      for (int64_t g = 0; g < segs; ++g) {
+        const int64_t first = g * VR_SEG;
+        const int64_t n = slots - first < VR_SEG ? slots - first : VR_SEG;
+        seg[s0 + g] = make_int4((int)r, (int)(l0 + first), (int)n, (int)(ss0 + g));
+      }
+      lrow[goff[r]] = make_int4((int)r, (int)ss0, (int)segs, 0);
     }
   }
 }
@@ -255,51 +282,65 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
   }
 }
 
-// Adds each long row's partial sums to that row of C: one warp per row (the
-// warp of its first slot), slots summed in order, 4 columns per lane.
-__global__ void vrow_fixup_k(int64_t nl, int64_t nk, const int64_t* __restrict__ part_row,
-                             const float* __restrict__ partial, float* __restrict__ C, int64_t ldc) {
+// Sums `n` partial-sum slots starting at `p` (rows of nk floats) in slot
+// order, 4 columns per lane starting at column c.
+__device__ __forceinline__ float4 vrow_sum_slots(const float* __restrict__ p, int64_t n, int64_t nk) {
+  float4 sum = *reinterpret_cast<const float4*>(p);
+  for (int64_t k0 = 1; k0 < n; k0 += 8) {
+    float4 x[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k0 + u < n) x[u] = *reinterpret_cast<const float4*>(p + (k0 + u) * nk);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k0 + u < n) {
+        sum.x += x[u].x;
+        sum.y += x[u].y;
+        sum.z += x[u].z;
+        sum.w += x[u].w;
+      }
+  }
+  return sum;
+}
+
+__device__ __forceinline__ void vrow_add_row(float* __restrict__ dst, float4 sum) {
+  float4 o = *reinterpret_cast<float4*>(dst);
+  o.x += sum.x;
+  o.y += sum.y;
+  o.z += sum.z;
+  o.w += sum.w;
+  *reinterpret_cast<float4*>(dst) = o;
+}
+
+// Fix-up, pass 1: one warp per segment (at most VR_SEG partial-sum slots of
+// one row, 4 columns per lane), its slots summed in order.  A row with one
+// segment adds the sum to C; a long row's segments leave their sums in
+// `segsum` for pass 2.  A long row's slots are thus summed by many warps at
+// once instead of one warp walking all of them.
+__global__ void vrow_fixup_seg_k(int64_t nseg, int64_t nk, const int4* __restrict__ seg,
+                                 const float* __restrict__ partial, float* __restrict__ segsum,
+                                 float* __restrict__ C, int64_t ldc) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nl; w += nwarps) {
-    const int64_t r = part_row[w];
-    if (w > 0 && part_row[w - 1] == r) continue;  // not the row's first slot
-    int64_t n = 1;  // the row's slots: [w, w + n)
-    while (true) {
-      const int64_t q = w + n + lane;
-      const unsigned m = __ballot_sync(0xffffffffu, q < nl && part_row[q] == r);
-      if (m == 0xffffffffu) {
-        n += 32;
-        continue;
-      }
-      n += __ffs(~m) - 1;
-      break;
-    }
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nseg; w += nwarps) {
+    const int4 rec = seg[w];  // row, first slot, slots, segment-sum slot (-1: C)
     for (int64_t c = (int64_t)lane * 4; c < nk; c += 128) {
-      const float* p = partial + w * nk + c;
-      float4 sum = *reinterpret_cast<const float4*>(p);
-      for (int64_t k0 = 1; k0 < n; k0 += 8) {
-        float4 x[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if (k0 + u < n) x[u] = *reinterpret_cast<const float4*>(p + (k0 + u) * nk);
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if (k0 + u < n) {
-            sum.x += x[u].x;
-            sum.y += x[u].y;
-            sum.z += x[u].z;
-            sum.w += x[u].w;
-          }
-      }
-      float4* dst = reinterpret_cast<float4*>(C + r * ldc + c);
-      float4 o = *dst;
-      o.x += sum.x;
-      o.y += sum.y;
-      o.z += sum.z;
-      o.w += sum.w;
-      *dst = o;
+      const float4 sum = vrow_sum_slots(partial + (int64_t)rec.y * nk + c, rec.z, nk);
+      if (rec.w < 0) vrow_add_row(C + (int64_t)rec.x * ldc + c, sum);
+      else *reinterpret_cast<float4*>(segsum + (int64_t)rec.w * nk + c) = sum;
     }
+  }
+}
+
+// Fix-up, pass 2: one warp per long row, its segment sums added in order to C.
+__global__ void vrow_fixup_rows_k(int64_t nlong, int64_t nk, const int4* __restrict__ lrow,
+                                  const float* __restrict__ segsum, float* __restrict__ C, int64_t ldc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nlong; w += nwarps) {
+    const int4 rec = lrow[w];  // row, first segment sum, segments
+    for (int64_t c = (int64_t)lane * 4; c < nk; c += 128)
+      vrow_add_row(C + (int64_t)rec.x * ldc + c, vrow_sum_slots(segsum + (int64_t)rec.y * nk + c, rec.z, nk));
   }
 }
 
@@ -314,13 +355,16 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   // Temporaries come from the stream-ordered pool (kept mapped across calls);
   // the schedule itself too when `pooled` (a schedule built for one call).
   int64_t *cnt_v = nullptr, *cnt_l = nullptr, *voff = nullptr, *loff = nullptr;
+  int64_t *cnt_s = nullptr, *cnt_g = nullptr, *cnt_ss = nullptr, *soff = nullptr, *goff = nullptr,
+          *ssoff = nullptr;
   void* cub_tmp = nullptr;
   char* tmp = nullptr;
   char* mem = nullptr;
   size_t cub_bytes = 0, b2 = 0;
   cudaError_t e = cudaSuccess;
   auto release = [&](bool keep_schedule) {
-    for (void* q : {(void*)cnt_v, (void*)cnt_l, (void*)voff, (void*)loff, cub_tmp, (void*)tmp})
+    for (void* q : {(void*)cnt_v, (void*)cnt_l, (void*)voff, (void*)loff, (void*)cnt_s, (void*)cnt_g,
+                    (void*)cnt_ss, (void*)soff, (void*)goff, (void*)ssoff, cub_tmp, (void*)tmp})
       if (q) cudaFreeAsync(q, s);
     if (!keep_schedule && mem) {
       if (pooled) cudaFreeAsync(mem, s);
@@ -338,30 +382,38 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   if ((e = cudaMallocAsync((void**)&cnt_l, rows_bytes, s)) != cudaSuccess) return fail("alloc");
   if ((e = cudaMallocAsync((void**)&voff, rows_bytes, s)) != cudaSuccess) return fail("alloc");
   if ((e = cudaMallocAsync((void**)&loff, rows_bytes, s)) != cudaSuccess) return fail("alloc");
-  cudaMemsetAsync(cnt_v + nrows, 0, sizeof(int64_t), s);
-  cudaMemsetAsync(cnt_l + nrows, 0, sizeof(int64_t), s);
-  vrow_count_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, T, cnt_v, cnt_l);
+  for (int64_t** q : {&cnt_s, &cnt_g, &cnt_ss, &soff, &goff, &ssoff})
+    if ((e = cudaMallocAsync((void**)q, rows_bytes, s)) != cudaSuccess) return fail("alloc");
+  for (int64_t* q : {cnt_v, cnt_l, cnt_s, cnt_g, cnt_ss}) cudaMemsetAsync(q + nrows, 0, sizeof(int64_t), s);
+  vrow_count_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, T, cnt_v, cnt_l, cnt_s, cnt_g, cnt_ss);
   cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, cnt_v, voff, nrows + 1, s);
   if ((e = cudaMallocAsync(&cub_tmp, cub_bytes, s)) != cudaSuccess) return fail("alloc");
   if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt_v, voff, nrows + 1, s)) != cudaSuccess)
     return fail("scan");
-  if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt_l, loff, nrows + 1, s)) != cudaSuccess)
-    return fail("scan");
-  int64_t tot[2] = {0, 0};
-  cudaMemcpyAsync(&tot[0], voff + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(&tot[1], loff + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  const int64_t* cnts[5] = {cnt_v, cnt_l, cnt_s, cnt_g, cnt_ss};
+  int64_t* offs[5] = {voff, loff, soff, goff, ssoff};
+  for (int q = 1; q < 5; ++q)
+    if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnts[q], offs[q], nrows + 1, s)) != cudaSuccess)
+      return fail("scan");
+  int64_t tot[5] = {0, 0, 0, 0, 0};
+  for (int q = 0; q < 5; ++q)
+    cudaMemcpyAsync(&tot[q], offs[q] + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail("count");
-  const int64_t nv = tot[0], nl = tot[1];
+  const int64_t nv = tot[0], nl = tot[1], nseg = tot[2], nlong = tot[3], nss = tot[4];
   if (nv > INT32_MAX || nl > INT32_MAX) {
     release(false);
     return set_error(FGB_EUNSUPPORTED, "vrow schedule: too many virtual rows");
   }
-  // the schedule: sorted records and part_row; temporaries: keys, order, unsorted records
-  const size_t keep = a256(16 * nv) + a256(8 * (nl > 0 ? nl : 1));
+  // the schedule: sorted records and fix-up records; temporaries: keys, order, unsorted records
+  const size_t keep = a256(16 * nv) + a256(16 * (nseg > 0 ? nseg : 1)) + a256(16 * (nlong > 0 ? nlong : 1));
   e = pooled ? cudaMallocAsync((void**)&mem, keep, s) : cudaMalloc((void**)&mem, keep);
   if (e != cudaSuccess) return fail("alloc");
   out->vr = (int4*)mem;
-  out->part_row = (int64_t*)(mem + a256(16 * nv));
+  out->seg = (int4*)(mem + a256(16 * nv));
+  out->lrow = (int4*)(mem + a256(16 * nv) + a256(16 * (nseg > 0 ? nseg : 1)));
+  out->nseg = nseg;
+  out->nlong = nlong;
+  out->nss = nss;
   out->mem = mem;
   out->pooled = pooled;
   out->nv = nv;
@@ -374,8 +426,8 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   int32_t* ord = (int32_t*)(tmp + 2 * a256(nv));
   int32_t* ord2 = (int32_t*)(tmp + 2 * a256(nv) + a256(4 * nv));
   int4* unsorted = (int4*)(tmp + 2 * a256(nv) + 2 * a256(4 * nv));
-  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, A->index_base, T, voff, loff, key, ord, unsorted,
-                                         out->part_row);
+  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, A->index_base, T, voff, loff, soff, goff, ssoff, key, ord,
+                                         unsorted, out->seg, out->lrow);
   b2 = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, 4, s);
   if (b2 > cub_bytes) {
@@ -437,15 +489,20 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
     kern<<<grid, VR_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val, B, (LdT)ldb, C,
                                         ldc, c0, nk, A->index_base, accumulate, partial);
-  if (v.nl > 0)
-    vrow_fixup_k<<<grid_for(v.nl * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nl, nk, v.part_row, partial,
-                                                                         C, ldc);
+  if (v.nseg > 0) {  // segment sums live after the nl partial-sum slots
+    float* segsum = partial + (int64_t)v.nl * nk;
+    vrow_fixup_seg_k<<<grid_for(v.nseg * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nseg, nk, v.seg, partial,
+                                                                            segsum, C, ldc);
+    if (v.nlong > 0)
+      vrow_fixup_rows_k<<<grid_for(v.nlong * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nlong, nk, v.lrow, segsum,
+                                                                                 C, ldc);
+  }
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
 }
 
 size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk) {
-  return sizeof(float) * (size_t)(v.nl > 0 ? v.nl : 0) * (size_t)nk;
+  return sizeof(float) * (size_t)(v.nl + v.nss) * (size_t)nk;  // partial sums, then segment sums
 }
 
 int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
