@@ -882,19 +882,44 @@ def run_serve(args):
         op = ("spmv", "spmm", "masked_mul")[int(rng.integers(3))]
         k = int(rng.integers(len(partners) if op == "masked_mul" else len(mats)))
         plan.append((op, k, 32 if op == "spmm" else 0))
-    window = 1024
+    # compulsory bytes per request: the matrix once (ptr int32, idx int32,
+    # val fp32; the partner too for a masked multiply), the input read once
+    # and the output written once -- inputs and outputs live in page-locked
+    # host memory, so they also cross the host link
+    def req_bytes(op, k, nk):
+        A = mats[k]
+        mat = 4 * (A.nrows + 1) + 8 * A.nnz
+        if op == "masked_mul":  # A .* partner, written on A's pattern
+            P = partners[k]
+            return mat + 4 * (P.nrows + 1) + 8 * P.nnz + 4 * A.nnz, 4 * A.nnz
+        io = 4 * (A.ncols + A.nrows) * max(nk, 1)
+        return mat + io, io
+
+    rb = [req_bytes(*r) for r in plan]
+    total_bytes = float(sum(b for b, _ in rb))
+    link_bytes = float(sum(l for _, l in rb))
+    # the closed loop measures capacity: as many requests in flight as the
+    # server has slots (4,096).  With 1,024 the loop was latency-bound at
+    # 256 K requests/s; 2,048 gave 330 K, 4,096 about 345 K.
+    window = 4096
     arena = torch.empty(512 << 20, dtype=torch.float32).pin_memory()  # 2 GiB ring
     torch.cuda.synchronize()
     out = {"suite": "served_4096_csr", "requests": n_req, "mix": "1/3 SpMV, 1/3 SpMM(32), 1/3 masked multiply",
+           "closed_loop_in_flight": window,
            "matrices": len(mats), "stored_entries": int(sum(A.nnz for A in mats)),
            "config": {"workload": "4096 CSR, rows log-uniform [64, 8192], density U[0.5%, 5%], FP32"}}
     # closed loop (saturation): up to `window` requests in flight
     for mode in ("batched", "per_call"):
         dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
         out[mode] = {"ops_per_s": round(n_req / dt, 1), "seconds": round(dt, 3),
+                     "compulsory_gbps": round(total_bytes / dt / 1e9, 1),
+                     "host_link_gbps": round(link_bytes / dt / 1e9, 1),
                      "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
                      "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
                      "launches": st["launches"], "batches": st["batches_published"],
+                     "dispatcher_ms": {k: round(st[k] / 1e6, 2) for k in
+                                       ("admit_ns", "scan_ns", "finish_ns", "queue_ns", "service_ns")
+                                       if k in st},
                      "client_submit_s": st["client_submit_s"], "client_wait_s": st["client_wait_s"]}
     out["throughput_ratio_batched_vs_per_call"] = round(
         out["batched"]["ops_per_s"] / out["per_call"]["ops_per_s"], 2)
