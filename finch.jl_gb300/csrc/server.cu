@@ -49,6 +49,11 @@ constexpr int64_t SRV_ITEM_CAP = int64_t(1) << 20;
 constexpr int SRV_MAX_MATRICES = 1 << 16;
 constexpr int SRV_THREADS = 256;
 constexpr int SRV_MAX_TAKE = 8;  // work items one claim may take
+// Completion ring: the device appends one record per finished request; at most
+// SRV_MAX_SLOTS records are unconsumed (a slot completes again only after the
+// host has taken its previous record and re-admitted it), so twice that never
+// overwrites one the host has not read.
+constexpr int SRV_DONE_CAP = 2 * SRV_MAX_SLOTS;
 
 struct __align__(16) DevMatrix {
   const int32_t* ptr;
@@ -86,7 +91,10 @@ struct HostShared {           // pinned, mapped into the device address space
   volatile uint64_t published;  // items published so far (host writes)
   volatile uint32_t stop;       // host asks the device loop to exit
   volatile uint32_t error;
-  volatile uint64_t status[SRV_MAX_SLOTS];  // seq of the last completed request per slot
+  // completion records, written in claim order by the device: bits 0-11 the
+  // slot, 12-43 the low 32 bits of the request's sequence number, 44-63 the
+  // ring lap + 1 (mod 2^20) of the position, so the host knows an entry is new
+  volatile uint64_t done_ring[SRV_DONE_CAP];
 };
 
 struct SrvArgs {
@@ -97,6 +105,7 @@ struct SrvArgs {
   unsigned long long* next_item;    // device counter
   unsigned int* done_items;         // per slot
   unsigned int* exit_epoch;         // device word: the last launch told to exit
+  unsigned long long* done_count;   // device counter: completion records written
   unsigned int epoch;               // this launch
   uint64_t idle_ns;
 };
@@ -279,8 +288,11 @@ __global__ void __launch_bounds__(SRV_THREADS, 5) serve_loop_k(SrvArgs a) {
           // re-arm the slot's counter before the host can see the request done
           // (and hand the slot to the next request)
           a.done_items[it.slot] = 0u;
+          const unsigned long long pos = atomicAdd(a.done_count, 1ull);
+          const uint64_t lap = ((uint64_t)(pos / SRV_DONE_CAP) + 1u) & 0xFFFFFull;
+          const uint64_t rec = (lap << 44) | ((uint64_t)(uint32_t)s.seq << 12) | (uint64_t)it.slot;
           __threadfence_system();
-          st_release_sys(&a.host->status[it.slot], s.seq);
+          st_release_sys(&a.host->done_ring[pos % SRV_DONE_CAP], rec);
         }
       }
     }
@@ -461,8 +473,14 @@ struct fgb_server {
     uint64_t id, seq, item0;
     int slot;
   };
-  std::vector<Inflight> inflight;  // admitted, not yet complete (admission order); worker only
+  // admitted requests in admission order (worker only); an entry is complete
+  // once slot_done_seq[slot] has reached its seq, and leaves from the front
+  std::deque<Inflight> inflight;
+  size_t n_inflight = 0;             // admitted, not yet complete
+  std::vector<uint64_t> slot_done_seq;
+  uint64_t done_cursor = 0;          // completion records consumed
   std::vector<uint64_t> done_scratch;
+  std::vector<uint64_t> done_recs;
   uint64_t next_ticket = 1;
   uint64_t published = 0;
   PoolAllocator* alloc = nullptr;
@@ -498,6 +516,7 @@ SrvArgs make_args(fgb_server* s) {
   a.next_item = s->d_next;
   a.done_items = s->d_done;
   a.exit_epoch = (unsigned*)(s->d_next + 2);
+  a.done_count = s->d_next + 3;
   a.epoch = s->loop_epoch;
   a.idle_ns = (uint64_t)s->cfg.idle_exit_us * 1000ull;
   return a;
@@ -565,8 +584,9 @@ void worker_main(fgb_server* s) {
     // A) admission: FIFO while a slot and pool memory are available
     std::vector<uint64_t> admitted;
     // ring positions still owned by in-flight requests start at the oldest one
-    uint64_t ring_tail = s->published;
-    for (const auto& f : s->inflight) ring_tail = std::min(ring_tail, f.item0);
+    while (!s->inflight.empty() && s->slot_done_seq[s->inflight.front().slot] >= s->inflight.front().seq)
+      s->inflight.pop_front();  // complete: its items no longer hold the ring
+    const uint64_t ring_tail = s->inflight.empty() ? s->published : s->inflight.front().item0;
     int64_t new_items = 0;
     while (!s->queue.empty() && s->worker_error == FGB_OK) {
       Ticket& t = s->tickets[s->queue.front()];
@@ -645,12 +665,13 @@ void worker_main(fgb_server* s) {
       for (uint64_t id : admitted) {
         const Ticket& t = s->tickets[id];
         s->inflight.push_back({id, t.seq, t.item0, t.slot});
+        ++s->n_inflight;
       }
       s->stats.batches_published++;
     }
     s->stats.admit_ns += ns_since(t_admit);
     // B) keep the device loop running while work is outstanding
-    if (s->cfg.mode == FGB_SERVE_BATCHED && !s->inflight.empty()) {
+    if (s->cfg.mode == FGB_SERVE_BATCHED && s->n_inflight > 0) {
       const bool running = s->kernel_launched && cudaEventQuery(s->kernel_done) == cudaErrorNotReady;
       if (!running) {
         cudaGetLastError();
@@ -664,23 +685,36 @@ void worker_main(fgb_server* s) {
         s->stats.launches++;
       }
     }
-    // C) completions: the status words are scanned without the lock (the
-    // in-flight list belongs to this thread, and submitters and waiters must
-    // not queue behind the scan); copies back and releases take it again
-    if (!s->inflight.empty()) {
+    // C) completions: new records of the completion ring are read without the
+    // lock (the cursor belongs to this thread, and submitters and waiters
+    // must not queue behind it); copies back and releases take it again
+    if (s->n_inflight > 0) {
       lk.unlock();
       const auto t_scan = clk::now();
-      std::vector<uint64_t>& done = s->done_scratch;
-      done.clear();
-      size_t keep = 0;
-      for (size_t k = 0; k < s->inflight.size(); ++k) {
-        const auto f = s->inflight[k];
-        if (s->host->status[f.slot] == f.seq) done.push_back(f.id); else s->inflight[keep++] = f;
+      std::vector<uint64_t>& recs = s->done_recs;
+      recs.clear();
+      while (true) {
+        const uint64_t want = ((s->done_cursor / SRV_DONE_CAP) + 1u) & 0xFFFFFull;
+        const uint64_t rec = s->host->done_ring[s->done_cursor % SRV_DONE_CAP];
+        if ((rec >> 44) != want) break;
+        recs.push_back(rec);
+        ++s->done_cursor;
       }
-      s->inflight.resize(keep);
       const uint64_t scan_ns = ns_since(t_scan);
       lk.lock();
       s->stats.scan_ns += scan_ns;
+      std::vector<uint64_t>& done = s->done_scratch;
+      done.clear();
+      for (uint64_t rec : recs) {
+        const int slot = (int)(rec & 0xFFFull);
+        const uint64_t id = s->slot_owner[slot];
+        if (!id) continue;
+        const Ticket& t = s->tickets[id];
+        if ((uint32_t)(rec >> 12) != (uint32_t)t.seq) continue;  // not this admission's record
+        s->slot_done_seq[slot] = t.seq;
+        done.push_back(id);
+      }
+      s->n_inflight -= done.size();
       if (!done.empty()) {
         const auto t_fin = clk::now();
         progressed = true;
@@ -706,7 +740,7 @@ void worker_main(fgb_server* s) {
       }
     }
     if (!progressed) {
-      if (s->queue.empty() && s->inflight.empty())
+      if (s->queue.empty() && s->n_inflight == 0)
         s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
       else {
         lk.unlock();
@@ -778,6 +812,7 @@ int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg_in, fgb_server*
   s->slot_owner.assign(cfg.max_inflight, 0);
   for (int k = cfg.max_inflight - 1; k >= 0; --k) s->free_slots.push_back(k);
   s->slot_seq.assign(cfg.max_inflight, 0);
+  s->slot_done_seq.assign(cfg.max_inflight, 0);
   s->stage_pub.assign(STAGE_CAP, 0);
   s->worker = std::thread(worker_main, s);
   *out = s;
