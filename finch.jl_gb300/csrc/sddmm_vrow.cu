@@ -74,7 +74,9 @@ __device__ __forceinline__ void sv_cp_async16(void* smem, const void* gmem, uint
                : "memory");
 }
 
-template <int L, int NB, int MINB>
+// ALL: every lane's 4 columns lie inside k, so no lane is masked; a full
+// batch (NB entries left) then issues and reduces without per-entry predicates.
+template <int L, int NB, int MINB, bool ALL>
 __global__ void __launch_bounds__(SV_THREADS, MINB) sddmm_vrow_async_k(
     int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx, const float* __restrict__ val,
     const float* __restrict__ X, int64_t ldx, const float* __restrict__ Y, int ldy, int64_t k,
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(SV_THREADS, MINB) sddmm_vrow_async_k(
   const int gid = (int)((blockIdx.x * blockDim.x + threadIdx.x) / L);  // nv < 2^31 (vrow_build)
   const int ngroups = (int)((gridDim.x * blockDim.x) / L);
   const int64_t col = (int64_t)sl * 4;
-  const bool active = col < k;
+  const bool active = ALL || col < k;
   const float* Yc = Y + col;
   float4* slot = sv_stage + threadIdx.x;
   const uint64_t pol_stream = policy_evict_first();
@@ -99,19 +101,31 @@ __global__ void __launch_bounds__(SV_THREADS, MINB) sddmm_vrow_async_k(
       // lane u of the sub-group loads entry t + u's column; the sub-group shares it
       int jm = 0;
       if (sl < NB && t + sl < rec.z) jm = __ldg(idx + rec.y + t + sl) - base;
-#pragma unroll
-      for (int u = 0; u < NB; ++u) {
-        const int j = __shfl_sync(gmask, jm, u, L);
-        if (t + u < rec.z && active) sv_cp_async16(slot + u * SV_THREADS, Yc + (int64_t)j * ldy, pol_keep);
-      }
-      asm volatile("cp.async.wait_all;" ::: "memory");
       float d[NB];
+      if (ALL && t + NB <= rec.z) {  // full batch, no masked lane
 #pragma unroll
-      for (int u = 0; u < NB; ++u) {
-        d[u] = 0.f;
-        if (t + u < rec.z && active) {
+        for (int u = 0; u < NB; ++u)
+          sv_cp_async16(slot + u * SV_THREADS, Yc + (int64_t)__shfl_sync(gmask, jm, u, L) * ldy, pol_keep);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
           const float4 y = slot[u * SV_THREADS];
           d[u] = __fmaf_rn(xr.x, y.x, __fmaf_rn(xr.y, y.y, __fmaf_rn(xr.z, y.z, xr.w * y.w)));
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          const int j = __shfl_sync(gmask, jm, u, L);
+          if (t + u < rec.z && active) sv_cp_async16(slot + u * SV_THREADS, Yc + (int64_t)j * ldy, pol_keep);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          d[u] = 0.f;
+          if (t + u < rec.z && active) {
+            const float4 y = slot[u * SV_THREADS];
+            d[u] = __fmaf_rn(xr.x, y.x, __fmaf_rn(xr.y, y.y, __fmaf_rn(xr.z, y.z, xr.w * y.w)));
+          }
         }
       }
 #pragma unroll
@@ -131,25 +145,34 @@ __global__ void __launch_bounds__(SV_THREADS, MINB) sddmm_vrow_async_k(
   }
 }
 
-template <int L>
-static int launch_sddmm_vrow_async(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* X,
-                                   int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
-                                   int mode, cudaStream_t s) {
+template <int L, bool ALL>
+static int launch_sddmm_vrow_async_t(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* X,
+                                     int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
+                                     int mode, cudaStream_t s) {
   constexpr int NB = L >= 8 ? 8 : L;
   constexpr size_t smem = sizeof(float4) * NB * SV_THREADS;
   static const int occ = [] {  // once per process (one device model); thread-safe
-    cudaFuncSetAttribute(sddmm_vrow_async_k<L, NB, 6>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(sddmm_vrow_async_k<L, NB, 6, ALL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int o = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_async_k<L, NB, 6>, SV_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_async_k<L, NB, 6, ALL>, SV_THREADS, smem);
     return o > 0 ? o : 1;
   }();
   const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
-  sddmm_vrow_async_k<L, NB, 6><<<grid, SV_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx,
-                                                             (const float*)A->val, X, ldx, Y, (int)ldy, k,
-                                                             out, A->index_base, mode);
+  sddmm_vrow_async_k<L, NB, 6, ALL><<<grid, SV_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx,
+                                                                  (const float*)A->val, X, ldx, Y, (int)ldy,
+                                                                  k, out, A->index_base, mode);
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
+}
+
+// The unmasked build when the launch's k fills every lane (k == 4L).
+template <int L>
+static int launch_sddmm_vrow_async(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* X,
+                                   int64_t ldx, const float* Y, int64_t ldy, int64_t k, float* out,
+                                   int mode, cudaStream_t s) {
+  if (k == 4 * L) return launch_sddmm_vrow_async_t<L, true>(ctx, v, A, X, ldx, Y, ldy, k, out, mode, s);
+  return launch_sddmm_vrow_async_t<L, false>(ctx, v, A, X, ldx, Y, ldy, k, out, mode, s);
 }
 
 template <int L>
