@@ -32,6 +32,13 @@ inline cudaStream_t pick_stream(fgb_ctx*, void* s) {
   return s ? static_cast<cudaStream_t>(s) : cudaStreamLegacy;
 }
 
+// True while `s` is being captured into a CUDA graph: paths that synchronise
+// (a schedule built for one call reads its sizes back) are then not taken.
+inline bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
 // Returns FGB_ECUDA with a message if the last launch failed.
 int check_launch(const char* what);
 

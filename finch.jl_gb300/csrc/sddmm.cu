@@ -262,7 +262,8 @@ static bool sddmm_default_vrow(const fgb_sparse* A, const void* X, int64_t ldx, 
 extern "C" int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
                          const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                          unsigned flags, void* stream) {
-  if (fgb::sddmm_default_vrow(A, X, ldx, Y, ldy, k, dtype, flags)) {
+  if (fgb::sddmm_default_vrow(A, X, ldx, Y, ldy, k, dtype, flags) &&
+      !fgb::stream_capturing(fgb::pick_stream(ctx, stream))) {
     const fgb_sddmm_tuning t{0, 2, 256, k > 32 ? 32 : 0};
     return fgb_sddmm_ex(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, &t, stream);
   }

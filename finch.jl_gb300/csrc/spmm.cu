@@ -235,7 +235,7 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
       A->val_t == FGB_F32 && A->idx_t == FGB_I32 && !(flags & FGB_FINCH_ORDER) && nk >= 32 && nk % 4 == 0 &&
       ldb % 4 == 0 && ldc % 4 == 0 && ldb <= INT32_MAX && (uintptr_t)B % 16 == 0 && (uintptr_t)C % 16 == 0 &&
       A->nrows <= INT32_MAX && A->nnz >= (1 << 20) && A->nnz <= INT32_MAX &&
-      (double)A->ncols * (double)nk * 4.0 > 64.0 * 1024 * 1024) {
+      (double)A->ncols * (double)nk * 4.0 > 64.0 * 1024 * 1024 && !stream_capturing(s)) {
     variant = 3;
     lanes = 8;
     path = 128;
