@@ -40,6 +40,7 @@ sys.path.insert(0, str(ROOT))
 
 NNZ_MEAN = 16.0
 NK = 128
+NSETS = 2  # e2e pipeline depth (3 measured no faster): buffer sets (device A, B, C and page-locked C) in rotation
 SEED = 20261203
 
 
@@ -323,10 +324,10 @@ def run_gpu(args):
                        "parallelism": f"replicas{world}"},
             "gpu_launches": args.steps * launches_per_step}
 
-    # ---- e2e: host buffers through the C ABI -> host result.  Two buffer
-    # sets with a plan each (the second plan's schedule comes from the tune
-    # cache); every step uploads A and B from pinned memory, runs the plan
-    # and reads C back, and step i+1's uploads overlap step i's SpMM and
+    # ---- e2e: host buffers through the C ABI -> host result.  NSETS buffer
+    # sets with a plan each (the others' schedules come from the tune cache);
+    # every step uploads A and B from pinned memory, runs the plan and reads
+    # C back, and later steps' uploads overlap earlier steps' SpMM and
     # read-back (copy-in, compute and copy-out streams).
     if not args.no_e2e:
         ctx = dev.context()
@@ -335,9 +336,9 @@ def run_gpu(args):
                   torch.from_numpy(A_h.idx.astype(np.int32)).pin_memory(),
                   torch.from_numpy(A_h.val).pin_memory()]
         B_pin = torch.from_numpy(B_h).pin_memory()
-        C_pin = [torch.empty((M, NK), dtype=torch.float32).pin_memory() for _ in range(2)]
+        C_pin = [torch.empty((M, NK), dtype=torch.float32).pin_memory() for _ in range(NSETS)]
         sets = []
-        for b in range(2):
+        for b in range(NSETS):
             if b == 0 and plan is not None:
                 A_b, B_b, C_b, plan_b = A, B, C, plan
             else:
@@ -355,23 +356,23 @@ def run_gpu(args):
         h2d = sum(h.numel() * h.element_size() for h in host_A) + B_pin.numel() * B_pin.element_size()
         d2h = C_pin[0].numel() * C_pin[0].element_size()
         s_in, s_comp, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
-        ev_in = [torch.cuda.Event() for _ in range(2)]
-        ev_comp = [torch.cuda.Event() for _ in range(2)]
-        ev_out = [torch.cuda.Event() for _ in range(2)]
-        for b in range(2):  # all events start signalled
+        ev_in = [torch.cuda.Event() for _ in range(NSETS)]
+        ev_comp = [torch.cuda.Event() for _ in range(NSETS)]
+        ev_out = [torch.cuda.Event() for _ in range(NSETS)]
+        for b in range(NSETS):  # all events start signalled
             for ev in (ev_in[b], ev_comp[b], ev_out[b]):
                 ev.record(stream)
 
         def e2e_step(i):
-            b = i % 2
+            b = i % NSETS
             A_b, B_b, C_b, plan_b = sets[b]
-            s_in.wait_event(ev_comp[b])  # the SpMM two steps back has read this set
+            s_in.wait_event(ev_comp[b])  # the SpMM NSETS steps back has read this set
             for d, h in zip((A_b.ptr, A_b.idx, A_b.val, B_b), (*host_A, B_pin)):
                 L.check(lib.fgb_upload(ctx, d.data_ptr(), h.data_ptr(), h.numel() * h.element_size(),
                                        s_in.cuda_stream))
             ev_in[b].record(s_in)
             s_comp.wait_event(ev_in[b])
-            s_comp.wait_event(ev_out[b])  # C of two steps back has been read out
+            s_comp.wait_event(ev_out[b])  # C of NSETS steps back has been read out
             with torch.cuda.stream(s_comp):
                 if plan_b is not None:
                     plan_b.execute()
@@ -382,7 +383,7 @@ def run_gpu(args):
             L.check(lib.fgb_download(ctx, C_pin[b].data_ptr(), C_b.data_ptr(), d2h, s_out.cuda_stream))
             ev_out[b].record(s_out)
 
-        for i in range(3):
+        for i in range(NSETS + 1):
             e2e_step(i)
         for st in (s_in, s_comp, s_out):
             stream.wait_stream(st)
@@ -402,12 +403,12 @@ def run_gpu(args):
             t = torch.tensor([e2e_ms], device=device)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
-        last = (e2e_steps - 1) % 2
+        last = (e2e_steps - 1) % NSETS
         ok = bool(np.array_equal(C_pin[last].numpy(), C.cpu().numpy()))
         line["e2e"] = {"value": round(nbytes * e2e_steps * world / (e2e_ms / 1e3) / 1e9, 1),
                        "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "steps": e2e_steps, "ms_per_step": round(e2e_ms / e2e_steps, 3),
-                       "pipeline": "2 buffer sets; copy-in / SpMM / copy-out streams overlap",
+                       "pipeline": f"{NSETS} buffer sets; copy-in / SpMM / copy-out streams overlap",
                        "result_matches_device_run": ok}
         line["gpu_launches"] += e2e_steps * launches_per_step
 
