@@ -32,6 +32,11 @@ constexpr int SG_SMALL_UB = 64;      // rows up to this bound take 8 lanes (128 
 constexpr int SG_WARPS = 4;          // warps per block of the warp tier
 constexpr int SG_BLOCK = 256;        // threads of the block tier
 constexpr int32_t SG_EMPTY = -1;
+// table slots per lane in the warp tiers: 8 lanes with at most 2 * 64 slots,
+// a warp with at most SG_WARP_SLOTS
+constexpr int SG_SLOTS_PER_LANE = 16;
+static_assert(SG_WARP_SLOTS / 32 <= SG_SLOTS_PER_LANE && 2 * SG_SMALL_UB / 8 <= SG_SLOTS_PER_LANE,
+              "a lane's share of a warp-tier table");
 
 __device__ __forceinline__ uint32_t sg_hash(int32_t c) { return (uint32_t)c * 2654435761u; }
 
@@ -128,20 +133,45 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
     }
     sync();  // the next k sees this one's sums
   }
-  if (!SYMB) {
+  if (!SYMB && warp) {
+    // Small table: the row's keys are first listed compactly -- (key, slot)
+    // pairs written over the key table, which holds at least twice as many
+    // slots as the row has keys -- and each key's rank among the n listed
+    // keys is its sorted position.  Ranking against the whole table instead
+    // ran a cap-long loop per occupied slot on every lane of the warp.
+    int32_t myk[SG_SLOTS_PER_LANE];
+    int cnt_mine = 0;
+#pragma unroll
+    for (int u = 0; u < SG_SLOTS_PER_LANE; ++u) {
+      const int64_t s = tid + (int64_t)u * nthreads;
+      myk[u] = s < cap ? keys[s] : SG_EMPTY;
+      cnt_mine += myk[u] != SG_EMPTY ? 1 : 0;
+    }
+    int incl = cnt_mine;  // inclusive scan over the group's lanes
+    for (int m = 1; m < nthreads; m <<= 1) {
+      const int t = __shfl_up_sync(smask, incl, m, nthreads);
+      if (tid >= m) incl += t;
+    }
+    const int n = __shfl_sync(smask, incl, nthreads - 1, nthreads);
+    int pos = incl - cnt_mine;
+    sync();  // every lane has read its keys before the list overwrites them
+    int2* list = reinterpret_cast<int2*>(keys);
+#pragma unroll
+    for (int u = 0; u < SG_SLOTS_PER_LANE; ++u)
+      if (myk[u] != SG_EMPTY) list[pos++] = make_int2(myk[u], (int)(tid + u * nthreads));
+    sync();
+    for (int p = tid; p < n; p += nthreads) {
+      const int2 e = list[p];
+      int o = 0;
+      for (int q = 0; q < n; ++q) o += list[q].x < e.x ? 1 : 0;
+      out_idx[out_pos + o] = e.x + out_base;
+      out_val[out_pos + o] = vals[e.y];
+    }
+  } else if (!SYMB) {  // large rows: unsorted here, ordered by a segmented sort afterwards
     for (int64_t s = tid; s < cap; s += nthreads) {
       const int32_t c = keys[s];
       if (c != SG_EMPTY) {
-        int o;
-        if (warp) {  // small table: the rank among the row's keys is the sorted position
-          o = 0;
-          for (int64_t t = 0; t < cap; ++t) {
-            const int32_t d = keys[t];
-            o += (d != SG_EMPTY && d < c) ? 1 : 0;
-          }
-        } else {  // large rows: unsorted here, ordered by a segmented sort afterwards
-          o = atomicAdd(cnt, 1);
-        }
+        const int o = atomicAdd(cnt, 1);
         out_idx[out_pos + o] = c + out_base;
         out_val[out_pos + o] = vals[s];
       }
@@ -161,7 +191,7 @@ __global__ void __launch_bounds__(SG_WARPS * 32) sg_warp_k(
     int32_t* __restrict__ out_idx, T* __restrict__ out_val) {
   constexpr int NG = SG_WARPS * 32 / G;      // groups per block
   constexpr int SLOTS = SG_WARP_SLOTS * G / 32;
-  __shared__ int32_t s_keys[NG][SLOTS];
+  __shared__ __align__(8) int32_t s_keys[NG][SLOTS];  // 8-byte aligned: the key list is int2 pairs
   __shared__ T s_vals[SYMB ? 1 : NG][SYMB ? 1 : SLOTS];
   __shared__ int s_cnt[NG];
   __shared__ int64_t s_rows[SG_WARPS * 32];  // this tile's rows of the tier
