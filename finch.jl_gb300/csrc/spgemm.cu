@@ -68,9 +68,11 @@ __global__ void sg_gsize_k(int64_t m, const int64_t* __restrict__ ub, int64_t* _
 }
 
 // Inserts key c into a table of `cap` slots (power of two); returns its slot
-// and whether this call created it.
-__device__ __forceinline__ int64_t sg_insert(int32_t* keys, int64_t cap, int32_t c, bool* created) {
-  int64_t s = sg_hash(c) & (cap - 1);
+// and whether this call created it.  I: the slot index type (32-bit for the
+// shared-memory tables).
+template <class I>
+__device__ __forceinline__ I sg_insert(int32_t* keys, I cap, int32_t c, bool* created) {
+  I s = (I)(sg_hash(c) & (uint32_t)(cap - 1));
   while (true) {
     const int32_t k = ((volatile int32_t*)keys)[s];
     if (k == c) {
@@ -99,12 +101,15 @@ __device__ __forceinline__ T sg_acc(T w, T a, T b, int fm) {
 
 // One row with `nthreads` cooperating threads (a warp or a block) over a
 // table of `cap` slots.  SYMB: count keys into *cnt.  Else: accumulate and
-// write the row's (column, value) pairs, unsorted, from out_pos.
-template <class T, class PtrT, bool SYMB>
+// write the row's (column, value) pairs, unsorted, from out_pos.  Positions
+// in A and B are counted in their ptr type, table slots in I (32-bit for the
+// shared-memory tables): the narrower loop arithmetic issues fewer
+// instructions.
+template <class T, class PtrT, bool SYMB, class I>
 __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict__ lp,
                        const int* __restrict__ li, const T* __restrict__ lv, int lbase,
                        const PtrT* __restrict__ rp, const int* __restrict__ ri,
-                       const T* __restrict__ rv, int rbase, int32_t* keys, T* vals, int64_t cap,
+                       const T* __restrict__ rv, int rbase, int32_t* keys, T* vals, I cap,
                        int fm, int* cnt, int out_base, int32_t* __restrict__ out_idx,
                        T* __restrict__ out_val, int64_t out_pos, unsigned smask) {
   // smask: the lanes of a (sub-)warp group; 0 for a whole block
@@ -112,26 +117,32 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
   auto sync = [&]() {
     if (warp) __syncwarp(smask); else __syncthreads();
   };
-  for (int64_t s = tid; s < cap; s += nthreads) keys[s] = SG_EMPTY;
+  for (I s = tid; s < cap; s += nthreads) keys[s] = SG_EMPTY;
   if (tid == 0) *cnt = 0;
   sync();
-  const int64_t q0 = ld_ptr(lp, r) - lbase, q1 = ld_ptr(lp, r + 1) - lbase;
-  for (int64_t q = q0; q < q1; ++q) {  // k in storage order
-    const int64_t k = __ldg(li + q) - lbase;
+  const PtrT q0 = __ldg(lp + r) - lbase, q1 = __ldg(lp + r + 1) - lbase;
+  int made = 0;  // SYMB in a warp tier: keys this lane created
+  for (PtrT q = q0; q < q1; ++q) {  // k in storage order
+    const int k = __ldg(li + q) - lbase;
     const T a = SYMB ? T(0) : lv[q];
-    const int64_t p0 = ld_ptr(rp, k) - rbase, p1 = ld_ptr(rp, k + 1) - rbase;
-    for (int64_t p = p0 + tid; p < p1; p += nthreads) {
+    const PtrT p0 = __ldg(rp + k) - rbase, p1 = __ldg(rp + k + 1) - rbase;
+    for (PtrT p = p0 + tid; p < p1; p += nthreads) {
       const int32_t c = __ldg(ri + p) - rbase;
       bool created;
-      const int64_t s = sg_insert(keys, cap, c, &created);
+      const I s = sg_insert<I>(keys, cap, c, &created);
       if (SYMB) {
-        if (created) atomicAdd(cnt, 1);
+        if (warp) made += created ? 1 : 0;
+        else if (created) atomicAdd(cnt, 1);
       } else {
         const T b = rv[p];
         vals[s] = sg_acc(created ? T(0) : vals[s], a, b, fm);
       }
     }
     sync();  // the next k sees this one's sums
+  }
+  if (SYMB && warp) {  // the group's count: a shuffle sum, not an atomic per key
+    for (int m = nthreads >> 1; m >= 1; m >>= 1) made += __shfl_xor_sync(smask, made, m, nthreads);
+    if (tid == 0) *cnt = made;
   }
   if (!SYMB && warp) {
     // Small table: the row's keys are first listed compactly -- (key, slot)
@@ -143,7 +154,7 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
     int cnt_mine = 0;
 #pragma unroll
     for (int u = 0; u < SG_SLOTS_PER_LANE; ++u) {
-      const int64_t s = tid + (int64_t)u * nthreads;
+      const I s = tid + u * nthreads;
       myk[u] = s < cap ? keys[s] : SG_EMPTY;
       cnt_mine += myk[u] != SG_EMPTY ? 1 : 0;
     }
@@ -168,7 +179,7 @@ __device__ void sg_row(int64_t r, int tid, int nthreads, const PtrT* __restrict_
       out_val[out_pos + o] = vals[e.y];
     }
   } else if (!SYMB) {  // large rows: unsorted here, ordered by a segmented sort afterwards
-    for (int64_t s = tid; s < cap; s += nthreads) {
+    for (I s = tid; s < cap; s += nthreads) {
       const int32_t c = keys[s];
       if (c != SG_EMPTY) {
         const int o = atomicAdd(cnt, 1);
@@ -213,9 +224,9 @@ __global__ void __launch_bounds__(SG_WARPS * 32) sg_warp_k(
     for (int t = grp; t < n; t += NG) {
       const int64_t r = s_rows[t];
       const int64_t u = ub[r];
-      int64_t cap = 16;  // a table sized to the row: at least twice its bound
+      int cap = 16;  // a table sized to the row: at least twice its bound
       while (cap < 2 * u) cap <<= 1;
-      sg_row<T, PtrT, SYMB>(r, gl, G, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[grp],
+      sg_row<T, PtrT, SYMB, int>(r, gl, G, lp, li, lv, lbase, rp, ri, rv, rbase, s_keys[grp],
                             SYMB ? nullptr : &s_vals[SYMB ? 0 : grp][0], cap, fm, &s_cnt[grp],
                             out_base, out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, gmask);
       if (SYMB && gl == 0) cnt_out[r] = s_cnt[grp];
@@ -245,7 +256,7 @@ __global__ void __launch_bounds__(SG_BLOCK) sg_block_k(
     for (int t = 0; t < n; ++t) {  // block-uniform
       const int64_t r = s_rows[t];
       const int64_t off = goff[r], cap = goff[r + 1] - off;
-      sg_row<T, PtrT, SYMB>(r, threadIdx.x, SG_BLOCK, lp, li, lv, lbase, rp, ri, rv, rbase,
+      sg_row<T, PtrT, SYMB, int64_t>(r, threadIdx.x, SG_BLOCK, lp, li, lv, lbase, rp, ri, rv, rbase,
                             gkeys + off, SYMB ? nullptr : gvals + off, cap, fm, &s_cnt, out_base,
                             out_idx, out_val, SYMB ? 0 : cptr[r] - out_base, 0u);
       if (SYMB && threadIdx.x == 0) cnt_out[r] = s_cnt;
