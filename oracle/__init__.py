@@ -200,6 +200,8 @@ def spgemm_csr(m, n, lp, li, lv, rp, ri, rv, fma=True):
     of C = L * R with m rows and n columns, sums in the order of k."""
     lp, li, rp, ri = _i64(lp), _i64(li), _i64(rp), _i64(ri)
     lv, rv = np.ascontiguousarray(lv), np.ascontiguousarray(rv)
+    if lv.dtype not in (np.float64, np.float32) or rv.dtype != lv.dtype:
+        raise TypeError("spgemm_csr: F64 or F32 values of one type")
     ptr = np.zeros(m + 1, dtype=np.int64)
     nnz = lib().orc_spgemm_csr(dtype_code(lv), int(fma), m, n, _p(lp), _p(li), _p(lv), _p(rp),
                                _p(ri), _p(rv), _p(ptr), None, None)

@@ -431,6 +431,7 @@ static float coo_fold_float(int combine, float a, float b) {
 static int32_t coo_fold_int32_t(int combine, int32_t a, int32_t b) {
   switch (combine) {
     case 0: return (int32_t)((uint32_t)a + (uint32_t)b);
+    case 1: return a | b;
     case 2: return b < a ? b : a;
     case 3: return b > a ? b : a;
     default: return b;
@@ -439,6 +440,7 @@ static int32_t coo_fold_int32_t(int combine, int32_t a, int32_t b) {
 static int64_t coo_fold_int64_t(int combine, int64_t a, int64_t b) {
   switch (combine) {
     case 0: return (int64_t)((uint64_t)a + (uint64_t)b);
+    case 1: return a | b;
     case 2: return b < a ? b : a;
     case 3: return b > a ? b : a;
     default: return b;
