@@ -456,6 +456,8 @@ class GalleyScheduler(GB300Scheduler):
     hands every other plan to the single-kernel matcher.  `last_plan` holds
     the chosen steps and their estimated seconds."""
 
+    OPTIONS = ("finch_order", "verbose", "estimator")
+
     def __init__(self, estimator: str = "dc", verbose: bool = False, **kw):
         super().__init__(verbose=verbose, **kw)
         if estimator not in ("dc", "uniform"):

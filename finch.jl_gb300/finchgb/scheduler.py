@@ -161,15 +161,31 @@ class GB300Scheduler:
     running value per output, j ascending), bit-identical to Finch's CPU
     nest; otherwise lane-parallel reductions are used."""
 
+    # the options that make two schedulers equal (src/scheduler/
+    # LogicExecutor.jl:77-78 compares and hashes the options, not the state)
+    OPTIONS = ("finch_order", "verbose")
+
     def __init__(self, finch_order: bool = False, verbose: bool = False):
         self.finch_order = finch_order
         self.verbose = verbose
         self.last_kernel = None
 
+    def options(self) -> dict:
+        return {k: getattr(self, k) for k in self.OPTIONS}
+
     def set_options(self, **kw):
-        for k, v in kw.items():
-            setattr(self, k, v)
-        return self
+        """A new scheduler with the given options changed, the others kept
+        (src/scheduler/LogicExecutor.jl:81-82); an unknown option raises."""
+        unknown = sorted(set(kw) - set(self.OPTIONS))
+        if unknown:
+            raise TypeError(f"unknown scheduler option(s) {unknown}; known: {list(self.OPTIONS)}")
+        return type(self)(**{**self.options(), **kw})
+
+    def __eq__(self, other):
+        return type(self) is type(other) and self.options() == other.options()
+
+    def __hash__(self):
+        return hash((type(self).__name__, tuple(sorted(self.options().items()))))
 
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
