@@ -314,7 +314,6 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   CgBuffers bufs;
-  double* hist_h = nullptr;
   int64_t hist_cap = 0;
   const int grid = grid_for(n, CG_THREADS, ctx->num_sms, 8);  // full occupancy: streaming kernels
   const bool i32 = A64->ptr_t == FGB_I32;  // ptr width of the FP64 matrix
@@ -433,6 +432,5 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(s);
   res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  (void)hist_h;
   return rc;
 }

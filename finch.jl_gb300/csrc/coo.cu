@@ -14,6 +14,7 @@
 #include <cub/cub.cuh>
 
 #include <cmath>
+#include <type_traits>
 
 #include "fgb_internal.cuh"
 
@@ -72,7 +73,10 @@ __device__ __forceinline__ bool fnan(T) { return false; }
 __device__ __forceinline__ bool fnan(double v) { return v != v; }
 __device__ __forceinline__ bool fnan(float v) { return v != v; }
 template <class T>
-__device__ __forceinline__ bool fneg(T v) { return v < 0; }
+__device__ __forceinline__ bool fneg(T v) {
+  if constexpr (std::is_signed<T>::value) return v < 0;
+  else return false;
+}
 __device__ __forceinline__ bool fneg(double v) { return signbit(v); }
 __device__ __forceinline__ bool fneg(float v) { return signbit(v); }
 // min(x, y): a NaN operand wins; otherwise the smaller, with -0.0 below +0.0

@@ -26,7 +26,6 @@
 
 namespace fgb {
 
-constexpr int VR_BATCH = 8;
 constexpr int VR_THREADS = 256;
 constexpr int VR_SEG = 16;  // partial-sum slots per fix-up segment
 
