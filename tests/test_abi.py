@@ -43,6 +43,13 @@ def test_library_exports_every_declared_symbol(lib_path):
     assert exported <= declared_symbols()
 
 
+def test_integration_guide_maps_every_entry_point():
+    # every declared entry point has a line saying which reference interface it replaces
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    unmapped = sorted(n for n in declared_symbols() if n not in guide)
+    assert not unmapped, unmapped
+
+
 def test_python_binding_covers_header():
     from finchgb import _lib
 
