@@ -428,6 +428,11 @@ def run_gpu(args):
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
                         "algorithmic_bytes_per_launch": nbytes,
                         "avg_launch_ms": round(avg_ms, 4)}
+    if traffic:
+        # the DRAM bytes ncu counted for one step, over this run's step time:
+        # how busy HBM is, against the compulsory-byte fraction above
+        line["roofline"]["traffic_gbs"] = round(traffic / (avg_ms / 1e3) / 1e9, 1)
+        line["roofline"]["traffic_frac"] = round(traffic / (avg_ms / 1e3) / 1e9 / peak, 4)
     # The slab kernel gathers a 4*lanes-column piece of one B row per stored
     # entry and slab: nnz * NK * 4 bytes per step, from a working set of one
     # slab of B.  Its ceiling is the random-gather rate at that width and
