@@ -239,11 +239,12 @@ def run_gpu(args):
     B = torch.from_numpy(B_h).to(device)
     C = torch.empty((M, NK), dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream()
-    fixed_variant = 0
-    if args.schedule:  # fixed schedule LANES,PATH[,VARIANT] through fgb_spmm_ex (profiling)
+    fixed_variant = fixed_bands = 0
+    if args.schedule:  # fixed schedule LANES,PATH[,VARIANT[,BANDS]] through fgb_spmm_ex (profiling)
         vals = [int(v) for v in args.schedule.split(",")]
         lanes, path = vals[0], vals[1]
         fixed_variant = vals[2] if len(vals) > 2 else 0
+        fixed_bands = vals[3] if len(vals) > 3 else 0
         table, plan, npanels = {}, None, 1
     else:
         # the plain schedules' table (for the e2e leg and the record), then the
@@ -276,7 +277,7 @@ def run_gpu(args):
         if plan is not None:
             plan.execute()
         else:
-            dev.spmm(A, B, C, lanes=lanes, path=path, variant=fixed_variant)
+            dev.spmm(A, B, C, lanes=lanes, path=path, variant=fixed_variant, bands=fixed_bands)
 
     def barrier():
         if world > 1:
@@ -377,7 +378,7 @@ def run_gpu(args):
                 if plan_b is not None:
                     plan_b.execute()
                 else:
-                    dev.spmm(A_b, B_b, C_b, lanes=lanes, path=path, variant=fixed_variant)
+                    dev.spmm(A_b, B_b, C_b, lanes=lanes, path=path, variant=fixed_variant, bands=fixed_bands)
             ev_comp[b].record(s_comp)
             s_out.wait_event(ev_comp[b])
             L.check(lib.fgb_download(ctx, C_pin[b].data_ptr(), C_b.data_ptr(), d2h, s_out.cuda_stream))

@@ -20,6 +20,14 @@ __device__ __forceinline__ uint32_t cal_hash(uint32_t x) {
   return x;
 }
 
+// A uniform place in [0, n) for a 32-bit hash: the high word of hash * n
+// (one multiply) for n < 2^32, so the index arithmetic stays a few
+// instructions per gather.  A 64-bit `%` costs dozens of instructions per
+// gather and made the probe issue-bound below the memory system's rate.
+__device__ __forceinline__ uint64_t cal_place(uint32_t h, uint64_t n) {
+  return n <= 0xffffffffull ? (uint64_t)__umulhi(h, (uint32_t)n) : (uint64_t)h % n;
+}
+
 // G lanes (16 bytes each) per gather; every lane keeps CAL_INFLIGHT loads in
 // flight.  `lines` = working set / gather width, so every address is inside
 // the buffer: line < lines and part < G.
@@ -35,7 +43,7 @@ __global__ void __launch_bounds__(CAL_THREADS) gather_ceiling_k(const float* __r
     float4 v[CAL_INFLIGHT];
 #pragma unroll
     for (int u = 0; u < CAL_INFLIGHT; ++u) {
-      const uint64_t line = cal_hash(gid * 0x9E3779B9u + (uint32_t)(it + u)) % lines;
+      const uint64_t line = cal_place(cal_hash(gid * 0x9E3779B9u + (uint32_t)(it + u)), lines);
       v[u] = ld_gather_f32x4(buf + (line * G + part) * 4, pol);
     }
 #pragma unroll
@@ -55,7 +63,8 @@ __global__ void __launch_bounds__(CAL_THREADS) gather_ceiling_word_k(const T* __
   for (int it = 0; it < iters; it += CAL_INFLIGHT) {
     T v[CAL_INFLIGHT];
 #pragma unroll
-    for (int u = 0; u < CAL_INFLIGHT; ++u) v[u] = __ldg(buf + cal_hash(gid * 0x9E3779B9u + (uint32_t)(it + u)) % n);
+    for (int u = 0; u < CAL_INFLIGHT; ++u)
+      v[u] = __ldg(buf + cal_place(cal_hash(gid * 0x9E3779B9u + (uint32_t)(it + u)), n));
 #pragma unroll
     for (int u = 0; u < CAL_INFLIGHT; ++u) acc += v[u];
   }

@@ -35,7 +35,13 @@ struct Choice {
   int64_t path = 0;
   int panels = 1;  // SpMM: column panels (1 = the plain merge-path schedule)
   int variant = 0;  // SpMM: 0 register gathers, 1 TMA stage ring, 2 virtual-row slabs
+  int bands = 1;    // virtual rows: column bands of A (1 = none)
 };
+
+static bool same_choice(const Choice& a, const Choice& b) {
+  return a.lanes == b.lanes && a.path == b.path && a.panels == b.panels && a.variant == b.variant &&
+         a.bands == b.bands;
+}
 
 static std::mutex g_tune_mu;
 static std::map<std::string, Choice> g_tune_cache;
@@ -58,9 +64,15 @@ static void tune_cache_load_locked() {
   const char* path = std::getenv("FGB_TUNE_CACHE");
   if (!path) return;
   std::ifstream in(path);
-  std::string key;
-  Choice c;
-  while (in >> key >> c.lanes >> c.path >> c.panels >> c.variant) g_tune_cache[key] = c;
+  std::string line;
+  while (std::getline(in, line)) {  // key lanes path panels variant [bands]
+    std::istringstream ls(line);
+    std::string key;
+    Choice c;
+    if (!(ls >> key >> c.lanes >> c.path >> c.panels >> c.variant)) continue;
+    if (!(ls >> c.bands)) c.bands = 1;
+    g_tune_cache[key] = c;
+  }
 }
 
 static void tune_cache_store_locked(const std::string& key, const Choice& c) {
@@ -68,7 +80,20 @@ static void tune_cache_store_locked(const std::string& key, const Choice& c) {
   const char* path = std::getenv("FGB_TUNE_CACHE");
   if (!path) return;
   std::ofstream out(path, std::ios::app);
-  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << ' ' << c.variant << '\n';
+  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << ' ' << c.variant << ' ' << c.bands
+      << '\n';
+}
+
+// FGB_TUNE_LOG names a file that receives one line per timed candidate
+// (shape key, lanes, path, panels, variant, bands, ms per run): the whole
+// search, not only the choice.
+static void tune_log(const std::string& key, const Choice& c, double ms) {
+  const char* path = std::getenv("FGB_TUNE_LOG");
+  if (!path) return;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::ofstream out(path, std::ios::app);
+  out << key << ' ' << c.lanes << ' ' << c.path << ' ' << c.panels << ' ' << c.variant << ' ' << c.bands << ' '
+      << ms << '\n';
 }
 
 }  // namespace fgb
@@ -77,7 +102,7 @@ using namespace fgb;
 
 struct fgb_plan {
   std::map<int, fgb_panels*> panels;  // SpMM column-panel layouts by panel count
-  std::map<int64_t, VrowSchedule> vrows;  // SpMM virtual-row schedules by length
+  std::map<std::pair<int64_t, int>, VrowSchedule> vrows;  // virtual-row schedules by (length, bands)
   void* partial = nullptr;            // their partial sums (largest candidate)
   size_t partial_bytes = 0;
   fgb_ctx* ctx = nullptr;
@@ -115,12 +140,12 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
                                d.flags, &t, s);
       }
       if (c.variant == 2 || c.variant == 3) {
-        auto it = p->vrows.find(c.path);
+        auto it = p->vrows.find({c.path, c.bands});
         if (it == p->vrows.end()) {  // built outside capture (the timing pass comes first)
           VrowSchedule v;
-          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s);
+          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s, false, c.bands);
           if (rc) return rc;
-          it = p->vrows.emplace(c.path, v).first;
+          it = p->vrows.emplace(std::make_pair(c.path, c.bands), v).first;
         }
         const size_t need = spmm_vrow_scratch_bytes(it->second, d.k);
         if (need > p->partial_bytes) {  // never during capture: the same choice ran before it
@@ -143,12 +168,12 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
                        c.lanes, 0, s);
     case FGB_PLAN_SDDMM:
       if (c.variant == 3 || c.variant == 4) {  // virtual rows (schedule built outside capture); 4: cp.async gathers
-        auto it = p->vrows.find(c.path);
+        auto it = p->vrows.find({c.path, c.bands});
         if (it == p->vrows.end()) {
           VrowSchedule v;
-          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s);
+          int rc = vrow_build(p->ctx, &p->A, (int)c.path, &v, s, false, c.bands);
           if (rc) return rc;
-          it = p->vrows.emplace(c.path, v).first;
+          it = p->vrows.emplace(std::make_pair(c.path, c.bands), v).first;
         }
         return sddmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.in1, d.ld_in1, d.k, d.out, s,
                           c.lanes > 0 ? 4 * c.lanes : 0, c.variant == 4);
@@ -186,6 +211,13 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int l : {2, 4, 8})  // column slabs over length-sorted virtual rows
         for (int64_t t : {32, 64, 128})
           for (int v : {2, 3}) out.push_back(Choice{l, t, 1, v});  // register / cp.async gathers
+    // the same with A's columns cut into bands, so each launch gathers from
+    // 1/bands of B's slab (worth it when the slab does not fit L2)
+    if (d.dtype == FGB_F32 && p->A.val_t == FGB_F32 && p->A.nrows <= INT32_MAX && p->A.idx_t == FGB_I32 &&
+        (double)p->A.ncols * 128.0 > 48.0 * 1024 * 1024)
+      for (int l : {4, 8})
+        for (int64_t t : {64, 128, 256})
+          for (int nb : {2, 4, 8}) out.push_back(Choice{l, t, 1, 3, nb});
     // column panels keep each panel's slice of B in L2 (worth it when B is not)
     const double b_bytes = (double)p->A.ncols * (double)d.k * (d.dtype == FGB_F64 ? 8 : 4);
     if (b_bytes > 32.0 * 1024 * 1024 && !(d.flags & FGB_ACCUMULATE))
@@ -201,11 +233,17 @@ std::vector<Choice> candidates(const fgb_plan* p) {
       for (int64_t chunk : {128, 256, 512}) out.push_back(Choice{d.dtype == FGB_F64 ? 16 : 8, chunk, 1, 2});
     if (d.dtype == FGB_F32 && p->A.orient == FGB_CSR && p->A.val_t == FGB_F32 && d.k <= 128 &&
         d.k % 4 == 0 && d.ld_in0 % 4 == 0 && d.ld_in1 % 4 == 0 && p->A.nnz <= INT32_MAX)
-      for (int64_t t : {64, 128, 256})  // virtual rows, all of k or 32-column slabs
+      for (int64_t t : {64, 128, 256}) {  // virtual rows, all of k or 32-column slabs
         for (int v : {3, 4}) {            // register / cp.async gathers
           out.push_back(Choice{0, t, 1, v});
           if (d.k > 32) out.push_back(Choice{8, t, 1, v});
         }
+        if ((double)p->A.ncols * 128.0 > 48.0 * 1024 * 1024)  // column bands of A
+          for (int nb : {2, 4, 8}) {
+            out.push_back(Choice{0, t, 1, 4, nb});
+            if (d.k > 32) out.push_back(Choice{8, t, 1, 4, nb});
+          }
+      }
   }
   return out;
 }
@@ -256,8 +294,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
       for (const Choice& c : cands)
-        if (c.lanes == it->second.lanes && c.path == it->second.path &&
-            c.panels == it->second.panels && c.variant == it->second.variant) {
+        if (same_choice(c, it->second)) {
           best = c;
           cached = true;
         }
@@ -282,6 +319,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
       ms /= tune_reps;
+      tune_log(key, c, ms);
       if (first_ms < 0) first_ms = ms;
       if (best_ms < 0 || ms < best_ms) {
         best_ms = ms;
@@ -322,7 +360,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   for (auto it = p->vrows.begin(); it != p->vrows.end();) {  // and the chosen schedule
     const bool vrow_choice = p->d.op == FGB_PLAN_SPMM ? (best.variant == 2 || best.variant == 3)
                                                        : (best.variant == 3 || best.variant == 4);
-    if (!vrow_choice || it->first != best.path) {
+    if (!vrow_choice || it->first != std::make_pair(best.path, best.bands)) {
       vrow_free(&it->second);
       it = p->vrows.erase(it);
     } else {
@@ -338,6 +376,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
     }
   }
   p->info.lanes = best.lanes;
+  p->info.bands = best.bands;
   p->info.panels = best.panels;
   p->info.variant = best.variant;
   p->info.path = best.path;

@@ -273,13 +273,17 @@ extern "C" int fgb_sddmm(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64
 extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
                             const void* Y, int64_t ldy, int64_t k, void* out_val, int dtype,
                             unsigned flags, const fgb_sddmm_tuning* tune, void* stream) {
-  if (!tune || (tune->lanes == 0 && tune->variant == 0 && tune->chunk == 0 && tune->slab == -1))
+  if (!tune || (tune->lanes == 0 && tune->variant == 0 && tune->chunk == 0 && tune->slab == -1 &&
+                tune->bands <= 1))
     return fgb_sddmm(ctx, A, X, ldx, Y, ldy, k, out_val, dtype, flags, stream);  // no schedule given
   const int lanes = tune->lanes;
   if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: lanes must be 0, 4, 8, 16 or 32");
   if (tune && (tune->chunk < 0 || tune->slab < -1))
     return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: negative chunk or slab");
+  if (tune->bands < 0 || tune->bands > 8) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: bands must be in [0, 8]");
+  if (tune->bands > 1 && tune->variant != 1 && tune->variant != 2)
+    return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: column bands need variant 1 or 2");
   if (tune && (tune->variant == 1 || tune->variant == 2)) {  // virtual rows: schedule built for this call
     if (!ctx) return fgb::set_error(FGB_EINVAL, "fgb_sddmm_ex: null ctx");
     int rc = fgb::check_sparse(A, "fgb_sddmm_ex: A", true);
@@ -290,7 +294,7 @@ extern "C" int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, in
     cudaStream_t s = fgb::pick_stream(ctx, stream);
     fgb::VrowSchedule v;
     rc = fgb::vrow_build(ctx, A, tune->chunk > 0 ? (int)std::min<int64_t>(tune->chunk, 4096) : 128, &v, s,
-                         true);
+                         true, tune->bands > 1 ? tune->bands : 1);
     if (rc) return rc;
     rc = fgb::sddmm_vrow(ctx, v, A, X, ldx, Y, ldy, k, out_val, s, tune->slab > 0 ? tune->slab : 0,
                          tune->variant == 2);

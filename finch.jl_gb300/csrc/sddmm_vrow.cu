@@ -10,7 +10,9 @@
 // sub-groups of a warp run similar trip counts.  Optionally k is cut into
 // column slabs of one 128-byte line of Y, one launch each (fewer L2 lines per
 // launch); the dot then accumulates in `out` across launches and the last
-// launch multiplies by A's value.
+// launch multiplies by A's value.  A schedule with column bands runs each
+// band's virtual rows in launches of their own, so a launch gathers from
+// 1/nbands of Y; entries do not combine, so bands change no result.
 #include "spmm_common.cuh"
 
 namespace fgb {
@@ -157,11 +159,15 @@ static int launch_sddmm_vrow_async_t(fgb_ctx* ctx, const VrowSchedule& v, const 
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_async_k<L, NB, 6, ALL>, SV_THREADS, smem);
     return o > 0 ? o : 1;
   }();
-  const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
-  sddmm_vrow_async_k<L, NB, 6, ALL><<<grid, SV_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx,
-                                                                  (const float*)A->val, X, ldx, Y, (int)ldy,
-                                                                  k, out, A->index_base, mode);
+  for (int b = 0; b < v.nbands; ++b) {  // column bands: one launch each (1/nbands of Y per launch)
+    const int64_t nvb = v.nbands > 1 ? v.band_off[b + 1] - v.band_off[b] : v.nv;
+    if (nvb == 0) continue;
+    const int64_t need = (nvb * L + SV_THREADS - 1) / SV_THREADS;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
+    sddmm_vrow_async_k<L, NB, 6, ALL><<<grid, SV_THREADS, smem, s>>>(
+        nvb, v.vr + (v.nbands > 1 ? v.band_off[b] : 0), (const int*)A->idx, (const float*)A->val, X, ldx, Y,
+        (int)ldy, k, out, A->index_base, mode);
+  }
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
 }
@@ -185,10 +191,15 @@ static int launch_sddmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_spar
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, sddmm_vrow_k<L, NB>, SV_THREADS, 0);
     return o > 0 ? o : 1;
   }();
-  const int64_t need = (v.nv * L + SV_THREADS - 1) / SV_THREADS;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
-  sddmm_vrow_k<L, NB><<<grid, SV_THREADS, 0, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val,
-                                                  X, ldx, Y, ldy, k, out, A->index_base, mode);
+  for (int b = 0; b < v.nbands; ++b) {
+    const int64_t nvb = v.nbands > 1 ? v.band_off[b + 1] - v.band_off[b] : v.nv;
+    if (nvb == 0) continue;
+    const int64_t need = (nvb * L + SV_THREADS - 1) / SV_THREADS;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
+    sddmm_vrow_k<L, NB><<<grid, SV_THREADS, 0, s>>>(nvb, v.vr + (v.nbands > 1 ? v.band_off[b] : 0),
+                                                    (const int*)A->idx, (const float*)A->val, X, ldx, Y, ldy,
+                                                    k, out, A->index_base, mode);
+  }
   FGB_CUDA_TRY(cudaGetLastError());
   return FGB_OK;
 }

@@ -219,7 +219,7 @@ static int run_typed(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t l
 
 int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
               int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream,
-              int variant) {
+              int variant, int bands) {
   if (!ctx) return set_error(FGB_EINVAL, "fgb_spmm: null ctx");
   int rc = check_sparse(A, "fgb_spmm: A", true);
   if (rc) return rc;
@@ -247,7 +247,8 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
     // the schedule and partial sums come from the stream-ordered pool and go
     // back to it behind the launches (no device-wide synchronisation)
     VrowSchedule v;
-    rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s, true);
+    rc = vrow_build(ctx, A, path > 0 ? (int)std::min<int64_t>(path, 4096) : 64, &v, s, true,
+                    bands > 1 ? bands : 1);
     if (rc) return rc;
     void* part = nullptr;
     const int slab = 4 * (lanes > 0 ? lanes : 4);
@@ -285,11 +286,15 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
   int lanes = tune ? tune->lanes : 0;
   int64_t path = tune ? tune->path : 0;
   const int variant = tune ? tune->variant : 0;
+  const int bands = tune ? tune->bands : 0;
   if (variant < 0 || variant > 3) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1, 2 or 3");
+  if (bands < 0 || bands > 8) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: bands must be in [0, 8]");
+  if (bands > 1 && variant != 2 && variant != 3)
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: column bands need variant 2 or 3");
   if (variant == 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant 2 takes lanes 2, 4 or 8");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
   if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");
-  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, lanes, path, stream, variant);
+  return fgb::spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, lanes, path, stream, variant, bands);
 }

@@ -10,7 +10,7 @@ namespace fgb {
 // fgb_spmm's dispatcher (spmm.cu); lanes/path 0 = defaults.
 int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
               int64_t ldc, int dtype, unsigned flags, int lanes, int64_t path, void* stream,
-              int variant = 0);
+              int variant = 0, int bands = 1);
 
 // Merge-path SpMM (spmm_merge.cu).
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path);
@@ -29,7 +29,7 @@ struct VrowSchedule {
   int64_t nv = 0, nl = 0;  // virtual rows; partial-sum slots (chunks after a row's first)
   int T = 0;
   int4* vr = nullptr;      // per virtual row (sorted): row, first entry, length, partial
-                           // slot (-1: writes C)
+                           // slot (-1: writes C, -2: adds to C)
   // fix-up of the partial sums: segments of at most 16 slots of one row
   // {row, first slot, slots, segment-sum slot (-1: add to C directly)}, and the
   // long rows {row, first segment-sum slot, segments, 0} whose segment sums a
@@ -39,12 +39,18 @@ struct VrowSchedule {
   int4* lrow = nullptr;
   void* mem = nullptr;
   bool pooled = false;  // mem from the stream-ordered pool (a schedule for one call)
+  // column bands: band b's virtual rows are vr[band_off[b] .. band_off[b+1])
+  // and run in launches of their own, band after band (1 = no bands)
+  int nbands = 1;
+  int64_t band_off[9] = {};
 };
 // pooled: allocate the schedule from the stream-ordered pool, to be freed by
 // vrow_free on a stream (a schedule built for one call); else cudaMalloc
 // (a plan's).  Stream-ordered: the schedule is ready for launches on s.
+// bands (1..8): cut A's columns into that many bands of consecutive columns,
+// each band's entries in launches of their own (SpMM only).
 int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s,
-               bool pooled = false);
+               bool pooled = false, int bands = 1);
 void vrow_free(VrowSchedule* v, cudaStream_t s = nullptr);
 // partial: the long rows' partial sums (spmm_vrow_scratch_bytes).
 size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk);

@@ -24,6 +24,7 @@
 // broadcast by shuffles; up to BATCH gathers of B are in flight per lane.  The
 // grid is persistent: occupancy-many blocks per SM, items handed out by warp.
 #include "spmm_common.cuh"
+#include "spmm_noalloc_plan.h"
 
 namespace fgb {
 
@@ -184,9 +185,7 @@ __global__ void spmm_fixup_k(int64_t n_items, int64_t nk, const int64_t* __restr
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 size_t spmm_merge_scratch_bytes(int64_t nrows, int64_t nnz, int64_t nk, size_t esz, int64_t path) {
-  const int64_t n_items = (nrows + nnz + path - 1) / path;
-  return align256(sizeof(int64_t) * (n_items + 1)) * 2 + align256(sizeof(int64_t) * n_items) +
-         align256(esz * n_items * nk);
+  return merge_scratch_bytes(nrows, nnz, nk, esz, path);  // the layout launch_merge carves below
 }
 
 template <class T, class VT, class PtrT, int L>

@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "spmm_common.cuh"
+#include "spmm_noalloc_plan.h"
 
 namespace fgb {
 
@@ -30,18 +31,15 @@ constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (looked up once).
+// Device address of the scratch array on `device`, which is current (looked
+// up once per device).
 static int noalloc_scratch(int device, void** out) {
   if (device < 0 || device >= kMaxDevices)
     return set_error(FGB_EINVAL, "fgb_spmm_noalloc: device %d out of range", device);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_ptr[device]) {
-    int cur = -1;
-    FGB_CUDA_TRY(cudaGetDevice(&cur));
-    if (cur != device) FGB_CUDA_TRY(cudaSetDevice(device));
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_noalloc_scratch);
-    if (cur != device) cudaSetDevice(cur);
     if (e != cudaSuccess)
       return set_error(FGB_ECUDA, "fgb_spmm_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     g_noalloc_ptr[device] = p;
@@ -74,16 +72,20 @@ extern "C" int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B
     return spmm_impl(ctx, A, B, ldb, nk, C, ldc, dtype, flags, 0, 0, stream);
   // The merge-path schedule: lengthen the items until the scratch fits.
   int64_t path = 256;
-  while (path < (int64_t(1) << 24) &&
-         spmm_merge_scratch_bytes(A->nrows, A->nnz, nk, esz, path) > FGB_NOALLOC_SCRATCH_BYTES)
-    path *= 2;
-  const size_t need = spmm_merge_scratch_bytes(A->nrows, A->nnz, nk, esz, path);
-  if (need > FGB_NOALLOC_SCRATCH_BYTES)
+  size_t need = 0;
+  if (!noalloc_pick_path(A->nrows, A->nnz, nk, esz, FGB_NOALLOC_SCRATCH_BYTES, &path, &need))
     return set_error(FGB_EINVAL,
                      "fgb_spmm_noalloc: %lld rows, %lld stored entries and %lld columns need %zu "
                      "bytes of scratch, above the fixed %zu",
                      (long long)A->nrows, (long long)A->nnz, (long long)nk, need,
                      (size_t)FGB_NOALLOC_SCRATCH_BYTES);
+  // The kernels run on the current device, so the scratch address must be
+  // that device's: the context's device must be current.
+  int cur = -1;
+  FGB_CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != ctx->device)
+    return set_error(FGB_EINVAL, "fgb_spmm_noalloc: device %d is current, the context is on device %d", cur,
+                     ctx->device);
   void* scratch = nullptr;
   rc = noalloc_scratch(ctx->device, &scratch);
   if (rc) return rc;

@@ -29,19 +29,92 @@ namespace fgb {
 constexpr int VR_THREADS = 256;
 constexpr int VR_SEG = 16;  // partial-sum slots per fix-up segment
 
+// Column bands.  With P > 1 bands the columns of A are cut into P ranges of
+// W consecutive columns, and a row's entries in band b (a contiguous run of
+// its ascending columns) are scheduled in band b's launches only: a launch
+// then gathers from 1/P of B's slab, which stays in L2.  A light row (no
+// band holds more than T of its entries) keeps one running sum in C: its
+// first non-empty band writes C and each later band continues from it,
+// launch after launch, so its sum runs over its entries in storage order and
+// equals the unbanded schedule's bit for bit.  A heavy row is
+// cut at band boundaries and every T entries; its first chunk writes C and
+// the others write partial-sum slots that the fix-up adds in order.  P = 1 is
+// the unbanded schedule.
+constexpr int VR_MAX_BANDS = 8;
+
+struct RowBands {
+  int64_t pos[VR_MAX_BANDS + 1];  // storage offsets (from the row's first entry) of the band starts
+};
+
+// Band starts of one row: pos[b] = number of the row's entries with column
+// < b * W (columns ascending; for unsorted columns the runs still cover the
+// row exactly once, only the locality is lost).
+__device__ __forceinline__ void row_bands(const int* __restrict__ idx, int64_t b0, int64_t len, int base,
+                                          int P, int64_t W, RowBands& rb) {
+  rb.pos[0] = 0;
+  rb.pos[P] = len;
+  for (int b = 1; b < P; ++b) {
+    const int64_t c = (int64_t)b * W;  // first column of band b
+    int64_t lo = rb.pos[b - 1], hi = len;
+    while (lo < hi) {  // first entry with column >= c
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)idx[b0 + mid] - base < c) lo = mid + 1;
+      else hi = mid;
+    }
+    rb.pos[b] = lo;
+  }
+}
+
+// Virtual rows of one row, in storage order: per band, ceil(len_b / T)
+// chunks for a heavy row, one chunk per non-empty band for a light row (an
+// empty row keeps one empty virtual row in band 0, which writes its zeros).
+__device__ __forceinline__ bool row_is_light(const RowBands& rb, int P, int T) {
+  for (int b = 0; b < P; ++b)
+    if (rb.pos[b + 1] - rb.pos[b] > T) return false;
+  return true;
+}
+
 // Per row: virtual rows, partial-sum slots, fix-up segments (a row's slots in
 // runs of at most VR_SEG), whether it is a long row (more than one segment:
-// its segment sums are combined by a second pass) and its segment sums.
+// its segment sums are combined by a second pass) and its segment sums; per
+// band (atomically, into band_cnt): the virtual rows of that band.
 template <class PtrT>
-__global__ void vrow_count_k(int64_t nrows, const PtrT* __restrict__ ptr, int T,
-                             int64_t* __restrict__ nv, int64_t* __restrict__ nl,
-                             int64_t* __restrict__ nseg, int64_t* __restrict__ nlong,
-                             int64_t* __restrict__ nss) {
+__global__ void vrow_count_k(int64_t nrows, const PtrT* __restrict__ ptr, const int* __restrict__ idx,
+                             int base, int T, int P, int64_t W, int64_t* __restrict__ nv,
+                             int64_t* __restrict__ nl, int64_t* __restrict__ nseg,
+                             int64_t* __restrict__ nlong, int64_t* __restrict__ nss,
+                             unsigned long long* __restrict__ band_cnt) {
+  unsigned long long mine[VR_MAX_BANDS] = {};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
        r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t len = ld_ptr(ptr, r + 1) - ld_ptr(ptr, r);
-    const int64_t nch = len <= T ? 1 : (len + T - 1) / T;
-    const int64_t slots = nch - 1;
+    const int64_t b0 = ld_ptr(ptr, r) - base;
+    const int64_t len = ld_ptr(ptr, r + 1) - base - b0;
+    RowBands rb;
+    if (P > 1) row_bands(idx, b0, len, base, P, W, rb);
+    else {
+      rb.pos[0] = 0;
+      rb.pos[1] = len;
+    }
+    int64_t nch = 0, slots = 0;
+    if (row_is_light(rb, P, T)) {
+      for (int b = 0; b < P; ++b)
+        if (rb.pos[b + 1] > rb.pos[b]) {
+          ++nch;
+          ++mine[b];
+        }
+      if (nch == 0) {
+        nch = 1;
+        ++mine[0];
+      }
+    } else {
+      for (int b = 0; b < P; ++b) {
+        const int64_t lb = rb.pos[b + 1] - rb.pos[b];
+        const int64_t c = (lb + T - 1) / T;
+        nch += c;
+        mine[b] += (unsigned long long)c;
+      }
+      slots = nch - 1;
+    }
     const int64_t segs = (slots + VR_SEG - 1) / VR_SEG;
     nv[r] = nch;
     nl[r] = slots;
@@ -49,6 +122,8 @@ __global__ void vrow_count_k(int64_t nrows, const PtrT* __restrict__ ptr, int T,
     nlong[r] = segs > 1 ? 1 : 0;
     nss[r] = segs > 1 ? segs : 0;
   }
+  for (int b = 0; b < P; ++b)
+    if (mine[b]) atomicAdd(band_cnt + b, mine[b]);
 }
 
 __device__ __forceinline__ uint8_t vrow_class(int64_t len) {
@@ -57,30 +132,50 @@ __device__ __forceinline__ uint8_t vrow_class(int64_t len) {
   return (uint8_t)(15 - b);
 }
 
-// The virtual rows of every row (unsorted, with their length-class keys) and
-// its fix-up records.  soff/goff/ssoff: exclusive scans of the segments, the
-// long rows and the segment sums (vrow_count_k).
+// The virtual rows of every row (unsorted, with their band and length-class
+// keys) and its fix-up records.  soff/goff/ssoff: exclusive scans of the
+// segments, the long rows and the segment sums (vrow_count_k).  Record w:
+// -1 writes C, -2 adds to C (a light row's later band), >= 0 a partial slot.
 template <class PtrT>
-__global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, int base, int T,
-                            const int64_t* __restrict__ voff, const int64_t* __restrict__ loff,
-                            const int64_t* __restrict__ soff, const int64_t* __restrict__ goff,
-                            const int64_t* __restrict__ ssoff, uint8_t* __restrict__ key,
-                            int32_t* __restrict__ ord, int4* __restrict__ unsorted,
-                            int4* __restrict__ seg, int4* __restrict__ lrow) {
+__global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, const int* __restrict__ idx,
+                            int base, int T, int P, int64_t W, const int64_t* __restrict__ voff,
+                            const int64_t* __restrict__ loff, const int64_t* __restrict__ soff,
+                            const int64_t* __restrict__ goff, const int64_t* __restrict__ ssoff,
+                            uint8_t* __restrict__ key, int32_t* __restrict__ ord,
+                            int4* __restrict__ unsorted, int4* __restrict__ seg, int4* __restrict__ lrow) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
        r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b0 = ld_ptr(ptr, r) - base;
     const int64_t len = ld_ptr(ptr, r + 1) - base - b0;
-    const int64_t v0 = voff[r], l0 = loff[r];
-    const int64_t nch = voff[r + 1] - v0;
-    for (int64_t c = 0; c < nch; ++c) {
-      const int64_t v = v0 + c;
-      const int64_t clen = len - c * T < T ? len - c * T : T;
-      key[v] = vrow_class(clen);
-      ord[v] = (int32_t)v;
-      unsorted[v] = make_int4((int)r, (int)(b0 + c * T), (int)clen, c == 0 ? -1 : (int)(l0 + c - 1));
+    RowBands rb;
+    if (P > 1) row_bands(idx, b0, len, base, P, W, rb);
+    else {
+      rb.pos[0] = 0;
+      rb.pos[1] = len;
     }
-    const int64_t slots = nch - 1, s0 = soff[r], segs = soff[r + 1] - s0;
+    const int64_t v0 = voff[r], l0 = loff[r];
+    int64_t c = 0;  // virtual rows written so far
+    auto emit = [&](int b, int64_t first, int64_t clen, int w) {
+      const int64_t v = v0 + c;
+      key[v] = (uint8_t)((b << 4) | vrow_class(clen));
+      ord[v] = (int32_t)v;
+      unsorted[v] = make_int4((int)r, (int)(b0 + first), (int)clen, w);
+      ++c;
+    };
+    if (row_is_light(rb, P, T)) {
+      for (int b = 0; b < P; ++b) {
+        const int64_t lb = rb.pos[b + 1] - rb.pos[b];
+        if (lb > 0) emit(b, rb.pos[b], lb, c == 0 ? -1 : -2);
+      }
+      if (c == 0) emit(0, 0, 0, -1);
+    } else {
+      for (int b = 0; b < P; ++b)
+        for (int64_t f = rb.pos[b]; f < rb.pos[b + 1]; f += T) {
+          const int64_t clen = rb.pos[b + 1] - f < T ? rb.pos[b + 1] - f : T;
+          emit(b, f, clen, c == 0 ? -1 : (int)(l0 + c - 1));
+        }
+    }
+    const int64_t slots = loff[r + 1] - l0, s0 = soff[r], segs = soff[r + 1] - s0;
     if (segs == 1) {
       seg[s0] = make_int4((int)r, (int)l0, (int)slots, -1);
     } else if (segs > 1) {
@@ -100,6 +195,36 @@ __global__ void vrow_gather_k(int64_t nv, const int32_t* __restrict__ ord,
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv;
        i += (int64_t)gridDim.x * blockDim.x)
     vr[i] = unsorted[ord[i]];
+}
+
+// The start of a virtual row: a light row's later column band (w = -2)
+// continues the running sum its earlier bands left in C, so the row is one
+// sequential sum over its entries in storage order, as without bands.
+__device__ __forceinline__ float4 vrow_init(const int4& rec, const float* __restrict__ C, int64_t ldc,
+                                            int64_t col, bool active) {
+  if (rec.w == -2 && active) return *reinterpret_cast<const float4*>(C + (int64_t)rec.x * ldc + col);
+  return make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// The end of a virtual row: w = -1 writes C (adds to it under `accumulate`),
+// w = -2 writes the continued running sum back to C, w >= 0 writes
+// partial-sum slot w.
+__device__ __forceinline__ void vrow_store(const int4& rec, float4 acc, float* __restrict__ C, int64_t ldc,
+                                           int64_t col, int64_t nk, int accumulate, float* __restrict__ partial,
+                                           uint64_t pol_stream) {
+  if (rec.w < 0) {
+    float* dst = C + (int64_t)rec.x * ldc + col;
+    if (accumulate && rec.w == -1) {
+      const float4 o = *reinterpret_cast<const float4*>(dst);
+      acc.x += o.x;
+      acc.y += o.y;
+      acc.z += o.z;
+      acc.w += o.w;
+    }
+    st_stream_f32x4(dst, acc, pol_stream);
+  } else {
+    *reinterpret_cast<float4*>(partial + (int64_t)rec.w * nk + col) = acc;
+  }
 }
 
 // One launch: C[:, c0 : c0 + 4L] (or the partial sums) for every virtual row.
@@ -126,7 +251,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
     const int len = rec.z;
     const int* ix = idx + rec.y;
     const float* vx = val + rec.y;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 acc = vrow_init(rec, C, ldc, col, active);
     for (int t = 0; t < len; t += NB) {
       int j[PER];
       float a[PER];
@@ -159,19 +284,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
       }
     }
     if (!active) continue;
-    if (rec.w < 0) {
-      float* dst = C + (int64_t)rec.x * ldc + col;
-      if (accumulate) {
-        const float4 o = *reinterpret_cast<const float4*>(dst);
-        acc.x += o.x;
-        acc.y += o.y;
-        acc.z += o.z;
-        acc.w += o.w;
-      }
-      st_stream_f32x4(dst, acc, pol_stream);
-    } else {
-      *reinterpret_cast<float4*>(partial + (int64_t)rec.w * nk + col) = acc;
-    }
+    vrow_store(rec, acc, C, ldc, col, nk, accumulate, partial, pol_stream);
   }
 }
 
@@ -214,7 +327,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
     const int len = rec.z;
     const int* ix = idx + rec.y;
     const float* vx = val + rec.y;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 acc = vrow_init(rec, C, ldc, col, active);
     for (int t = 0; t < len; t += NB) {
       int j[PER];
       float a[PER];
@@ -265,19 +378,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
       }
     }
     if (!active) continue;
-    if (rec.w < 0) {
-      float* dst = C + (int64_t)rec.x * ldc + col;
-      if (accumulate) {
-        const float4 o = *reinterpret_cast<const float4*>(dst);
-        acc.x += o.x;
-        acc.y += o.y;
-        acc.z += o.z;
-        acc.w += o.w;
-      }
-      st_stream_f32x4(dst, acc, pol_stream);
-    } else {
-      *reinterpret_cast<float4*>(partial + (int64_t)rec.w * nk + col) = acc;
-    }
+    vrow_store(rec, acc, C, ldc, col, nk, accumulate, partial, pol_stream);
   }
 }
 
@@ -346,7 +447,7 @@ __global__ void vrow_fixup_rows_k(int64_t nlong, int64_t nk, const int4* __restr
 static inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 template <class PtrT>
-static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s,
+static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, int P, VrowSchedule* out, cudaStream_t s,
                         bool pooled) {
   const int64_t nrows = A->nrows;
   const PtrT* ptr = (const PtrT*)A->ptr;
@@ -359,11 +460,13 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   void* cub_tmp = nullptr;
   char* tmp = nullptr;
   char* mem = nullptr;
+  unsigned long long* band_cnt = nullptr;
   size_t cub_bytes = 0, b2 = 0;
   cudaError_t e = cudaSuccess;
   auto release = [&](bool keep_schedule) {
     for (void* q : {(void*)cnt_v, (void*)cnt_l, (void*)voff, (void*)loff, (void*)cnt_s, (void*)cnt_g,
-                    (void*)cnt_ss, (void*)soff, (void*)goff, (void*)ssoff, cub_tmp, (void*)tmp})
+                    (void*)cnt_ss, (void*)soff, (void*)goff, (void*)ssoff, cub_tmp, (void*)tmp,
+                    (void*)band_cnt})
       if (q) cudaFreeAsync(q, s);
     if (!keep_schedule && mem) {
       if (pooled) cudaFreeAsync(mem, s);
@@ -383,8 +486,14 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   if ((e = cudaMallocAsync((void**)&loff, rows_bytes, s)) != cudaSuccess) return fail("alloc");
   for (int64_t** q : {&cnt_s, &cnt_g, &cnt_ss, &soff, &goff, &ssoff})
     if ((e = cudaMallocAsync((void**)q, rows_bytes, s)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMallocAsync((void**)&band_cnt, sizeof(unsigned long long) * VR_MAX_BANDS, s)) != cudaSuccess)
+    return fail("alloc");
+  cudaMemsetAsync(band_cnt, 0, sizeof(unsigned long long) * VR_MAX_BANDS, s);
   for (int64_t* q : {cnt_v, cnt_l, cnt_s, cnt_g, cnt_ss}) cudaMemsetAsync(q + nrows, 0, sizeof(int64_t), s);
-  vrow_count_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, T, cnt_v, cnt_l, cnt_s, cnt_g, cnt_ss);
+  const int64_t W = (A->ncols + P - 1) / P;  // columns per band
+  const int* idx = (const int*)A->idx;
+  vrow_count_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, idx, A->index_base, T, P, W, cnt_v, cnt_l, cnt_s, cnt_g,
+                                          cnt_ss, band_cnt);
   cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, cnt_v, voff, nrows + 1, s);
   if ((e = cudaMallocAsync(&cub_tmp, cub_bytes, s)) != cudaSuccess) return fail("alloc");
   if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt_v, voff, nrows + 1, s)) != cudaSuccess)
@@ -395,8 +504,10 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
     if ((e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnts[q], offs[q], nrows + 1, s)) != cudaSuccess)
       return fail("scan");
   int64_t tot[5] = {0, 0, 0, 0, 0};
+  unsigned long long bcnt[VR_MAX_BANDS] = {};
   for (int q = 0; q < 5; ++q)
     cudaMemcpyAsync(&tot[q], offs[q] + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(bcnt, band_cnt, sizeof(bcnt), cudaMemcpyDeviceToHost, s);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail("count");
   const int64_t nv = tot[0], nl = tot[1], nseg = tot[2], nlong = tot[3], nss = tot[4];
   if (nv > INT32_MAX || nl > INT32_MAX) {
@@ -418,6 +529,9 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   out->nv = nv;
   out->nl = nl;
   out->T = T;
+  out->nbands = P;
+  out->band_off[0] = 0;
+  for (int b = 0; b < P; ++b) out->band_off[b + 1] = out->band_off[b] + (int64_t)bcnt[b];
   const size_t tmp_bytes = a256(nv) * 2 + a256(4 * nv) * 2 + a256(16 * nv);
   if ((e = cudaMallocAsync((void**)&tmp, tmp_bytes, s)) != cudaSuccess) return fail("alloc");
   uint8_t* key = (uint8_t*)tmp;
@@ -425,17 +539,18 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   int32_t* ord = (int32_t*)(tmp + 2 * a256(nv));
   int32_t* ord2 = (int32_t*)(tmp + 2 * a256(nv) + a256(4 * nv));
   int4* unsorted = (int4*)(tmp + 2 * a256(nv) + 2 * a256(4 * nv));
-  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, A->index_base, T, voff, loff, soff, goff, ssoff, key, ord,
-                                         unsorted, out->seg, out->lrow);
+  vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, idx, A->index_base, T, P, W, voff, loff, soff, goff, ssoff,
+                                         key, ord, unsorted, out->seg, out->lrow);
+  const int end_bit = P > 1 ? 8 : 4;  // key: band << 4 | length class
   b2 = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, 4, s);
+  cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, end_bit, s);
   if (b2 > cub_bytes) {
     cudaFreeAsync(cub_tmp, s);
     cub_tmp = nullptr;
     if ((e = cudaMallocAsync(&cub_tmp, b2, s)) != cudaSuccess) return fail("alloc");
     cub_bytes = b2;
   }
-  e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, key, key2, ord, ord2, (int)nv, 0, 4, s);
+  e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, key, key2, ord, ord2, (int)nv, 0, end_bit, s);
   if (e == cudaSuccess) {
     vrow_gather_k<<<grid_for(nv, 256, ctx->num_sms), 256, 0, s>>>(nv, ord2, unsorted, out->vr);
     e = cudaGetLastError();
@@ -445,14 +560,19 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* 
   return FGB_OK;
 }
 
-int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s, bool pooled) {
+int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cudaStream_t s, bool pooled,
+               int bands) {
   *out = VrowSchedule{};
   if (A->orient != FGB_CSR) return set_error(FGB_EUNSUPPORTED, "vrow schedule: CSR only");
   if (T < 8 || T > 4096) return set_error(FGB_EINVAL, "vrow schedule: chunk %d outside [8, 4096]", T);
+  if (bands < 1 || bands > VR_MAX_BANDS)
+    return set_error(FGB_EINVAL, "vrow schedule: %d column bands outside [1, %d]", bands, VR_MAX_BANDS);
+  if (bands > 1 && A->idx_t != FGB_I32)
+    return set_error(FGB_EUNSUPPORTED, "vrow schedule: column bands need int32 indices");
   if (A->nrows > INT32_MAX || A->nnz > INT32_MAX)
     return set_error(FGB_EUNSUPPORTED, "vrow schedule: needs fewer than 2^31 rows and entries");
-  return A->ptr_t == FGB_I32 ? vrow_build_t<int32_t>(ctx, A, T, out, s, pooled)
-                             : vrow_build_t<int64_t>(ctx, A, T, out, s, pooled);
+  return A->ptr_t == FGB_I32 ? vrow_build_t<int32_t>(ctx, A, T, bands, out, s, pooled)
+                             : vrow_build_t<int64_t>(ctx, A, T, bands, out, s, pooled);
 }
 
 void vrow_free(VrowSchedule* v, cudaStream_t s) {
@@ -483,11 +603,18 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, VR_THREADS, smem);
     return o > 0 ? o : 1;
   }();
-  const int64_t need = (v.nv * L + VR_THREADS - 1) / VR_THREADS;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
+  // slab after slab; inside a slab, band after band (a light row's later
+  // bands add to what its earlier bands wrote)
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
-    kern<<<grid, VR_THREADS, smem, s>>>(v.nv, v.vr, (const int*)A->idx, (const float*)A->val, B, (LdT)ldb, C,
-                                        ldc, c0, nk, A->index_base, accumulate, partial);
+    for (int b = 0; b < v.nbands; ++b) {
+      const int64_t nvb = v.nbands > 1 ? v.band_off[b + 1] - v.band_off[b] : v.nv;
+      if (nvb == 0) continue;
+      const int64_t need = (nvb * L + VR_THREADS - 1) / VR_THREADS;
+      const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
+      kern<<<grid, VR_THREADS, smem, s>>>(nvb, v.vr + (v.nbands > 1 ? v.band_off[b] : 0), (const int*)A->idx,
+                                          (const float*)A->val, B, (LdT)ldb, C, ldc, c0, nk, A->index_base,
+                                          accumulate, partial);
+    }
   if (v.nseg > 0) {  // segment sums live after the nl partial-sum slots
     float* segsum = partial + (int64_t)v.nl * nk;
     vrow_fixup_seg_k<<<grid_for(v.nseg * 32, 256, ctx->num_sms), 256, 0, s>>>(v.nseg, nk, v.seg, partial,

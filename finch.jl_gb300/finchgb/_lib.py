@@ -1,7 +1,7 @@
 """ctypes binding of libfinchgb.so, the C ABI declared in include/finchgb.h.
 
-This is the same binding a Julia `ccall` layer makes:
-plain pointers, sizes and int status codes.  There is no CPU fallback: if
+This is the same binding a Julia `ccall` layer makes: plain pointers, sizes
+and int status codes.  There is no CPU fallback: if
 the shared library is missing, every entry point raises.
 """
 from __future__ import annotations
@@ -40,11 +40,13 @@ class FinchGBError(RuntimeError):
 
 
 class FgbSpmmTuning(ctypes.Structure):
-    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("path", c_int64)]
+    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("path", c_int64), ("bands", c_int32),
+                ("reserved", c_int32)]
 
 
 class FgbSddmmTuning(ctypes.Structure):
-    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("chunk", c_int64), ("slab", c_int64)]
+    _fields_ = [("lanes", c_int32), ("variant", c_int32), ("chunk", c_int64), ("slab", c_int64),
+                ("bands", c_int32), ("reserved", c_int32)]
 
 
 class FgbCgOptions(ctypes.Structure):
@@ -65,7 +67,7 @@ class FgbPlanDesc(ctypes.Structure):
 
 
 class FgbPlanInfo(ctypes.Structure):
-    _fields_ = [("lanes", c_int32), ("reserved", c_int32), ("path", c_int64),
+    _fields_ = [("lanes", c_int32), ("bands", c_int32), ("path", c_int64),
                 ("tuned_ms", c_double), ("first_candidate_ms", c_double),
                 ("candidates", c_int32), ("from_cache", c_int32), ("panels", c_int32),
                 ("variant", c_int32)]

@@ -214,14 +214,15 @@ def spmv(A: DeviceSparse, x: torch.Tensor, y: torch.Tensor | None = None,
 
 
 def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags: int = 0,
-         lanes: int = 0, path: int = 0, variant: int = 0) -> torch.Tensor:
-    """C (+)= A @ B for row-major B (n x nk); lanes/path override the schedule."""
+         lanes: int = 0, path: int = 0, variant: int = 0, bands: int = 0) -> torch.Tensor:
+    """C (+)= A @ B for row-major B (n x nk); lanes/path/variant/bands override
+    the schedule (bands: column bands of the virtual-row variants 2 and 3)."""
     nk = B.shape[1]
     if C is None:
         C = torch.empty((A.nrows, nk), dtype=B.dtype, device=B.device)
         flags &= ~L.ACCUMULATE
     d = A.desc()
-    tune = L.FgbSpmmTuning(lanes, variant, path)
+    tune = L.FgbSpmmTuning(lanes, variant, path, bands)
     L.call("fgb_spmm_ex", _ctx_for(B), ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
            C.stride(0), dtype_code(B), flags, ctypes.byref(tune), stream_ptr())
     return C
@@ -265,14 +266,15 @@ class Panels:
 
 def sddmm(A: DeviceSparse, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None,
           flags: int = 0, lanes: int = 0, chunk: int = 0, slab: int = -1,
-          variant: int = 0) -> torch.Tensor:
+          variant: int = 0, bands: int = 0) -> torch.Tensor:
     """out[e] = A.val[e] * <X[i,:], Y[j,:]> over A's stored entries
     (lanes/chunk/slab/variant override the schedule; slab 0 = all of k per
-    launch; variant 1 = virtual rows of at most `chunk` entries)."""
+    launch; variant 1 = virtual rows of at most `chunk` entries; bands:
+    column bands of the virtual-row variants)."""
     if out is None:
         out = torch.empty(A.nnz, dtype=X.dtype, device=X.device)
     d = A.desc()
-    tune = L.FgbSddmmTuning(lanes, variant, chunk, slab)
+    tune = L.FgbSddmmTuning(lanes, variant, chunk, slab, bands)
     L.call("fgb_sddmm_ex", _ctx_for(X), ctypes.byref(d), _dptr(X), X.stride(0), _dptr(Y),
            Y.stride(0), X.shape[1], _dptr(out), dtype_code(X), flags, ctypes.byref(tune),
            stream_ptr())

@@ -238,6 +238,12 @@ typedef struct fgb_spmm_tuning {
                       3: variant 2 with the gathers staged in shared memory by
                       cp.async (more warps per SM; identical results) */
   int64_t path;    /* merge-path item length (variants 2, 3: virtual-row length) */
+  int32_t bands;   /* variants 2, 3: cut A's columns into this many bands of
+                      consecutive columns (0 or 1: none, at most 8), each band's
+                      entries in launches of their own, so a launch gathers from
+                      1/bands of B's slab; a row's sum still runs over its
+                      entries in storage order, band after band */
+  int32_t reserved;
 } fgb_spmm_tuning;
 
 /* fgb_spmm with an explicit schedule (NULL = defaults).  The result does not
@@ -259,9 +265,10 @@ FGB_API int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_
  * device, held from first use until the process exits.  The schedule
  * lengthens its merge-path items until its scratch fits; a matrix whose
  * scratch exceeds the array even at the longest items (2^24 steps) is
- * rejected with FGB_EINVAL before any device work.  The first call on a device
- * looks the array's address up (cudaGetSymbolAddress) with that device
- * current, so make it before any stream capture.  All calls share the array:
+ * rejected with FGB_EINVAL before any device work.  The context's device must
+ * be the current device (FGB_EINVAL otherwise).  The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller. */
 FGB_API int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb,
                              int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags,
@@ -290,6 +297,8 @@ typedef struct fgb_sddmm_tuning {
   int32_t variant;
   int64_t chunk;
   int64_t slab;
+  int32_t bands; /* variants 1, 2: column bands of A as in fgb_spmm_tuning (0 or 1: none) */
+  int32_t reserved;
 } fgb_sddmm_tuning;
 
 FGB_API int fgb_sddmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* X, int64_t ldx,
@@ -419,7 +428,7 @@ typedef struct fgb_plan_desc {
 
 typedef struct fgb_plan_info {
   int32_t lanes;             /* chosen lanes per fiber / row group / entry */
-  int32_t reserved;
+  int32_t bands;             /* SpMM/SDDMM virtual rows: column bands (1 = none) */
   int64_t path;              /* chosen merge-path item (SpMM) or entry chunk (SDDMM) */
   double tuned_ms;           /* time of the chosen schedule (-1 if not tuned) */
   double first_candidate_ms; /* time of the first schedule tried */

@@ -1,7 +1,6 @@
 """Extracts known-answer tests from Finch.jl's own test fixtures.
 
-Reads (text only) the reference checkout given as argv[1] (default
-/root/reference) and writes tests/golden/finch_kats.json plus the
+Reads (text only) the Finch.jl checkout given as the one argument and writes tests/golden/finch_kats.json plus the
 MatrixMarket test matrices as tests/golden/mtx_<name>.npz.  Every value in
 the JSON is parsed out of the file named beside it; nothing is typed in by
 hand.  Run once where the reference is mounted; the outputs are committed so
@@ -127,4 +126,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of a Finch.jl checkout>")
+    main(Path(sys.argv[1]))

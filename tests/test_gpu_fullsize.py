@@ -45,40 +45,72 @@ def zipf():
 
 
 def test_spmm_headline_full_size(gpu_lib, zipf):
+    """The headline SpMM, all 1M x 128 outputs, against the oracle's row nest
+    run in FP64 (only the GPU's FP32 rounding is tolerated), for the plan's
+    banded schedule, the unbanded slab schedule and the merge path."""
     A_h, B_h = zipf
     A, B = upload(A_h), torch.from_numpy(B_h).cuda()
-    C3 = to_host(dev.spmm(A, B, lanes=8, path=128, variant=3))  # the headline schedule
-    assert np.array_equal(C3, to_host(dev.spmm(A, B, lanes=8, path=128, variant=3)))  # deterministic
-    assert np.array_equal(C3, to_host(dev.spmm(A, B, lanes=8, path=128, variant=2)))  # register gathers
-    Cm = to_host(dev.spmm(A, B))  # merge-path schedule: another summation order
-    rows = sample_rows(A_h, np.random.default_rng(1))
-    sub = rows_of(A_h, rows)
-    B64 = B_h.astype(np.float64)  # the oracle in FP64: only the GPU's FP32 rounding is tolerated
-    want = oracle.spmm_csr(sub.nrows, sub.ncols, sub.ptr, sub.idx, sub.val.astype(np.float64), B64,
-                           nthreads=oracle.max_threads())
-    scale = oracle.spmm_csr(sub.nrows, sub.ncols, sub.ptr, sub.idx, np.abs(sub.val).astype(np.float64),
-                            np.abs(B64), nthreads=oracle.max_threads())
-    tol = RTOL[np.dtype(np.float32)] * scale.astype(np.float64) + 1e-30
-    for got in (C3[rows], Cm[rows]):
-        assert (np.abs(got.astype(np.float64) - want) <= tol).all()
+    Cb = to_host(dev.spmm(A, B, lanes=8, path=128, variant=3, bands=4))  # column bands
+    assert np.array_equal(Cb, to_host(dev.spmm(A, B, lanes=8, path=128, variant=3, bands=4)))  # deterministic
+    assert np.array_equal(Cb, to_host(dev.spmm(A, B, lanes=8, path=128, variant=2, bands=4)))  # register gathers
+    C3 = to_host(dev.spmm(A, B, lanes=8, path=128, variant=3))  # unbanded slabs
+    assert np.array_equal(C3, to_host(dev.spmm(A, B, lanes=8, path=128, variant=2)))
+    Cm = to_host(dev.spmm(A, B))  # the per-call default schedule
+    B64 = B_h.astype(np.float64)
+    nt = oracle.max_threads()
+    want = oracle.spmm_csr(A_h.nrows, A_h.ncols, A_h.ptr, A_h.idx, A_h.val.astype(np.float64), B64, nthreads=nt)
+    np.abs(B64, out=B64)
+    scale = oracle.spmm_csr(A_h.nrows, A_h.ncols, A_h.ptr, A_h.idx, np.abs(A_h.val).astype(np.float64), B64,
+                            nthreads=nt)
+    del B64
+    tol = RTOL[np.dtype(np.float32)] * scale + 1e-30
+    for name, got in (("banded", Cb), ("slabs", C3), ("default", Cm)):
+        err = np.abs(got.astype(np.float64) - want)
+        assert (err <= tol).all(), f"{name}: {int((err > tol).sum())} of {err.size} outside tolerance"
 
 
 def test_sddmm_full_size(gpu_lib, zipf):
+    """All 16M SDDMM outputs against an FP64 evaluation of A .* (X Y^T)."""
     A_h, _ = zipf
     rng = np.random.default_rng(SEED + 1)
     X = rng.standard_normal((1_000_000, 64), dtype=np.float32)
     Y = rng.standard_normal((1_000_000, 64), dtype=np.float32)
     A, Xd, Yd = upload(A_h), torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
-    o2 = to_host(dev.sddmm(A, Xd, Yd, chunk=256, variant=2, slab=32))  # the plan's choice
+    o2 = to_host(dev.sddmm(A, Xd, Yd, chunk=256, variant=2, slab=32))
     assert np.array_equal(o2, to_host(dev.sddmm(A, Xd, Yd, chunk=256, variant=1, slab=32)))
-    e = np.random.default_rng(2).choice(A_h.nnz, 200_000, replace=False)
-    rows = np.searchsorted(A_h.ptr - 1, e, side="right") - 1
-    cols = A_h.idx[e] - 1
-    dots = np.einsum("ij,ij->i", X[rows].astype(np.float64), Y[cols].astype(np.float64))
-    want = A_h.val[e].astype(np.float64) * dots
-    scale = np.abs(A_h.val[e]) * np.einsum("ij,ij->i", np.abs(X[rows]).astype(np.float64),
-                                           np.abs(Y[cols]).astype(np.float64))
-    assert (np.abs(o2[e] - want) <= RTOL[np.dtype(np.float32)] * scale + 1e-30).all()
+    assert np.array_equal(o2, to_host(dev.sddmm(A, Xd, Yd, chunk=256, variant=2, slab=32, bands=4)))
+    nt = oracle.max_threads()
+    want = oracle.sddmm_csr(A_h.nrows, A_h.ptr, A_h.idx, A_h.val, X, Y, acc64=True, nthreads=nt)
+    scale = oracle.sddmm_csr(A_h.nrows, A_h.ptr, A_h.idx, np.abs(A_h.val), np.abs(X), np.abs(Y), acc64=True,
+                             nthreads=nt)
+    err = np.abs(o2.astype(np.float64) - want)
+    assert (err <= RTOL[np.dtype(np.float32)] * scale + 1e-30).all()
+
+
+def test_spmv_config1_full_size(gpu_lib):
+    """SpMV y[i] += A[i,j]*x[j] at its full size: A 10,000 x 10,000 CSC from
+    fsprand(0.001), FP64, seeded as the benchmark seeds it.  The push over
+    columns (atomics) lies within the FP64 tolerance of Finch's serial CSC
+    nest; the pull in Finch's order equals that nest bit for bit, fused and
+    unfused."""
+    from finchgb.workloads import fsprand
+
+    rng = np.random.default_rng(SEED + 1)
+    n = 10_000
+    b = fsprand(rng, n, n, 0.001)
+    x = rng.random(n)
+    Ad = upload(b)
+    Ar = Ad.transposed_storage()
+    xd = torch.from_numpy(x).cuda()
+    want_f = oracle.spmv_csc(oracle.SR_PT, n, n, b.ptr, b.idx, b.val, x, fma=True)
+    want_u = oracle.spmv_csc(oracle.SR_PT, n, n, b.ptr, b.idx, b.val, x, fma=False)
+    scale = oracle.spmv_csc(oracle.SR_PT, n, n, b.ptr, b.idx, np.abs(b.val), np.abs(x))
+    push = to_host(dev.spmv(Ad, xd))
+    assert (np.abs(push - want_f) <= RTOL[np.dtype(np.float64)] * scale + 1e-300).all()
+    pull = to_host(dev.spmv(Ar, xd))
+    assert (np.abs(pull - want_f) <= RTOL[np.dtype(np.float64)] * scale + 1e-300).all()
+    assert to_host(dev.spmv(Ar, xd, flags=L.FINCH_ORDER | L.FMA)).tobytes() == want_f.tobytes()
+    assert to_host(dev.spmv(Ar, xd, flags=L.FINCH_ORDER | L.NO_FMA)).tobytes() == want_u.tobytes()
 
 
 @pytest.fixture(scope="module")
