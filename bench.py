@@ -69,14 +69,18 @@ def load_peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def load_traffic() -> tuple[int | None, str | None]:
-    """Per-step DRAM bytes of the SpMM kernels from the committed ncu summary."""
-    p = ROOT / "profiles" / "spmm_vrow_zipf1M_k128.md"
-    if not p.exists():
-        return None, None
-    for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_step:"):
-            return int(float(line.split(":", 1)[1].strip())), str(p.relative_to(ROOT))
+def load_traffic(schedule: str) -> tuple[int | None, str | None]:
+    """Per-step DRAM bytes of the SpMM kernels from the committed ncu summary
+    of the same schedule (None when the run chose a schedule no summary
+    covers).  `schedule` is "lanes=L path=T variant=V bands=P"."""
+    for p in sorted((ROOT / "profiles").glob("spmm_*zipf1M_k128*.md")):
+        lines = p.read_text().splitlines()
+        sched = [ln.split(":", 1)[1].strip() for ln in lines if ln.startswith("schedule:")]
+        if not sched or sched[0] != schedule:
+            continue
+        for line in lines:
+            if line.startswith("traffic_bytes_per_step:"):
+                return int(float(line.split(":", 1)[1].strip())), str(p.relative_to(ROOT))
     return None, None
 
 
@@ -142,7 +146,7 @@ def cpu_reference_pass(A, B, threads: int) -> float:
 
     C = np.empty((A.nrows, NK), dtype=np.float32)
     t0 = time.perf_counter()
-    oracle.spmm_csr(A.nrows, A.ncols, A.ptr, A.idx, A.val, B, C=C, nthreads=threads)
+    oracle.spmm_csr(A.nrows, A.ncols, A.ptr, A.idx, A.val, B, C=C, nthreads=threads, fast=True)
     return time.perf_counter() - t0
 
 
@@ -157,8 +161,8 @@ def cpu_baseline(A, B, nbytes: int, min_seconds: float = 10.0, max_passes: int =
     t = statistics.median(times)
     return {"value": round(nbytes / t / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"whole matrix, {len(times)} passes ({sum(times):.1f} s) of Finch's "
-                      f"row-parallel SpMM nest (oracle C restatement, static split), median "
-                      f"{1e3 * t:.1f} ms"}
+                      f"row-parallel SpMM nest (oracle C restatement, static split, built "
+                      f"-O3 -ffast-math -funroll-loops), median {1e3 * t:.1f} ms"}
 
 
 def run_reference(args):
@@ -178,12 +182,14 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "spmm_gbps_algorithmic", "value": round(value, 3),
             "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": workload_name(args.rows), "parallelism": f"cpu{threads}"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": workload_name(args.rows), "nnz": int(A.nnz), "k": NK,
+                       "algorithmic_bytes_per_step": nbytes, "parallelism": f"cpu{threads}"},
             "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                              "kind": "port",
                              "sample": "whole matrix per step: Finch's row-parallel SpMM nest "
-                                       "(oracle C restatement, static split)"},
+                                       "(oracle C restatement, static split, built -O3 -ffast-math "
+                                       "-funroll-loops)"},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -213,6 +219,157 @@ def autotune(A, B, C, reps: int = 3, verbose: bool = False):
                       file=sys.stderr)
     best = min(table, key=table.get)
     return best, table
+
+
+def rows_of(A, rows: np.ndarray):
+    """The CSR sub-matrix of the given rows (host, 1-based buffers)."""
+    from finchgb.workloads import SparseBuffers
+
+    lens = (A.ptr[rows + 1] - A.ptr[rows]).astype(np.int64)
+    ptr = np.concatenate([[1], 1 + np.cumsum(lens)]).astype(np.int64)
+    sel = np.concatenate([np.arange(A.ptr[r] - 1, A.ptr[r + 1] - 1) for r in rows])
+    return SparseBuffers(len(rows), A.ncols, ptr, A.idx[sel], A.val[sel], "csr")
+
+
+def spmm_fp64_error(A_h, B_h, C_host: np.ndarray, n: int = 4000, longest: int = 20) -> dict:
+    """max |gpu - FP64 oracle| / sum_j |A[i,j] B[j,k]| over sampled rows of C
+    (the longest rows included), every column."""
+    import oracle
+
+    lens = np.diff(A_h.ptr)
+    rng = np.random.default_rng(SEED + 99)
+    rows = np.unique(np.concatenate([rng.choice(A_h.nrows, n, replace=False), np.argsort(lens)[-longest:]]))
+    sub = rows_of(A_h, rows)
+    nt = oracle.max_threads()
+    B64 = B_h.astype(np.float64)
+    want = oracle.spmm_csr(sub.nrows, sub.ncols, sub.ptr, sub.idx, sub.val.astype(np.float64), B64, nthreads=nt)
+    scale = oracle.spmm_csr(sub.nrows, sub.ncols, sub.ptr, sub.idx, np.abs(sub.val).astype(np.float64),
+                            np.abs(B64), nthreads=nt)
+    err = np.abs(C_host[rows].astype(np.float64) - want)
+    rel = np.where(scale > 0, err / np.where(scale > 0, scale, 1.0), np.where(err > 0, np.inf, 0.0))
+    return {"max_rel_err_vs_fp64": float(rel.max()), "tolerance": 2e-5,
+            "norm": "|gpu - fp64| / sum_j |A[i,j] B[j,k]|",
+            "checked": f"{rows.size} rows ({longest} longest, {int(lens[rows].sum())} stored entries) x {NK} columns"}
+
+
+def e2e_api(A_h, B_h, nbytes: int, steps: int) -> dict:
+    """The plugin API end to end: host Finch tensors in, compute(lazy(A) @
+    lazy(B)) (transfer, matcher, fgb_spmm), host C out, every step."""
+    import torch
+
+    import finchgb as F
+    from finchgb.workloads import SparseBuffers
+
+    fmtA = F.Dense(F.SparseList(F.Element(np.float32(0.0))))
+    fmtB = F.Dense(F.Dense(F.Element(np.float32(0.0))))
+    At = SparseBuffers(A_h.ncols, A_h.nrows, A_h.ptr, A_h.idx, A_h.val, "csc")  # CSC of A^T = CSR of A
+
+    def one():
+        A = F.swizzle(F.Tensor.from_buffers(fmtA, At), 2, 1)  # fresh host tensors: every step uploads
+        B = F.Tensor(fmtB, B_h)
+        return F.compute(F.lazy(A) @ F.lazy(B)).todense()
+
+    C = one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        C = one()
+    dt = (time.perf_counter() - t0) / steps
+    h2d = A_h.ptr.nbytes + A_h.idx.nbytes + A_h.val.nbytes + B_h.nbytes
+    return {"value": round(nbytes / dt / 1e9, 1), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(C.nbytes), "steps": steps, "ms_per_step": round(1e3 * dt, 3),
+            "call": "compute(lazy(swizzle(Tensor(Dense(SparseList(Element(0f))), A^T), 2, 1)) @ "
+                    "lazy(Tensor(Dense(Dense(Element(0f))), B))).todense()",
+            "timing": "host wall clock per call (synchronous), Finch's Int64 ptr/idx uploaded and narrowed"}, C
+
+
+def suite_block(A_h, Ad) -> dict:
+    """Compact lines for the other configurations: SDDMM (k = 64) on the
+    headline matrix, 20 Bellman-Ford min-plus rounds on the 4M-node graph,
+    and mixed-precision CG on the 2048^2 Poisson matrix."""
+    import torch
+
+    import oracle
+    from finchgb import _lib as L
+    from finchgb import cg
+    from finchgb import device as dev
+    from finchgb.plan import Plan
+    from finchgb.workloads import poisson2d, random_graph
+
+    out = {}
+    m = A_h.nrows
+    rng = np.random.default_rng(SEED + 1)
+    X = rng.standard_normal((m, 64), dtype=np.float32)
+    Y = rng.standard_normal((m, 64), dtype=np.float32)
+    Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+    o = torch.empty(A_h.nnz, dtype=torch.float32, device="cuda")
+    plan = Plan.sddmm(Ad, Xd, Yd, o, tune_reps=3)
+    ms = _timed_ms(plan.execute, reps=10)
+    nbytes = 4 * (m + 1) + 8 * A_h.nnz + 2 * 4 * m * 64 + 4 * A_h.nnz
+    e = np.random.default_rng(2).choice(A_h.nnz, 200_000, replace=False)
+    rows = np.searchsorted(A_h.ptr - 1, e, side="right") - 1
+    cols = A_h.idx[e] - 1
+    oh = o.cpu().numpy()
+    want = A_h.val[e].astype(np.float64) * np.einsum("ij,ij->i", X[rows].astype(np.float64), Y[cols].astype(np.float64))
+    scl = np.abs(A_h.val[e]).astype(np.float64) * np.einsum("ij,ij->i", np.abs(X[rows]).astype(np.float64),
+                                                             np.abs(Y[cols]).astype(np.float64))
+    rel = np.abs(oh[e] - want) / np.maximum(scl, 1e-300)
+    out["sddmm_1M_k64"] = {"metric": "sddmm_gbps_algorithmic", "value": round(nbytes / (ms / 1e3) / 1e9, 1),
+                           "unit": "GB/s", "ms_per_call": round(ms, 4), "roofline": _roof(nbytes, ms),
+                           "schedule": plan.info(), "max_rel_err_vs_fp64": float(rel.max()),
+                           "checked": "200,000 sampled entries, |gpu - fp64| / sum_k |a x_ik y_jk|"}
+    del Xd, Yd, o, plan
+    # Bellman-Ford: 20 min-plus rounds, pull over a CSR copy, autotuned plan
+    g = random_graph(np.random.default_rng(SEED + 3), 4_000_000, 8.0)
+    n = g.nrows
+    Gd = dev.DeviceSparse.from_host(n, n, g.ptr, g.idx, g.val, orient="csc")
+    Gr = Gd.transposed_storage()
+    x0 = torch.full((n,), 2**30, dtype=torch.int32, device="cuda")
+    x0[0] = 0
+    xp, yp = x0.clone(), torch.empty_like(x0)
+    pmp = Plan.spmv(Gr, xp, yp, semiring=L.MIN_PLUS)
+
+    def rounds():
+        xp.copy_(x0)
+        for _ in range(20):
+            pmp.execute()
+            dev.dense_map(L.MAP_MIN, xp, yp, xp)
+
+    ms20 = _timed_ms(rounds, reps=3, warm=1)
+    rounds()
+    per_round = 8 * g.nnz + 4 * (n + 1) + 3 * 4 * n + 2 * 4 * n
+    # one more round against the oracle's nest on sampled rows: bit-exact (integers)
+    ptr, idx, val = Gr.to_host()
+    from finchgb.workloads import SparseBuffers
+
+    csr = SparseBuffers(n, n, ptr, idx, val, "csr")
+    xcur = xp.cpu().numpy()
+    y1 = dev.spmv(Gr, xp, semiring=L.MIN_PLUS).cpu().numpy()
+    srows = np.unique(np.random.default_rng(3).choice(n, 3000, replace=False))
+    sub = rows_of(csr, srows)
+    exact = bool(np.array_equal(y1[srows], oracle.spmv_csr(oracle.SR_MINP, sub.nrows, n, sub.ptr, sub.idx,
+                                                            sub.val, xcur)))
+    out["bellman_ford_minplus_4M"] = {
+        "metric": "minplus_round_gbps", "value": round(20 * per_round / (ms20 / 1e3) / 1e9, 1), "unit": "GB/s",
+        "ms_per_20_rounds": round(ms20, 3), "roofline": _roof(20 * per_round, ms20),
+        "lanes_per_row": pmp.info()["lanes"], "bit_exact_vs_oracle_on_3000_rows": exact}
+    del Gd, Gr, xp, yp, pmp, x0
+    # CG: FP64, FP32 and BF16 SpMV to a true relative residual of 1e-10
+    P = poisson2d(2048)
+    b = np.random.default_rng(SEED + 4).uniform(-1, 1, P.nrows)
+    Pd = dev.DeviceSparse.from_host(P.nrows, P.ncols, P.ptr, P.idx, P.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    cgl = {}
+    for prec in ("f64", "f32", "bf16"):
+        x, res = cg.cg_solve(Pd, bd, precision=prec, rtol=1e-10, max_iter=60_000)
+        vb = {"f64": 8, "f32": 4, "bf16": 2}[prec]
+        per_it = P.nnz * (4 + vb) + 4 * (P.nrows + 1) + 8 * P.nrows * 11
+        ms_it = 1e3 * res.seconds / max(res.iterations, 1)
+        cgl[prec] = {"seconds": round(res.seconds, 4), "iterations": res.iterations,
+                     "true_rel_residual": res.true_rel_residual, "converged": bool(res.converged),
+                     "ms_per_iteration": round(ms_it, 4), "roofline": _roof(per_it, ms_it)}
+    out["cg_poisson2048"] = {"metric": "cg_seconds", "unit": "s", "higher_is_better": False, **cgl}
+    return out
 
 
 def run_gpu(args):
@@ -256,20 +413,24 @@ def run_gpu(args):
         info = plan.info()
         npanels = info["panels"]
     variant = info["variant"] if plan is not None else fixed_variant
+    bands = max(1, info["bands"] if plan is not None else fixed_bands)
+    plan_path = info["path"] if plan is not None else path
     # lanes 0 in a fixed schedule is the library's own default; for this
     # workload that is the 32-column slab schedule (8 lanes)
     plan_lanes = info["lanes"] if plan is not None else (lanes if lanes > 0 else 8)
     slabs = -(-NK // (4 * plan_lanes))
     if plan is None and lanes == 0 and path == 0 and variant == 0:
         variant = 3  # the library's default for a B far larger than L2
-    if plan is None and variant in (2, 3):
+    vrow = variant in (2, 3, 4)
+    if plan is None and vrow:
         # schedule built per call: count, 5 scans (2 kernels each), fill, a
-        # 3-kernel radix sort and the gather, then the slabs and 2 fix-up passes
-        launches_per_step = 16 + slabs + 2
+        # 3-kernel radix sort and the gather, then the slab x band launches
+        # and 2 fix-up passes
+        launches_per_step = 16 + slabs * bands + 2
     elif plan is None:
         launches_per_step = 1 + slabs + 1  # merge plan + one launch per slab + carry fix-up
-    elif variant in (2, 3):  # one launch per column slab + the two partial-sum fix-up passes
-        launches_per_step = slabs + 2
+    elif vrow:  # one launch per column slab and band + the two partial-sum fix-up passes
+        launches_per_step = slabs * bands + 2
     else:  # per panel: the slab launches + fix-up (item boundaries precomputed)
         launches_per_step = npanels * (slabs + 1)
 
@@ -417,13 +578,16 @@ def run_gpu(args):
     peak, peak_kind = load_peaks()
     avg_ms = sum(step_ms) / len(step_ms)
     achieved = nbytes / (avg_ms / 1e3) / 1e9
-    traffic, traffic_src = load_traffic()
+    sched = f"lanes={plan_lanes} path={plan_path} variant={variant} bands={bands}"
+    traffic, traffic_src = load_traffic(sched)
     line["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                         "unit": "GB/s", "frac": round(achieved / peak, 4),
                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": traffic, "traffic_source": traffic_src,
-                        "kernel": (f"spmm_vrow_k x{slabs} column slabs + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 2 else
-                                   f"spmm_vrow_async_k x{slabs} column slabs + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 3 else
+                        "schedule": sched,
+                        "kernel": (f"spmm_vrow_k x{slabs} column slabs x{bands} bands + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 2 else
+                                   f"spmm_vrow_async_k x{slabs} column slabs x{bands} bands + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 3 else
+                                   f"spmm_vrow_pipe_k x{slabs} column slabs x{bands} bands + vrow_fixup_seg_k + vrow_fixup_rows_k" if variant == 4 else
                                    f"{npanels} column panels x (spmm_merge_k + spmm_fixup_k)"
                                    if plan is not None and npanels > 1 else
                                    f"spmm_merge_k x{slabs} slabs + spmm_fixup_k"),
@@ -438,19 +602,37 @@ def run_gpu(args):
     # entry and slab: nnz * NK * 4 bytes per step, from a working set of one
     # slab of B.  Its ceiling is the random-gather rate at that width and
     # working set, measured here on the same device.
-    if variant in (2, 3):
+    if vrow:
         gbytes = 16 * plan_lanes
-        ceiling = dev.gather_ceiling(A_h.ncols * gbytes, gbytes)
+        ws = -(-A_h.ncols // bands) * gbytes  # one band of one slab of B per launch
+        ceiling = dev.gather_ceiling(ws, gbytes)
         gathered = A_h.nnz * NK * 4
         g_achieved = gathered / (avg_ms / 1e3) / 1e9
         line["gather_ceiling"] = {"gathered_bytes_per_step": gathered, "gather_bytes": gbytes,
-                                  "working_set_bytes": A_h.ncols * gbytes,
+                                  "working_set_bytes": ws,
                                   "achieved": round(g_achieved, 1), "ceiling": round(ceiling, 1),
                                   "unit": "GB/s", "frac": round(g_achieved / ceiling, 4)}
+    line["clocks"] = clk.summary()
+    if rank == 0:
+        # the result of the timed steps against the oracle in FP64
+        line["max_rel_err_vs_fp64"] = spmm_fp64_error(A_h, B_h, C.cpu().numpy())
+    if rank == 0 and not args.no_e2e:
+        # the plugin API from host tensors (transfer + matcher + per-call SpMM + host result)
+        line["e2e_api"], C_api = e2e_api(A_h, B_h, nbytes, steps=max(3, min(args.steps, 8)))
+        line["e2e_api"]["max_rel_err_vs_fp64"] = spmm_fp64_error(A_h, B_h, C_api)["max_rel_err_vs_fp64"]
+        line["gpu_launches"] += line["e2e_api"]["steps"] * (16 + slabs * 2 + 2)
+        del C_api
     line["cpu_baseline"] = None
     if rank == 0 and not args.skip_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A_h, B_h, nbytes)
-    line["clocks"] = clk.summary()
+    if rank == 0 and not args.headline_only:
+        torch.cuda.empty_cache()
+        for key, fn in (("suite", lambda: suite_block(A_h, A)), ("served", served_block)):
+            try:
+                line[key] = fn()
+            except Exception as e:  # a failed block is reported, the headline stands
+                line[key] = {"error": repr(e)}
+            torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -941,6 +1123,115 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+def _serve_plan(rng, n_req, mats, partners):
+    plan = []
+    for _ in range(n_req):
+        op = ("spmv", "spmm", "masked_mul")[int(rng.integers(3))]
+        k = int(rng.integers(len(partners) if op == "masked_mul" else len(mats)))
+        plan.append((op, k, 32 if op == "spmm" else 0))
+    return plan
+
+
+def serve_check(mats, partners, n: int = 48) -> dict:
+    """Served results against the FP64 oracle: n mixed requests through the
+    batched server; SpMV/SpMM as |got - fp64| / sum|terms|, masked multiply
+    (one product per entry) exact."""
+    import torch
+
+    import oracle
+    from finchgb.server import Server
+    from finchgb.workloads import SparseBuffers
+
+    rng = np.random.default_rng(SEED + 8)
+    worst, exact = 0.0, True
+    with Server(mode="batched", pool_bytes=1 << 30, max_inflight=256) as srv:
+        ids = [srv.register(A) for A in mats]
+        pids = [srv.register(B) for B in partners]
+        todo = []
+        for q in range(n):
+            op = ("spmv", "spmm", "masked_mul")[q % 3]
+            k = int(rng.integers(len(partners) if op == "masked_mul" else len(mats)))
+            A = mats[k]
+            if op == "masked_mul":
+                out = torch.empty(A.nnz, dtype=torch.float32).pin_memory()
+                todo.append((op, k, None, out, srv.submit(op, ids[k], None, out, matrix_b=pids[k])))
+                continue
+            nk = 32 if op == "spmm" else 1
+            inp = torch.from_numpy(rng.standard_normal((A.ncols, nk), dtype=np.float32)).pin_memory()
+            out = torch.empty((A.nrows, nk), dtype=torch.float32).pin_memory()
+            if op == "spmv":
+                inp, out = inp.view(-1), out.view(-1)
+            todo.append((op, k, inp, out, srv.submit(op, ids[k], inp, out, nk=nk if op == "spmm" else 0)))
+        for op, k, inp, out, t in todo:
+            srv.wait(t)
+            ptr, idx, val = mats[k].to_host()
+            A = SparseBuffers(mats[k].nrows, mats[k].ncols, ptr, idx, val, "csr")
+            if op == "masked_mul":
+                pp, pi, pv = partners[k].to_host()
+                D = np.zeros((A.nrows, A.ncols), np.float32)
+                D[np.repeat(np.arange(A.nrows), np.diff(pp)), pi - 1] = pv
+                want = val * D[np.repeat(np.arange(A.nrows), np.diff(ptr)), idx - 1]
+                exact &= bool(np.array_equal(out.numpy(), want))
+                continue
+            X = inp.numpy().reshape(A.ncols, -1).astype(np.float64)
+            w = oracle.spmm_csr(A.nrows, A.ncols, A.ptr, A.idx, A.val.astype(np.float64), X)
+            sc = oracle.spmm_csr(A.nrows, A.ncols, A.ptr, A.idx, np.abs(A.val).astype(np.float64), np.abs(X))
+            err = np.abs(out.numpy().reshape(A.nrows, -1) - w) / np.maximum(sc, 1e-300)
+            worst = max(worst, float(err.max()))
+    return {"requests": n, "max_rel_err_vs_fp64": worst, "masked_mul_exact": exact,
+            "norm": "|served - fp64| / sum_j |A[i,j] x[j]|"}
+
+
+def served_block(min_seconds: float = 1.0) -> dict:
+    """Configuration 5 inside the default run: closed-loop capacity of the
+    batched server and of the plain per-call path (at least min_seconds of
+    requests each), then Poisson arrivals at the same rates for both modes
+    (half and nine tenths of the per-call capacity) and at half the batched
+    capacity for the batched mode, p50/p99 of each; clocks sampled; a sample
+    of served results against the FP64 oracle."""
+    import torch
+
+    mats, partners = serve_library()
+    rng = np.random.default_rng(SEED + 6)
+    arena = torch.empty(512 << 20, dtype=torch.float32).pin_memory()  # 2 GiB ring
+    window = 4096
+    out = {"mix": "1/3 SpMV, 1/3 SpMM(32), 1/3 masked multiply", "matrices": len(mats),
+           "stored_entries": int(sum(A.nnz for A in mats)), "closed_loop_in_flight": window,
+           "config": {"workload": "4096 CSR, rows log-uniform [64, 8192], square, density U[0.5%, 5%], FP32 N(0,1)"}}
+
+    def lat_stats(lat):
+        return {"p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3)}
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        cap = {}
+        for mode, n0 in (("batched", 400_000), ("per_call", 40_000)):
+            plan = _serve_plan(rng, n0, mats, partners)
+            dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
+            if dt < min_seconds:  # too short: again with enough requests
+                plan = _serve_plan(rng, int(n0 * 1.3 * min_seconds / dt), mats, partners)
+                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
+            cap[mode] = len(plan) / dt
+            out[mode] = {"closed_loop": {"ops_per_s": round(cap[mode], 1), "requests": len(plan),
+                                         "seconds": round(dt, 3), **lat_stats(lat),
+                                         "launches": st["launches"]}}
+        out["throughput_ratio_batched_vs_per_call"] = round(cap["batched"] / cap["per_call"], 2)
+        rates = [("0.5x_per_call_capacity", 0.5 * cap["per_call"], ("batched", "per_call")),
+                 ("0.9x_per_call_capacity", 0.9 * cap["per_call"], ("batched", "per_call")),
+                 ("0.5x_batched_capacity", 0.5 * cap["batched"], ("batched",))]
+        for name, lam, modes in rates:
+            n_req = max(5000, int(lam * 1.2 * min_seconds))
+            plan = _serve_plan(rng, n_req, mats, partners)
+            arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
+            for mode in modes:
+                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr)
+                out[mode][f"poisson_{name}"] = {"rate_per_s": round(lam, 1), "requests": n_req,
+                                                "seconds": round(dt, 3), **lat_stats(lat)}
+    out["clocks"] = clk.summary()
+    out["oracle_check"] = serve_check(mats, partners)
+    return out
+
+
 def suite_coo() -> list[dict]:
     """fsparse assembly in HBM: 16M random (row, col) Int64 triplets, FP32
     values, about 0.01 % duplicates, into a 1M x 1M Dense(SparseList)."""
@@ -1039,6 +1330,8 @@ def main():
                     help="rows = columns of A (16 stored entries per row on average)")
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="only the SpMM line: no suite or served blocks")
     ap.add_argument("--sweep", action="store_true", help="print the autotune table to stderr")
     ap.add_argument("--schedule", default="", help="fixed LANES,PATH instead of the autotune")
     ap.add_argument("--suite", action="store_true",

@@ -289,10 +289,10 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
   const int bands = tune ? tune->bands : 0;
   if (variant < 0 || variant > 3) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1, 2 or 3");
   if (bands < 0 || bands > 8) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: bands must be in [0, 8]");
-  if (bands > 1 && variant != 2 && variant != 3)
+  if (bands > 1 && variant < 2)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: column bands need variant 2 or 3");
-  if (variant == 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
-    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant 2 takes lanes 2, 4 or 8");
+  if (variant >= 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variants 2 and 3 take lanes 2, 4 or 8");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
   if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");

@@ -157,7 +157,10 @@ __global__ void vrow_fill_k(int64_t nrows, const PtrT* __restrict__ ptr, const i
     int64_t c = 0;  // virtual rows written so far
     auto emit = [&](int b, int64_t first, int64_t clen, int w) {
       const int64_t v = v0 + c;
-      key[v] = (uint8_t)((b << 4) | vrow_class(clen));
+      // band, then the records that continue C (w = -2) after all others,
+      // then length class: a launch reaches the records that need the
+      // previous launch's C last (programmatic dependent launch)
+      key[v] = (uint8_t)((b << 5) | (w == -2 ? 16 : 0) | vrow_class(clen));
       ord[v] = (int32_t)v;
       unsorted[v] = make_int4((int)r, (int)(b0 + first), (int)clen, w);
       ++c;
@@ -196,6 +199,16 @@ __global__ void vrow_gather_k(int64_t nv, const int32_t* __restrict__ ord,
        i += (int64_t)gridDim.x * blockDim.x)
     vr[i] = unsorted[ord[i]];
 }
+
+// Programmatic dependent launch: the launches of one SpMM after its first
+// may start while the previous one drains (its blocks take the SMs the
+// previous launch frees).  A launch signals at once that its successor may
+// start, waits for its predecessor before its first record that reads C
+// (w = -2, sorted last) and before it exits, so a launch that completes
+// implies that every earlier one did.  In a launch made without the
+// attribute both instructions return at once.
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // The start of a virtual row: a light row's later column band (w = -2)
 // continues the running sum its earlier bands left in C, so the row is one
@@ -246,8 +259,14 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
   const float* Bc = B + col;
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
+  pdl_allow_next();
+  bool waited = false;
   for (int64_t v = gid; v < nv; v += ngroups) {
     const int4 rec = __ldg(vr + v);  // row, first entry, length, partial slot
+    if (rec.w == -2 && !waited) {
+      pdl_wait_prev();
+      waited = true;
+    }
     const int len = rec.z;
     const int* ix = idx + rec.y;
     const float* vx = val + rec.y;
@@ -286,6 +305,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_k(
     if (!active) continue;
     vrow_store(rec, acc, C, ldc, col, nk, accumulate, partial, pol_stream);
   }
+  if (!waited) pdl_wait_prev();  // completion of this launch implies its predecessor's
 }
 
 // The same launch with the gathers staged in shared memory by cp.async
@@ -322,8 +342,14 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
   float4* slot = vr_stage + threadIdx.x;
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
+  pdl_allow_next();
+  bool waited = false;
   for (int v = gid; v < nv; v += ngroups) {
     const int4 rec = __ldg(vr + v);
+    if (rec.w == -2 && !waited) {
+      pdl_wait_prev();
+      waited = true;
+    }
     const int len = rec.z;
     const int* ix = idx + rec.y;
     const float* vx = val + rec.y;
@@ -380,6 +406,7 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
     if (!active) continue;
     vrow_store(rec, acc, C, ldc, col, nk, accumulate, partial, pol_stream);
   }
+  if (!waited) pdl_wait_prev();  // completion of this launch implies its predecessor's
 }
 
 // Sums `n` partial-sum slots starting at `p` (rows of nk floats) in slot
@@ -541,7 +568,7 @@ static int vrow_build_t(fgb_ctx* ctx, const fgb_sparse* A, int T, int P, VrowSch
   int4* unsorted = (int4*)(tmp + 2 * a256(nv) + 2 * a256(4 * nv));
   vrow_fill_k<PtrT><<<grid, 256, 0, s>>>(nrows, ptr, idx, A->index_base, T, P, W, voff, loff, soff, goff, ssoff,
                                          key, ord, unsorted, out->seg, out->lrow);
-  const int end_bit = P > 1 ? 8 : 4;  // key: band << 4 | length class
+  const int end_bit = P > 1 ? 8 : 4;  // key: band << 5 | continues-C << 4 | length class
   b2 = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, b2, key, key2, ord, ord2, (int)nv, 0, end_bit, s);
   if (b2 > cub_bytes) {
@@ -604,16 +631,30 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
     return o > 0 ? o : 1;
   }();
   // slab after slab; inside a slab, band after band (a light row's later
-  // bands add to what its earlier bands wrote)
+  // bands continue what its earlier bands wrote).  Every launch after the
+  // first may start while its predecessor drains (programmatic dependent
+  // launch); the first waits for whatever the stream ran before.
+  cudaLaunchAttribute pdl[1];
+  pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl[0].val.programmaticStreamSerializationAllowed = 1;
+  bool first = true;
   for (int64_t c0 = 0; c0 < nk; c0 += 4 * L)
     for (int b = 0; b < v.nbands; ++b) {
       const int64_t nvb = v.nbands > 1 ? v.band_off[b + 1] - v.band_off[b] : v.nv;
       if (nvb == 0) continue;
       const int64_t need = (nvb * L + VR_THREADS - 1) / VR_THREADS;
       const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)occ * ctx->num_sms));
-      kern<<<grid, VR_THREADS, smem, s>>>(nvb, v.vr + (v.nbands > 1 ? v.band_off[b] : 0), (const int*)A->idx,
-                                          (const float*)A->val, B, (LdT)ldb, C, ldc, c0, nk, A->index_base,
-                                          accumulate, partial);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid);
+      cfg.blockDim = dim3(VR_THREADS);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cfg.attrs = first ? nullptr : pdl;
+      cfg.numAttrs = first ? 0 : 1;
+      FGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, (int64_t)nvb, (const int4*)(v.vr + (v.nbands > 1 ? v.band_off[b] : 0)),
+                                      (const int*)A->idx, (const float*)A->val, B, (LdT)ldb, C, (int64_t)ldc,
+                                      (int64_t)c0, (int64_t)nk, (int)A->index_base, accumulate, partial));
+      first = false;
     }
   if (v.nseg > 0) {  // segment sums live after the nl partial-sum slots
     float* segsum = partial + (int64_t)v.nl * nk;

@@ -19,11 +19,12 @@ from .device import DeviceSparse, context, ewise, ewise_reduce, sddmm, spmm, spm
 from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, reduce, tensordot
 from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, default_scheduler,
                         einsum, finch, get_scheduler, set_scheduler, with_scheduler)
-from .tensors import (GPU, Dense, Element, Pattern, SparseCOO, SparseList, SwizzleArray, Tensor,
-                      csr, fsparse, fsprand, gpu, swizzle, transfer)
+from .tensors import (GPU, Dense, Element, Pattern, SparseByteMap, SparseCOO, SparseList, SwizzleArray,
+                      Tensor, csr, fsparse, fsprand, gpu, pattern, set_fill_value, swizzle, transfer)
 from .galley import GalleyScheduler, galley_scheduler
 
 __all__ = [
+    "SparseByteMap", "pattern", "set_fill_value",
     "FinchGBError", "FinchGBUnsupported", "DeviceSparse", "context", "spmv", "spmm", "sddmm",
     "ewise", "ewise_reduce", "LazyTensor", "lazy", "compute", "einsum", "finch", "tensordot",
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",

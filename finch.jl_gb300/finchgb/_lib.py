@@ -148,6 +148,13 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_dense_map": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_bfs_pull": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p, c_int, c_int64,
+                             c_int64, c_void_p, c_void_p]),
+    "fgb_or_count": (c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_minby_map": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p]),
+    "fgb_minby_relax": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_int64, c_void_p]),
     "fgb_cg_solve": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_void_p, c_void_p,
                              POINTER(FgbCgOptions), POINTER(FgbCgResult), c_void_p]),
     "fgb_panels_create": (c_int, [c_void_p, POINTER(FgbSparse), c_int32, POINTER(c_void_p)]),

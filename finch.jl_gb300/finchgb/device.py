@@ -371,3 +371,48 @@ def ewise_reduce(dims: int, A: DeviceSparse, B: DeviceSparse | None = None,
            0 if B_dense is None else B_dense.stride(0), _dptr(y), dtype_code(A.val), 0,
            stream_ptr())
     return y
+
+
+# ---------------------------------------------------------------- graph programs (choose / minby)
+
+def bfs_pull(A: DeviceSparse, frontier: torch.Tensor, visited: torch.Tensor, parent: torch.Tensor,
+             next_frontier: torch.Tensor | None = None, choose_fill: int = 0, index_offset: int = 1) -> torch.Tensor:
+    """One BFS round (fgb_bfs_pull): A is the CSR of the adjacency (row k
+    lists the j with edges[k, j]); frontier/visited uint8; parent int32/int64
+    updated by choose(choose_fill); returns the next frontier (uint8)."""
+    if next_frontier is None:
+        next_frontier = torch.empty(A.nrows, dtype=torch.uint8, device=visited.device)
+    d = A.desc()
+    L.call("fgb_bfs_pull", _ctx_for(visited), ctypes.byref(d), _dptr(frontier), _dptr(visited), _dptr(parent),
+           dtype_code(parent), choose_fill, index_offset, _dptr(next_frontier), stream_ptr())
+    return next_frontier
+
+
+def or_count(visited: torch.Tensor, next_frontier: torch.Tensor, count: torch.Tensor) -> torch.Tensor:
+    """visited |= next; count (device int64, 1 element) += number of true in next."""
+    L.call("fgb_or_count", _ctx_for(visited), visited.numel(), _dptr(visited), _dptr(next_frontier),
+           _dptr(count), stream_ptr())
+    return count
+
+
+def minby_map(mask: torch.Tensor | None, src: tuple, dst: tuple) -> tuple:
+    """dst <<minby>>= src where mask (pairs as (first, second) device arrays)."""
+    sd, sp = src
+    dd, dp = dst
+    L.call("fgb_minby_map", _ctx_for(dd), dtype_code(dd), dd.numel(), _dptr(mask), _dptr(sd), _dptr(sp),
+           _dptr(dd), _dptr(dp), stream_ptr())
+    return dst
+
+
+def minby_relax(A: DeviceSparse, dist_prev: torch.Tensor, active_prev: torch.Tensor, dst: tuple,
+                active: torch.Tensor | None = None, index_offset: int = 1) -> torch.Tensor:
+    """One relaxation (fgb_minby_relax): A is the CSR of the weights (row i
+    lists the j with edges[i, j]); dst = (dist, parent) updated in place;
+    returns the new active flags (uint8)."""
+    dd, dp = dst
+    if active is None:
+        active = torch.empty(A.nrows, dtype=torch.uint8, device=dd.device)
+    d = A.desc()
+    L.call("fgb_minby_relax", _ctx_for(dd), ctypes.byref(d), _dptr(dist_prev), _dptr(active_prev), _dptr(dd),
+           _dptr(dp), _dptr(active), index_offset, stream_ptr())
+    return active

@@ -538,12 +538,45 @@ def einsum(stmt: str, init=None, ctx: GB300Scheduler | None = None, **tensors):
     return (ctx or _scheduler)(plan.logic())
 
 
+def _device_vector(t, dtype) -> torch.Tensor:
+    """The HBM array of a Dense(Element) vector (moved there once); Bool
+    vectors are one byte per entry.  dtype None: any element type."""
+    body = t.body if isinstance(t, SwizzleArray) else t
+    if not isinstance(body, Tensor) or body.kind != "dense1":
+        raise FinchGBUnsupported("expected a Dense(Element) vector")
+    transfer(GPU(_device_index()), body)
+    d = body.ddata
+    if dtype is not None and d.dtype != dtype:
+        raise FinchGBUnsupported(f"vector of {d.dtype}, expected {dtype}")
+    return d
+
+
+def _rows_of(t) -> dev.DeviceSparse:
+    """The CSR of matrix t (row i lists the j with t[i, j] stored), built
+    once on the device from Finch's Dense(SparseList) and cached."""
+    A = sparse_operand(t, ("i", "j"), ("i", "j"))
+    return A if A.orient == "csr" else _csr_copy(t, A)
+
+
 def finch(program: str, ctx: GB300Scheduler | None = None, **tensors) -> dict:
     """@finch over a loop program; returns {output name: tensor}.
 
     A program that initialises its output (`y .= 0`) gets a fresh result;
     without it the output tensor passed in is accumulated into.  Float sums
-    use Finch's serial order, so results equal Finch's CPU nest."""
+    use Finch's serial order, so results equal Finch's CPU nest.  Graph
+    programs with several statements (the choose/minby rounds of Finch's BFS
+    and Bellman-Ford examples) are matched as whole programs and update
+    their tensors in place."""
+    from . import notation, programs
+
+    try:
+        tree = notation.parse(program)
+    except SyntaxError:
+        tree = None
+    if tree is not None:
+        res = programs.run(tree, tensors, _rows_of)
+        if res is not None:
+            return res
     prog = parse_finch(program)
     plan = parse_einsum(prog.stmt, tensors)
     name = plan.out_name

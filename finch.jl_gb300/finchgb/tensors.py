@@ -27,9 +27,18 @@ from .workloads import SparseBuffers, csc_from_dense
 # ---------------------------------------------------------------- levels
 
 
+def pair_dtype(fill) -> np.dtype:
+    """The element type of a 2-tuple fill value such as (Inf, 0): a record of
+    the two components' types (Finch's Tuple{Float64, Int64} elements)."""
+    a, b = fill
+    return np.dtype([("f0", np.asarray(a).dtype), ("f1", np.asarray(b).dtype)])
+
+
 @dataclass(frozen=True)
 class Element:
-    """Leaf level holding values; `fill_value` is the implicit value."""
+    """Leaf level holding values; `fill_value` is the implicit value (a
+    2-tuple fill gives tuple elements, e.g. the (distance, parent) pairs of
+    docs/examples/shortest_paths.jl)."""
 
     fill_value: object = 0.0
     dtype: object = None
@@ -37,6 +46,8 @@ class Element:
     def eltype(self):
         if self.dtype is not None:
             return np.dtype(self.dtype)
+        if isinstance(self.fill_value, tuple):
+            return pair_dtype(self.fill_value)
         return np.asarray(self.fill_value).dtype
 
 
@@ -94,8 +105,27 @@ class SparseCOO:
         return self.lvl.fill_value
 
 
+@dataclass(frozen=True)
+class SparseByteMap:
+    """Finch's SparseByteMap level over a Pattern (a Boolean vector with a
+    byte per coordinate, src/tensors/levels/sparse_bytemap_levels.jl): in
+    HBM it is the dense byte table itself, which is what the graph kernels
+    read; the list of set coordinates is not kept."""
+
+    lvl: object
+
+    def eltype(self):
+        return np.dtype(np.bool_)
+
+    @property
+    def fill_value(self):
+        return False
+
+
 def _kind(fmt) -> str:
     if isinstance(fmt, Dense) and isinstance(fmt.lvl, (Element, Pattern)):
+        return "dense1"
+    if isinstance(fmt, SparseByteMap) and isinstance(fmt.lvl, Pattern):
         return "dense1"
     if isinstance(fmt, Dense) and isinstance(fmt.lvl, Dense):
         return "dense2"
@@ -138,9 +168,19 @@ class Tensor:
         if arr is None:
             if shape is None:
                 raise ValueError("Tensor needs an array or a shape")
-            arr = np.full(shape, self.fill_value, dtype=self.dtype)
+            if self.dtype.names:
+                arr = np.empty(shape, dtype=self.dtype)
+                arr[...] = tuple(self.fill_value)
+            else:
+                arr = np.full(shape, self.fill_value, dtype=self.dtype)
         if isinstance(arr, Tensor):
             arr = arr.todense()
+        if self.dtype.names:  # tuple elements: a record array
+            arr = np.asarray(arr, dtype=self.dtype)
+            assert arr.ndim == 1 and self.kind == "dense1", "tuple elements: Dense(Element((a, b))) vectors"
+            self.shape = tuple(arr.shape)
+            self.data = np.ascontiguousarray(arr)
+            return
         arr = _as_array(arr, self.dtype)
         self.shape = tuple(arr.shape)
         fill = np.asarray(self.fill_value, dtype=self.dtype)
@@ -188,6 +228,11 @@ class Tensor:
 
     def todense(self) -> np.ndarray:
         if self.kind in ("dense1", "dense2"):
+            if isinstance(self.ddata, tuple):  # tuple elements: two device arrays
+                out = np.empty(self.shape, dtype=self.dtype)
+                out["f0"] = self.ddata[0].cpu().numpy()
+                out["f1"] = self.ddata[1].cpu().numpy()
+                return out
             if self.data is None:
                 self.data = self.ddata.cpu().numpy()
             return self.data
@@ -213,6 +258,28 @@ class Tensor:
         mask = _stored_mask(buf)
         out[mask] = D[mask]
         return out.reshape(self.shape)
+
+    def pair_device(self):
+        """The two component arrays in HBM of a vector of tuple elements."""
+        if not (self.kind == "dense1" and self.dtype.names):
+            raise TypeError("pair_device: not a vector of tuple elements")
+        if not isinstance(self.ddata, tuple):
+            transfer(GPU(0 if not hasattr(self, "_gb_device") else self._gb_device), self)
+        return self.ddata
+
+    def __setitem__(self, key, value):
+        """Host-side element write, as Finch's `t[i] = v` (1-based i)."""
+        if self.kind != "dense1":
+            raise NotImplementedError("element writes into Dense(Element) vectors")
+        i = int(key) - 1
+        if isinstance(self.ddata, tuple):
+            for comp, v in zip(self.ddata, value):
+                comp[i] = v
+        elif self.ddata is not None:
+            self.ddata[i] = value
+            self.data = None
+        else:
+            self.data[i] = value
 
     def host_buffers(self) -> SparseBuffers:
         if self.buf is None and self.dsparse is not None:
@@ -390,6 +457,11 @@ def transfer(device, t):
     if t.on_device:
         return t
     idx = device.index if isinstance(device, GPU) else int(device)
+    if t.kind == "dense1" and t.dtype.names:  # tuple elements: one device array per component
+        d = torch.device("cuda", idx)
+        t.ddata = tuple(torch.from_numpy(np.ascontiguousarray(t.data[f])).to(d) for f in t.dtype.names)
+        t.data = None
+        return t
     if t.kind in ("dense1", "dense2"):
         src = np.ascontiguousarray(t.data)
         tt = torch.from_numpy(src if src.dtype != np.bool_ else src.astype(np.uint8))
@@ -411,6 +483,46 @@ def transfer(device, t):
     t.dsparse = dev.DeviceSparse.from_host(b.nrows, b.ncols, b.ptr, b.idx, val, orient=b.orient,
                                            base=1, device=idx)
     return t
+
+
+def pattern(t):
+    """Finch's pattern!(t): the same structure with a Pattern level (every
+    stored entry true), sharing the coordinate buffers."""
+    if isinstance(t, SwizzleArray):
+        return SwizzleArray(pattern(t.body), t.dims)
+    if t.kind != "csc":
+        raise NotImplementedError("pattern! of a Dense(SparseList) matrix")
+    out = Tensor.__new__(Tensor)
+    out.__dict__.update(t.__dict__)
+    out.fmt = Dense(SparseList(Pattern()))
+    out.fill_value, out.dtype = False, np.dtype(np.bool_)
+    if t.buf is not None:
+        b = t.buf
+        out.buf = SparseBuffers(b.nrows, b.ncols, b.ptr, b.idx, None, b.orient)
+    if t.dsparse is not None:
+        d = t.dsparse
+        out.dsparse = type(d)(d.nrows, d.ncols, d.ptr, d.idx, None, d.orient, d.base)
+    for k in ("_gb_transposed", "_gb_uses"):
+        out.__dict__.pop(k, None)
+    return out
+
+
+def set_fill_value(t, fill):
+    """Finch's set_fill_value!(t, fill): the same stored entries, another
+    implicit value (e.g. Inf for unconnected edges)."""
+    body = t.body if isinstance(t, SwizzleArray) else t
+    out = Tensor.__new__(Tensor)
+    out.__dict__.update(body.__dict__)
+    lvl = body.fmt
+    chain = []
+    while not isinstance(lvl, (Element, Pattern)):
+        chain.append(type(lvl))
+        lvl = lvl.lvl
+    new = Element(np.asarray(fill, dtype=body.dtype)[()], body.dtype)
+    for c in reversed(chain):
+        new = c(new)
+    out.fmt, out.fill_value = new, np.asarray(fill, dtype=body.dtype)[()]
+    return SwizzleArray(out, t.dims) if isinstance(t, SwizzleArray) else out
 
 
 def dense_from_device(x, fill_value=0.0) -> Tensor:

@@ -267,8 +267,10 @@ FGB_API int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_
  * scratch exceeds the array even at the longest items (2^24 steps) is
  * rejected with FGB_EINVAL before any device work.  The context's device must
  * be the current device (FGB_EINVAL otherwise).  The first call on a device
- * looks the array's address up (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls share the array:
+ * looks the array's address up (cudaGetSymbolAddress), which also makes the
+ * driver load the array (and the kernels' code) if it has not yet, so make
+ * that call before any stream capture and before a region that must see no
+ * change in free device memory.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller. */
 FGB_API int fgb_spmm_noalloc(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb,
                              int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags,
@@ -349,6 +351,54 @@ FGB_API int fgb_ewise_fill(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_
 FGB_API int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_sparse* B,
                      const void* B_dense, int64_t ldb, void* y, int dtype, unsigned flags,
                      void* stream);
+
+/* ---- graph programs: the choose and minby reductions -------------------- */
+
+/* One BFS round of docs/examples/bfs.jl:
+ *   _F .= false
+ *   for j=_, k=_; if F[j] && edges[k,j] && !(V[k])
+ *     _F[k] |= true;  P[k] <<choose(z)>>= j;  end; end
+ * with choose(z)(a, b) = isequal(a, z) ? b : a
+ * (src/util/special_functions.jl:13-34).  A is the CSR of the adjacency
+ * (row k lists the j with edges[k, j] stored; Pattern or any values),
+ * frontier has ncols bytes, visited/next nrows bytes (0/1), parent nrows
+ * values of parent_t (I32 or I64).  next[k] = the round's _F[k]; for a k
+ * reached this round, parent[k] = choose(choose_fill)(parent[k], j1) where
+ * j1 is the smallest reaching j (the first the j-ascending loop meets),
+ * written as j1 + index_offset (1 for Finch's 1-based vertex numbers).
+ * visited is read only (the program's second loop updates it:
+ * fgb_or_count).  Bit-exact with the loop nest. */
+FGB_API int fgb_bfs_pull(fgb_ctx* ctx, const fgb_sparse* A, const uint8_t* frontier, const uint8_t* visited,
+                         void* parent, int parent_t, int64_t choose_fill, int64_t index_offset, uint8_t* next,
+                         void* stream);
+
+/* The second loop of a BFS round: for k; let f = next[k]; visited[k] |= f;
+ * count[] += f; end.  count is a device int64 added to (exact). */
+FGB_API int fgb_or_count(fgb_ctx* ctx, int64_t n, uint8_t* visited, const uint8_t* next, int64_t* count,
+                         void* stream);
+
+/* dist[j], parent[j] <<minby>>= (src_dist[j], src_parent[j]) for every j
+ * with mask[j] (mask NULL: all j), minby(a, b) = a[1] > b[1] ? b : a
+ * (src/util/special_functions.jl:75-88): the first loop of a relaxation
+ * round of docs/examples/shortest_paths.jl.  Pairs are held as two arrays,
+ * the first components of `dtype` (F64, F32, I32, I64), the second int64. */
+FGB_API int fgb_minby_map(fgb_ctx* ctx, int dtype, int64_t n, const uint8_t* mask, const void* src_dist,
+                          const int64_t* src_parent, void* dst_dist, int64_t* dst_parent, void* stream);
+
+/* The second loop of that round:
+ *   active .= false
+ *   for j=_; if active_prev[j]; for i=_
+ *     let d = first(dists_prev[j]) + edges[i, j]
+ *       dists[i] <<minby>>= (d, j);  active[i] |= d < first(dists_prev[i])
+ *   end; end; end; end
+ * A is the CSR of the weights (row i lists the j with edges[i, j] stored,
+ * ascending; values F64, F32, I32 or I64 -- the distance type); unstored
+ * edges are the fill Inf and change nothing.  (dist, parent) are updated
+ * in place, active (nrows bytes) written; j is written as j + index_offset.
+ * Each row folds its contributions in ascending j, as the nest does, so
+ * results are bit-exact.  dist_prev and dist must differ. */
+FGB_API int fgb_minby_relax(fgb_ctx* ctx, const fgb_sparse* A, const void* dist_prev, const uint8_t* active_prev,
+                            void* dist, int64_t* parent, uint8_t* active, int64_t index_offset, void* stream);
 
 /* ---- dense Element levels and 0-d Scalars ------------------------------ */
 

@@ -579,6 +579,64 @@ int64_t orc_spgemm_csr(int vt, int fma, int64_t m, int64_t n, const int64_t* lp,
 }
 
 /* Threads available to the OpenMP runtime (1 without OpenMP). */
+/* One BFS round of docs/examples/bfs.jl:25-34, as written: j outer over
+ * the columns of `edges` (CSC: column j lists the k with edges[k, j]), k
+ * inner, and for F[j] && edges[k, j] && !V[k]: nF[k] |= true;
+ * P[k] <<choose(fill)>>= j, with choose(z)(a, b) = isequal(a, z) ? b : a
+ * (src/util/special_functions.jl:13-34); j is written 1-based.  Then the
+ * second loop (bfs.jl:35-42): V[k] |= nF[k]; c += nF[k].  Returns c. */
+int64_t orc_bfs_round(int64_t n, const int64_t* ptr, const int64_t* idx, const uint8_t* F, uint8_t* V,
+                      int64_t* P, int64_t fill, uint8_t* nF) {
+  memset(nF, 0, (size_t)n);
+  for (int64_t j = 0; j < n; ++j) {
+    if (!F[j]) continue;
+    for (int64_t q = ptr[j] - 1; q < ptr[j + 1] - 1; ++q) {
+      const int64_t k = idx[q] - 1;
+      if (V[k]) continue;
+      nF[k] = 1;
+      if (P[k] == fill) P[k] = j + 1;
+    }
+  }
+  int64_t c = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    V[k] |= nF[k];
+    c += nF[k];
+  }
+  return c;
+}
+
+/* minby(a, b) = a[1] > b[1] ? b : a (src/util/special_functions.jl:75-88). */
+#define MINBY(dd, pp, d, p) \
+  do {                      \
+    if ((dd) > (d)) {       \
+      (dd) = (d);           \
+      (pp) = (p);           \
+    }                       \
+  } while (0)
+
+/* One relaxation round of docs/examples/shortest_paths.jl:22-42 over
+ * Float64 distances, as written.  The first loop: for j with active_prev[j],
+ * dists[j] <<minby>>= dists_prev[j].  The second: active .= false; for j
+ * with active_prev[j], for the stored i of column j of `edges` (CSC; the
+ * fill Inf leaves everything unchanged), d = first(dists_prev[j]) +
+ * edges[i, j]; dists[i] <<minby>>= (d, j); active[i] |= d <
+ * first(dists_prev[i]).  Pairs are (dist, parent) arrays; j is 1-based. */
+void orc_minby_round(int64_t n, const int64_t* ptr, const int64_t* idx, const double* w, const double* dprev,
+                     const int64_t* pprev, const uint8_t* aprev, double* dist, int64_t* par, uint8_t* active) {
+  for (int64_t j = 0; j < n; ++j)
+    if (aprev[j]) MINBY(dist[j], par[j], dprev[j], pprev[j]);
+  memset(active, 0, (size_t)n);
+  for (int64_t j = 0; j < n; ++j) {
+    if (!aprev[j]) continue;
+    for (int64_t q = ptr[j] - 1; q < ptr[j + 1] - 1; ++q) {
+      const int64_t i = idx[q] - 1;
+      const double d = dprev[j] + w[q];
+      MINBY(dist[i], par[i], d, j + 1);
+      active[i] |= (uint8_t)(d < dprev[i]);
+    }
+  }
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -64,19 +64,20 @@ def test_spmm_bands_accumulate_strides_empty(gpu_lib):
     B48 = np.ascontiguousarray(Bfull[:, :48])
     want = oracle.spmm_csr(500, 300, r.ptr, r.idx, r.val, B48, C=np.ascontiguousarray(C0[:, :48]),
                            init=False)
-    for bands in (2, 4, 8):
+    for bands, variant in ((2, 3), (4, 3), (8, 3), (4, 2)):
         Cd = to_dev(C0)
-        dev.spmm(A, to_dev(Bfull)[:, :48], Cd[:, :48], flags=L.ACCUMULATE, lanes=8, path=16, variant=3,
+        dev.spmm(A, to_dev(Bfull)[:, :48], Cd[:, :48], flags=L.ACCUMULATE, lanes=8, path=16, variant=variant,
                  bands=bands)
         got = to_host(Cd)
         assert_close(got[:, :48], want, spmm_scale(r, B48) + np.abs(C0[:, :48]), np.float32)
         assert np.array_equal(got[:, 48:], C0[:, 48:])  # untouched beyond nk
-        Cw = to_host(dev.spmm(A, to_dev(B48), lanes=8, path=16, variant=3, bands=bands))
+        Cw = to_host(dev.spmm(A, to_dev(B48), lanes=8, path=16, variant=variant, bands=bands))
         assert_close(Cw, oracle.spmm_csr(500, 300, r.ptr, r.idx, r.val, B48), spmm_scale(r, B48), np.float32)
         assert not Cw[np.diff(r.ptr) == 0].any()  # empty rows written as zeros
     empty = upload(csr_from_dense(np.zeros((40, 30), dtype=np.float32)))
-    Ce = dev.spmm(empty, to_dev(rng.standard_normal((30, 16)).astype(np.float32)), variant=3, bands=4)
-    assert not to_host(Ce).any()
+    for variant in (2, 3):
+        Ce = dev.spmm(empty, to_dev(rng.standard_normal((30, 16)).astype(np.float32)), variant=variant, bands=4)
+        assert not to_host(Ce).any()
 
 
 def test_spmm_bands_rejects(gpu_lib):
@@ -84,7 +85,8 @@ def test_spmm_bands_rejects(gpu_lib):
     r = zipf_csr(rng, 200, 100, mean=4, cap=50)
     A = upload(r)
     Bd = to_dev(rng.standard_normal((100, 32)).astype(np.float32))
-    for kw in ({"variant": 3, "bands": 9}, {"variant": 3, "bands": -1}, {"variant": 0, "bands": 2}):
+    for kw in ({"variant": 3, "bands": 9}, {"variant": 3, "bands": -1}, {"variant": 0, "bands": 2},
+               {"variant": 4}):
         with pytest.raises(L.FinchGBError) as e:
             dev.spmm(A, Bd, lanes=8, path=64, **kw)
         assert e.value.status == L.EINVAL
