@@ -6,18 +6,20 @@
 //   x += alpha p;  r -= alpha q;  rr' = r.r;  p = r + (rr'/rr) p
 //
 // run on the GPU.  The iteration SpMV reads FP32 or BF16 values (or FP64),
-// converts p to FP32 per product and accumulates in FP32; x, r, p, q, the dot
-// products and the updates are FP64.  Accuracy is won back by reliable
+// converts p to FP32 per product and accumulates in FP32 (or, when asked,
+// widens the values to FP64 and accumulates in FP64); x, r, p, q, the dot
+// products and the updates are FP64.  A matrix whose columns lie within
+// 32,767 of the diagonal is read through 16-bit column offsets j - i.  Accuracy is won back by reliable
 // updates: every `replace_every` iterations, and whenever the recursive
 // residual reaches the tolerance, the true residual r = b - A x is recomputed
 // with the FP64 matrix and replaces the recursive one (residual replacement
 // keeping the search direction), and the solve stops only when that true
 // residual is below rtol * ||b||.
 //
-// One iteration is three kernels -- SpMV fused with the p.q partials; the
-// x/r update (every block folds the p.q partials itself) fused with the r.r
-// partials; the p update fused with the fold of r.r -- so no scalar ever
-// leaves the device.  Every partial is folded in a fixed order: the solve is
+// One iteration is three kernels -- SpMV fused with the p.q partials; the r
+// update (every block folds the p.q partials itself) fused with the r.r
+// partials; the x and p updates fused with the folds -- so no scalar ever
+// leaves the device, and p is read once by the updates.  Every partial is folded in a fixed order: the solve is
 // deterministic.  A chunk of iterations is captured once in a CUDA graph and
 // replayed; the host reads the residual history once per chunk.
 #include <chrono>
@@ -67,21 +69,32 @@ __device__ __forceinline__ float cg_val(const VT* v, int64_t k) {
   return to_acc<float>(v[k]);
 }
 
+// Column j of stored entry k of row i: from the int32 index, or (IX =
+// int16_t) from the 16-bit offset j - i of a banded matrix's compact copy.
+template <class IX>
+__device__ __forceinline__ int64_t cg_col(const IX* __restrict__ ix, int64_t k, int64_t i, int base) {
+  if constexpr (sizeof(IX) == 2) return i + (int64_t)__ldg(ix + k);
+  else return (int64_t)__ldg(ix + k) - base;
+}
+
 // q = A p (one row per thread, j ascending) and the block partial of p.q.
 // ACC = float: values converted to FP32 and p rounded to FP32 per product;
-// ACC = double: the FP64 SpMV.
-template <class VT, class ACC, class PtrT>
+// ACC = double: values (FP64, FP32 or BF16) widened to FP64 and the products
+// summed in FP64 -- with the FP64 values, the FP64 SpMV.
+template <class VT, class ACC, class PtrT, class IX>
 __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
-    int64_t n, const PtrT* __restrict__ ptr, const int* __restrict__ idx, const VT* __restrict__ val,
+    int64_t n, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const double* __restrict__ p, double* __restrict__ q, double* __restrict__ part) {
   __shared__ double sh[33];
   double dot = 0.0;
-  auto term = [&](int64_t k, ACC acc) -> ACC {
-    const int j = __ldg(idx + k) - base;
+  auto term = [&](int64_t k, int64_t row, ACC acc) -> ACC {
+    const int64_t j = cg_col(idx, k, row, base);
     if constexpr (sizeof(ACC) == 4)
       return __fmaf_rn(cg_val(val, k), (float)__ldg(p + j), acc);
-    else
+    else if constexpr (sizeof(VT) == 8)
       return __fma_rn((double)__ldg((const double*)val + k), __ldg(p + j), acc);
+    else
+      return __fma_rn((double)cg_val(val, k), __ldg(p + j), acc);
   };
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   // two rows (i, i + stride) per thread in flight; rows and their products
@@ -94,8 +107,8 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
     ACC acc_a = ACC(0), acc_b = ACC(0);
     const int64_t la = a1 - a0, lb = b1 - b0;
     for (int64_t t = 0; t < (la > lb ? la : lb); ++t) {
-      if (t < la) acc_a = term(a0 + t, acc_a);
-      if (t < lb) acc_b = term(b0 + t, acc_b);
+      if (t < la) acc_a = term(a0 + t, i, acc_a);
+      if (t < lb) acc_b = term(b0 + t, i2, acc_b);
     }
     const double qa = (double)acc_a;
     q[i] = qa;
@@ -110,11 +123,29 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
   if (threadIdx.x == 0) part[blockIdx.x] = dot;
 }
 
-// alpha = rr[slot] / (p.q);  x += alpha p;  r -= alpha q;  partials of r.r
-__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xr(
-    int64_t n, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
-    const double* __restrict__ q, const double* __restrict__ part_pq, int nparts,
-    const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
+// The compact index of a banded matrix: off[k] = j - i for the stored
+// entries of row i, and *bad set when some |j - i| does not fit 16 bits.
+template <class PtrT>
+__global__ void cg_offsets(int64_t n, const PtrT* __restrict__ ptr, const int* __restrict__ idx, int base,
+                           int16_t* __restrict__ off, int* __restrict__ bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t k = ld_ptr(ptr, i) - base; k < ld_ptr(ptr, i + 1) - base; ++k) {
+      const int64_t d = (int64_t)idx[k] - base - i;
+      if (d < -32768 || d > 32767) {
+        *bad = 1;
+        off[k] = 0;
+      } else {
+        off[k] = (int16_t)d;
+      }
+    }
+  }
+}
+
+// alpha = rr[slot] / (p.q);  r -= alpha q;  partials of r.r.  (x += alpha p
+// waits for the p update, which reads p anyway: one pass over p less.)
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_r(
+    int64_t n, double* __restrict__ r, const double* __restrict__ q, const double* __restrict__ part_pq,
+    int nparts, const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
   __shared__ double sh[33];
   const double pq = fold_parts(part_pq, nparts, sh);
   // a vanished curvature (p.q == 0) only happens once r is exactly zero
@@ -125,24 +156,20 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xr(
   // CG_ILP elements per thread in flight: all loads first, then the updates
   // in the same element order as the plain loop (bit-identical partials)
   for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
-    double pv[CG_ILP], qv[CG_ILP], xv[CG_ILP], rv[CG_ILP];
+    double qv[CG_ILP], rv[CG_ILP];
 #pragma unroll
     for (int u = 0; u < CG_ILP; ++u) {
-      pv[u] = p[i + u * stride];
       qv[u] = q[i + u * stride];
-      xv[u] = x[i + u * stride];
       rv[u] = r[i + u * stride];
     }
 #pragma unroll
     for (int u = 0; u < CG_ILP; ++u) {
-      x[i + u * stride] = __fma_rn(alpha, pv[u], xv[u]);
       const double ri = __fma_rn(-alpha, qv[u], rv[u]);
       r[i + u * stride] = ri;
       acc = __fma_rn(ri, ri, acc);
     }
   }
   for (; i < n; i += stride) {
-    x[i] = __fma_rn(alpha, p[i], x[i]);
     const double ri = __fma_rn(-alpha, q[i], r[i]);
     r[i] = ri;
     acc = __fma_rn(ri, ri, acc);
@@ -151,28 +178,40 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xr(
   if (threadIdx.x == 0) part_rr[blockIdx.x] = acc;
 }
 
-// rr' = fold(r.r partials);  p = r + (rr' / rr[slot_in]) p;  rr[slot_out] = rr'
-__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_p(
-    int64_t n, const double* __restrict__ r, double* __restrict__ p,
-    const double* __restrict__ part_rr, int nparts, double* __restrict__ rr, int slot_in,
-    int slot_out, double* __restrict__ hist, int64_t it) {
+// alpha as cg_update_r formed it (the same fold of the p.q partials);
+// x += alpha p; rr' = fold(r.r partials); p = r + (rr' / rr[slot_in]) p;
+// rr[slot_out] = rr'.  x's update is the one of the plain loop, bit for bit.
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xp(
+    int64_t n, double* __restrict__ x, const double* __restrict__ r, double* __restrict__ p,
+    const double* __restrict__ part_pq, int nparts_pq, const double* __restrict__ part_rr, int nparts,
+    double* __restrict__ rr, int slot_in, int slot_out, double* __restrict__ hist, int64_t it) {
   __shared__ double sh[33];
+  const double pq = fold_parts(part_pq, nparts_pq, sh);
+  const double alpha = pq != 0.0 ? rr[slot_in] / pq : 0.0;
   const double rr_new = fold_parts(part_rr, nparts, sh);
   const double beta = rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
-    double pv[CG_ILP], rv[CG_ILP];
+    double pv[CG_ILP], rv[CG_ILP], xv[CG_ILP];
 #pragma unroll
     for (int u = 0; u < CG_ILP; ++u) {
       pv[u] = p[i + u * stride];
       rv[u] = r[i + u * stride];
+      xv[u] = x[i + u * stride];
     }
 #pragma unroll
-    for (int u = 0; u < CG_ILP; ++u) p[i + u * stride] = __fma_rn(beta, pv[u], rv[u]);
+    for (int u = 0; u < CG_ILP; ++u) {
+      x[i + u * stride] = __fma_rn(alpha, pv[u], xv[u]);
+      p[i + u * stride] = __fma_rn(beta, pv[u], rv[u]);
+    }
   }
-  for (; i < n; i += stride) p[i] = __fma_rn(beta, p[i], r[i]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  for (; i < n; i += stride) {
+    const double pi = p[i];
+    x[i] = __fma_rn(alpha, pi, x[i]);
+    p[i] = __fma_rn(beta, pi, r[i]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // slot_out != slot_in: no block reads it here
     rr[slot_out] = rr_new;
     hist[it] = rr_new;
   }
@@ -228,34 +267,50 @@ struct CgBuffers {
 
 // The SpMV's own grid: at most `grid` blocks and no more than fit the SMs at
 // once (its two rows per thread take more registers than the updates).
-template <class VT, class ACC, class PtrT>
+template <class VT, class ACC, class PtrT, class IX>
 static int dot_grid_t(int grid, int sms) {
   static const int occ = [] {  // once per process (one device model); thread-safe
     int o = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cg_spmv_dot<VT, ACC, PtrT>, CG_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cg_spmv_dot<VT, ACC, PtrT, IX>, CG_THREADS, 0);
     return o > 0 ? o : 1;
   }();
   return std::max(1, std::min(grid, occ * sms));
 }
 
-template <class PtrT>
-static int spmv_dot_grid(int precision, int grid, int sms) {
-  if (precision == FGB_F64) return dot_grid_t<double, double, PtrT>(grid, sms);
-  if (precision == FGB_BF16) return dot_grid_t<__nv_bfloat16, float, PtrT>(grid, sms);
-  return dot_grid_t<float, float, PtrT>(grid, sms);
+// The iteration SpMV: value type (precision), accumulation (FP64 for the
+// FP64 matrix or when asked) and index form (16-bit offsets when compact).
+template <class VT, class ACC, class PtrT, class IX>
+static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int grid, int sms, const double* p, double* q,
+                      double* part, cudaStream_t s, bool launch) {
+  const int g = dot_grid_t<VT, ACC, PtrT, IX>(grid, sms);
+  if (launch)
+    cg_spmv_dot<VT, ACC, PtrT, IX><<<g, CG_THREADS, 0, s>>>(A->nrows, (const PtrT*)A->ptr, ix, (const VT*)A->val,
+                                                           A->index_base, p, q, part);
+  return g;
 }
 
-template <class PtrT>
-static void launch_spmv_dot(const fgb_sparse* A, int precision, int grid, const double* p,
-                            double* q, double* part, cudaStream_t s) {
-  const PtrT* ptr = (const PtrT*)A->ptr;
-  const int* idx = (const int*)A->idx;
+template <class PtrT, class IX>
+static int spmv_dot_ix(const fgb_sparse* A, const IX* ix, int precision, bool acc64, int grid, int sms,
+                       const double* p, double* q, double* part, cudaStream_t s, bool launch) {
   if (precision == FGB_F64)
-    cg_spmv_dot<double, double, PtrT><<<grid, CG_THREADS, 0, s>>>(A->nrows, ptr, idx, (const double*)A->val, A->index_base, p, q, part);
-  else if (precision == FGB_BF16)
-    cg_spmv_dot<__nv_bfloat16, float, PtrT><<<grid, CG_THREADS, 0, s>>>(A->nrows, ptr, idx, (const __nv_bfloat16*)A->val, A->index_base, p, q, part);
-  else
-    cg_spmv_dot<float, float, PtrT><<<grid, CG_THREADS, 0, s>>>(A->nrows, ptr, idx, (const float*)A->val, A->index_base, p, q, part);
+    return spmv_dot_t<double, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
+  if (precision == FGB_BF16)
+    return acc64 ? spmv_dot_t<__nv_bfloat16, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch)
+                 : spmv_dot_t<__nv_bfloat16, float, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
+  return acc64 ? spmv_dot_t<float, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch)
+               : spmv_dot_t<float, float, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
+}
+
+// Launches (launch = true) or sizes (false) the iteration SpMV; returns its grid.
+static int spmv_dot(const fgb_sparse* A, const int16_t* off, int precision, bool acc64, int grid, int sms,
+                    const double* p, double* q, double* part, cudaStream_t s, bool launch) {
+  const bool i32 = A->ptr_t == FGB_I32;
+  if (off)
+    return i32 ? spmv_dot_ix<int32_t, int16_t>(A, off, precision, acc64, grid, sms, p, q, part, s, launch)
+               : spmv_dot_ix<int64_t, int16_t>(A, off, precision, acc64, grid, sms, p, q, part, s, launch);
+  const int* idx = (const int*)A->idx;
+  return i32 ? spmv_dot_ix<int32_t, int>(A, idx, precision, acc64, grid, sms, p, q, part, s, launch)
+             : spmv_dot_ix<int64_t, int>(A, idx, precision, acc64, grid, sms, p, q, part, s, launch);
 }
 
 template <class PtrT>
@@ -314,6 +369,8 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   CgBuffers bufs;
+  int16_t* off = nullptr;  // the compact index (16-bit column offsets), when it fits
+  const bool acc64 = precision == FGB_F64 || opt->accumulate_fp64 != 0;
   int64_t hist_cap = 0;
   const int grid = grid_for(n, CG_THREADS, ctx->num_sms, 8);  // full occupancy: streaming kernels
   const bool i32 = A64->ptr_t == FGB_I32;  // ptr width of the FP64 matrix
@@ -353,19 +410,36 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
       res->true_rel_residual = bnorm > 0 ? sqrt(rr_bb[0]) / bnorm : 0.0;
       break;
     }
+    // The compact index: 16-bit column offsets j - i when the matrix is
+    // banded that tightly (built once; the int32 index otherwise).
+    if (n > 0 && Ait->nnz > 0) {
+      int bad = 0;
+      if ((e = cudaMallocAsync((void**)&off, sizeof(int16_t) * Ait->nnz + 256, s)) != cudaSuccess) { fail(FGB_ENOMEM, "offsets", e); break; }
+      int* dbad = (int*)((char*)off + ((sizeof(int16_t) * Ait->nnz + 15) & ~size_t(15)));
+      cudaMemsetAsync(dbad, 0, sizeof(int), s);
+      if (Ait->ptr_t == FGB_I32)
+        cg_offsets<int32_t><<<grid, CG_THREADS, 0, s>>>(n, (const int32_t*)Ait->ptr, (const int*)Ait->idx, Ait->index_base, off, dbad);
+      else
+        cg_offsets<int64_t><<<grid, CG_THREADS, 0, s>>>(n, (const int64_t*)Ait->ptr, (const int*)Ait->idx, Ait->index_base, off, dbad);
+      if ((e = cudaMemcpyAsync(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(s)) != cudaSuccess) { fail(FGB_ECUDA, "offsets", e); break; }
+      if (bad) {
+        cudaFreeAsync(off, s);
+        off = nullptr;
+      }
+    }
+    res->compact_index = off ? 1 : 0;
     // one chunk of iterations, captured once (slots alternate; chunk is even)
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { fail(FGB_ECUDA, "capture", e); break; }
     const int grid_upd = grid_for(n, CG_UPD_THREADS, ctx->num_sms, 1);  // <= grid partial slots
-    const int grid_dot = Ait->ptr_t == FGB_I32 ? spmv_dot_grid<int32_t>(precision, grid, ctx->num_sms)
-                                               : spmv_dot_grid<int64_t>(precision, grid, ctx->num_sms);
+    const int grid_dot = spmv_dot(Ait, off, precision, acc64, grid, ctx->num_sms, nullptr, nullptr, nullptr, s, false);
     for (int t = 0; t < chunk; ++t) {
       const int si = t & 1, so = si ^ 1;
-      if (Ait->ptr_t == FGB_I32) launch_spmv_dot<int32_t>(Ait, precision, grid_dot, bufs.p, bufs.q, bufs.part_a, s);
-      else launch_spmv_dot<int64_t>(Ait, precision, grid_dot, bufs.p, bufs.q, bufs.part_a, s);
-      cg_update_xr<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
-                                              bufs.part_b);
-      cg_update_p<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.p, bufs.part_b, grid_upd, bufs.rr, si, so,
-                                                     bufs.hist, t);
+      spmv_dot(Ait, off, precision, acc64, grid, ctx->num_sms, bufs.p, bufs.q, bufs.part_a, s, true);
+      cg_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
+                                                     bufs.part_b);
+      cg_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.part_a, grid_dot, bufs.part_b,
+                                                      grid_upd, bufs.rr, si, so, bufs.hist, t);
     }
     e = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -423,6 +497,7 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   if (bufs.r) cudaFreeAsync(bufs.r, s);
+  if (off) cudaFreeAsync(off, s);
   // the caller's stream waits for the solve
   if (ev) {
     cudaEventRecord(ev, s);

@@ -137,3 +137,71 @@ extern "C" int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr
   if (A->ptr_t == FGB_I32) return transpose_typed<int32_t>(ctx, A, out_ptr, out_idx, out_val, s);
   return transpose_typed<int64_t>(ctx, A, out_ptr, out_idx, out_val, s);
 }
+
+namespace fgb {
+
+// out = fill everywhere (esz-byte elements, row-major m x n with leading
+// dimension ld), then the stored entries of A over it.
+__global__ void fill_bytes_k(int64_t m, int64_t n, int64_t ld, int esz, const unsigned char* __restrict__ fillv,
+                             unsigned char* __restrict__ out) {
+  unsigned char f[8];
+  for (int b = 0; b < esz; ++b) f[b] = fillv[b];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n; e += (int64_t)gridDim.x * blockDim.x) {
+    unsigned char* dst = out + ((e / n) * ld + e % n) * esz;
+    for (int b = 0; b < esz; ++b) dst[b] = f[b];
+  }
+}
+
+template <class PtrT>
+__global__ void scatter_dense_k(int64_t nf, const PtrT* __restrict__ ptr, const int* __restrict__ idx, int base,
+                                const unsigned char* __restrict__ val, int esz, int csc, int64_t ld,
+                                unsigned char* __restrict__ out) {
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t p = ld_ptr(ptr, f) - base; p < ld_ptr(ptr, f + 1) - base; ++p) {
+      const int64_t c = (int64_t)idx[p] - base;
+      const int64_t i = csc ? c : f, j = csc ? f : c;
+      unsigned char* dst = out + (i * ld + j) * esz;
+      if (val)
+        for (int b = 0; b < esz; ++b) dst[b] = val[p * esz + b];
+      else
+        dst[0] = 1;  // a Pattern entry is true
+    }
+  }
+}
+
+}  // namespace fgb
+
+extern "C" int fgb_sparse_to_dense(fgb_ctx* ctx, const fgb_sparse* A, const void* fill, void* out, int64_t ld,
+                                   void* stream) {
+  using namespace fgb;
+  FGB_REQUIRE(ctx && A && fill, "fgb_sparse_to_dense: null argument");
+  int rc = check_sparse(A, "fgb_sparse_to_dense: A", true);
+  if (rc) return rc;
+  FGB_REQUIRE(ld >= A->ncols, "fgb_sparse_to_dense: leading dimension below the column count");
+  if (A->nrows == 0 || A->ncols == 0) return FGB_OK;
+  FGB_REQUIRE(out, "fgb_sparse_to_dense: null output");
+  const int esz = A->val_t == FGB_NONE ? 1 : dtype_size(A->val_t);
+  cudaStream_t s = pick_stream(ctx, stream);
+  unsigned char* fdev = nullptr;
+  FGB_CUDA_TRY(cudaMallocAsync((void**)&fdev, 8, s));
+  cudaError_t e = cudaMemcpyAsync(fdev, fill, esz, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    fill_bytes_k<<<grid_for(A->nrows * A->ncols, 256, ctx->num_sms), 256, 0, s>>>(A->nrows, A->ncols, ld, esz, fdev,
+                                                                                  (unsigned char*)out);
+    const int64_t nf = A->orient == FGB_CSC ? A->ncols : A->nrows;
+    const int grid = grid_for(nf, 256, ctx->num_sms);
+    if (A->ptr_t == FGB_I32)
+      scatter_dense_k<int32_t><<<grid, 256, 0, s>>>(nf, (const int32_t*)A->ptr, (const int*)A->idx, A->index_base,
+                                                    (const unsigned char*)A->val, esz, A->orient == FGB_CSC, ld,
+                                                    (unsigned char*)out);
+    else
+      scatter_dense_k<int64_t><<<grid, 256, 0, s>>>(nf, (const int64_t*)A->ptr, (const int*)A->idx, A->index_base,
+                                                    (const unsigned char*)A->val, esz, A->orient == FGB_CSC, ld,
+                                                    (unsigned char*)out);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(fdev, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the fill value's host memory may go after return
+  if (e != cudaSuccess) return set_error(FGB_ECUDA, "fgb_sparse_to_dense: %s", cudaGetErrorString(e));
+  return FGB_OK;
+}

@@ -51,13 +51,14 @@ class FgbSddmmTuning(ctypes.Structure):
 
 class FgbCgOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("max_iter", c_int64), ("chunk", c_int32),
-                ("precision", c_int32), ("replace_every", c_int64)]
+                ("precision", c_int32), ("replace_every", c_int64), ("accumulate_fp64", c_int32),
+                ("reserved", c_int32)]
 
 
 class FgbCgResult(ctypes.Structure):
     _fields_ = [("iterations", c_int64), ("replacements", c_int64),
                 ("true_rel_residual", c_double), ("seconds", c_double), ("converged", c_int32),
-                ("reserved", c_int32)]
+                ("compact_index", c_int32)]
 
 
 class FgbPlanDesc(ctypes.Structure):
@@ -148,6 +149,11 @@ SIGNATURES: dict[str, tuple] = {
     "fgb_dense_map": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fgb_spgemm_dense": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_int, c_uint, c_void_p,
+                                 c_int64, c_void_p]),
+    "fgb_sparse_to_dense": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_int64, c_void_p]),
+    "fgb_spmm_semiring": (c_int, [c_void_p, c_int, POINTER(FgbSparse), c_void_p, c_int64, c_int64, c_void_p,
+                                  c_int64, c_int, c_uint, c_void_p]),
     "fgb_bfs_pull": (c_int, [c_void_p, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p, c_int, c_int64,
                              c_int64, c_void_p, c_void_p]),
     "fgb_or_count": (c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),

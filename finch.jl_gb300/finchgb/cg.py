@@ -31,6 +31,7 @@ class CGResult:
     true_rel_residual: float
     seconds: float
     converged: bool
+    compact_index: bool = False
 
 
 def low_precision_copy(A: dev.DeviceSparse, precision: str) -> dev.DeviceSparse:
@@ -41,9 +42,11 @@ def low_precision_copy(A: dev.DeviceSparse, precision: str) -> dev.DeviceSparse:
 
 def cg_solve(A64: dev.DeviceSparse, b: torch.Tensor, x: torch.Tensor | None = None,
              precision: str = "f32", rtol: float = 1e-10, max_iter: int = 100_000,
-             chunk: int = 64, replace_every: int = 512, Alow: dev.DeviceSparse | None = None
-             ) -> tuple[torch.Tensor, CGResult]:
-    """Solves A x = b (A SPD, CSR, FP64 values); returns (x, result)."""
+             chunk: int = 64, replace_every: int = 512, Alow: dev.DeviceSparse | None = None,
+             accumulate: str = "f32") -> tuple[torch.Tensor, CGResult]:
+    """Solves A x = b (A SPD, CSR, FP64 values); returns (x, result).
+    precision: the stored values of the iteration SpMV (f64, f32, bf16);
+    accumulate: its sums for f32/bf16 values, "f32" or "f64" (values widened)."""
     if A64.orient != "csr":
         raise ValueError("cg_solve needs a CSR matrix")
     if x is None:
@@ -51,14 +54,14 @@ def cg_solve(A64: dev.DeviceSparse, b: torch.Tensor, x: torch.Tensor | None = No
     prec = PRECISIONS[precision]
     if prec != L.F64 and Alow is None:
         Alow = low_precision_copy(A64, precision)
-    opts = L.FgbCgOptions(rtol, max_iter, chunk, prec, replace_every)
+    opts = L.FgbCgOptions(rtol, max_iter, chunk, prec, replace_every, 1 if accumulate == "f64" else 0, 0)
     res = L.FgbCgResult()
     da = A64.desc()
     dl = None if prec == L.F64 else ctypes.byref(Alow.desc())
     L.call("fgb_cg_solve", dev.context(b.device.index), ctypes.byref(da), dl, b.data_ptr(),
            x.data_ptr(), ctypes.byref(opts), ctypes.byref(res), dev.stream_ptr())
     return x, CGResult(res.iterations, res.replacements, res.true_rel_residual, res.seconds,
-                       bool(res.converged))
+                       bool(res.converged), bool(res.compact_index))
 
 
 def cg_finch(A, b, rtol: float = 1e-10, max_iter: int = 10_000):

@@ -228,6 +228,33 @@ def spmm(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, flags:
     return C
 
 
+def sparse_to_dense(A: DeviceSparse, fill) -> torch.Tensor:
+    """Row-major dense copy of A with `fill` where nothing is stored
+    (fgb_sparse_to_dense); a Pattern becomes a uint8 0/1 matrix."""
+    dt = torch.uint8 if A.val is None else A.val.dtype
+    out = torch.empty((A.nrows, A.ncols), dtype=dt, device=A.idx.device)
+    npdt = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32, torch.int64: np.int64,
+            torch.uint8: np.uint8}[dt]
+    f = np.array([fill], dtype=npdt)
+    d = A.desc()
+    L.call("fgb_sparse_to_dense", _ctx_for(A.idx), ctypes.byref(d), f.ctypes.data, _dptr(out), A.ncols,
+           stream_ptr())
+    return out
+
+
+def spmm_semiring(A: DeviceSparse, B: torch.Tensor, C: torch.Tensor | None = None, semiring: int = L.MAX_PLUS,
+                  flags: int = 0) -> torch.Tensor:
+    """C <<add>>= A (*) B over an exact semiring (fgb_spmm_semiring), row-major B."""
+    nk = B.shape[1]
+    if C is None:
+        C = torch.empty((A.nrows, nk), dtype=B.dtype, device=B.device)
+        flags &= ~L.ACCUMULATE
+    d = A.desc()
+    L.call("fgb_spmm_semiring", _ctx_for(B), semiring, ctypes.byref(d), _dptr(B), B.stride(0), nk, _dptr(C),
+           C.stride(0), dtype_code(B), flags, stream_ptr())
+    return C
+
+
 class Panels:
     """Column-panel layout of a CSR matrix (fgb_panels_*) for SpMM with an
     L2-resident slice of B per panel."""
@@ -303,6 +330,15 @@ def spgemm(A: DeviceSparse, B: DeviceSparse, flags: int = 0) -> DeviceSparse:
         L.call("fgb_narrow_index", ctx, c_ptr.data_ptr(), p32.data_ptr(), nf + 1, 0, stream_ptr())
         c_ptr = p32
     return DeviceSparse(A.nrows, B.ncols, c_ptr, c_idx[:k], c_val[:k], A.orient, A.base)
+
+
+def spgemm_dense(A: DeviceSparse, B: DeviceSparse, flags: int = 0) -> torch.Tensor:
+    """C = A * B into a dense row-major array (fgb_spgemm_dense)."""
+    C = torch.empty((A.nrows, B.ncols), dtype=A.val.dtype, device=A.idx.device)
+    da, db = A.desc(), B.desc()
+    L.call("fgb_spgemm_dense", _ctx_for(A.idx), ctypes.byref(da), ctypes.byref(db), dtype_code(A.val), flags,
+           _dptr(C), B.ncols, stream_ptr())
+    return C
 
 
 def ewise(op: int, A: DeviceSparse, B: DeviceSparse) -> DeviceSparse:

@@ -213,6 +213,22 @@ class GalleyPlan:
     result_idxs: tuple
 
 
+# Output formats by estimated density (src/Galley/PhysicalOptimizer/
+# format-selector.jl:27-65): dense past one half while the dense copy stays
+# under 3e10 elements, a sparse list below.  Galley's middle choice between
+# 5% and 50% (a bytemap) has no GPU kernel here; such outputs stay sparse lists.
+DENSE_FRACTION = 0.5
+DENSE_LIMIT = 3e10
+
+
+def select_output_format(nnz: float, rows: float, cols: float, esz: int) -> str:
+    """'dense' or 'sparse' for a rows x cols output of about nnz entries."""
+    cells = rows * cols
+    if cells > 0 and nnz / cells > DENSE_FRACTION and cells < DENSE_LIMIT:
+        return "dense"
+    return "sparse"
+
+
 def _uniform_products(a: Stats, b: Stats, v: str) -> float:
     return a.nnz * b.nnz / max(a.dims[v], 1)
 
@@ -275,14 +291,23 @@ def _step_options(fs: list, v: str, red_left: set, out: tuple, estimator: str):
                 cost = g + stream / HBM_BPS + LAUNCH_S * (slabs + 1)
                 rs = Stats({i: int(m), k: int(nk)}, m * nk, True, {i: nk, k: m}, sy.esz)
                 opts.append(("spmm", (v,), (i, k), rs, cost))
-        # S[i,v] * T[v,k] -> sparse C[i,k]
+        # S[i,v] * T[v,k] -> C[i,k], sparse or dense by its estimated density
         if not sy.dense and len(y.idxs) == 2 and v in y.idxs:
             k = y.idxs[0] if y.idxs[1] == v else y.idxs[1]
             if k != i:
                 prods, nnz, deg = spgemm_estimate(sx, x.idxs, sy, y.idxs, v, estimator)
-                cost = prods / SPGEMM_PRODUCTS + (12 * nnz + 8 * m) / HBM_BPS + 6 * LAUNCH_S
-                rs = Stats({i: int(m), k: sy.dims[k]}, nnz, False, deg, max(sx.esz, sy.esz))
-                opts.append(("spgemm", (v,), (i, k), rs, cost))
+                esz = max(sx.esz, sy.esz)
+                fmt = select_output_format(nnz, m, float(sy.dims[k]), esz)
+                if fmt == "dense":
+                    cells = m * float(sy.dims[k])
+                    cost = prods / SPGEMM_PRODUCTS + esz * cells / HBM_BPS + LAUNCH_S
+                    rs = Stats({i: int(m), k: sy.dims[k]}, cells, True,
+                               {i: float(sy.dims[k]), k: m}, esz)
+                    opts.append(("spgemm_dense", (v,), (i, k), rs, cost))
+                else:
+                    cost = prods / SPGEMM_PRODUCTS + (12 * nnz + 8 * m) / HBM_BPS + 6 * LAUNCH_S
+                    rs = Stats({i: int(m), k: sy.dims[k]}, nnz, False, deg, esz)
+                    opts.append(("spgemm", (v,), (i, k), rs, cost))
         # S[i,v] * X[i,v] -> y[i] (or a scalar when i is reduced too)
         if set(y.idxs) == set(x.idxs):
             elim = (v, i) if i in red_left else (v,)
@@ -417,6 +442,16 @@ def _run_step(st: Step, env: dict):
         if B.orient != A.orient:
             B = _other_orientation(b, B)
         return sparse_from_device(dev.spgemm(A, B)), (i, k)
+    if st.kind == "spgemm_dense":
+        i = ai[0] if ai[1] == v else ai[1]
+        k = bi[0] if bi[1] == v else bi[1]
+        A = sparse_operand(a, ai, (i, v))
+        B = sparse_operand(b, bi, (v, k))
+        if A.orient != "csr":
+            A = _other_orientation(a, A)
+        if B.orient != "csr":
+            B = _other_orientation(b, B)
+        return dense_from_device(dev.spgemm_dense(A, B)), (i, k)
     if st.kind == "ewise_reduce":
         i = ai[0] if ai[1] == v else ai[1]
         A = sparse_operand(a, ai, (i, v))

@@ -53,6 +53,12 @@ class Scalar:
     def value(self):
         return self.t.item()
 
+    def device_value(self, dtype) -> torch.Tensor:
+        """The 0-d device value, which kernels update in place (of `dtype`)."""
+        if self.t.dtype != dtype:
+            raise FinchGBUnsupported(f"Scalar of {self.t.dtype}, expected {dtype}")
+        return self.t
+
     def __float__(self):
         return float(self.t.item())
 
@@ -189,8 +195,8 @@ class GB300Scheduler:
 
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
-        for rule in (self._spmv, self._spmm, self._spgemm, self._sddmm, self._ewise, self._ewise_reduce,
-                     self._dot, self._dense_map, self._scalar):
+        for rule in (self._spmv, self._spmm, self._spmm_semiring, self._spgemm, self._sddmm, self._ewise,
+                     self._ewise_reduce, self._dot, self._dense_map, self._scalar):
             r = rule(m, out, accumulate)
             if r is not None:
                 if self.verbose:
@@ -253,6 +259,46 @@ class GB300Scheduler:
                 self.last_kernel = "fgb_spmm"
                 C = dev.spmm(A, B, C, flags=flags)
                 return dense_from_device(C)
+        return None
+
+    # -- C[i,k] <<min|max>>= A[i,j] + B[j,k], C[i,k] |= A[i,j] & B[j,k]: exact semiring products
+    def _spmm_semiring(self, m: Match, out, accumulate):
+        if m.agg not in ("min", "max", "|") or len(m.outs) != 2 or len(m.red) != 1:
+            return None
+        (i, k), (j,) = m.outs, m.red
+        for mul in ("+", "&"):
+            args = _args(m.core, mul)
+            if args is None or len(args) != 2 or (m.agg, mul) not in _SEMIRINGS:
+                continue
+            for a, b in (args, args[::-1]):
+                if not (isinstance(a, Access) and _is_sparse(a.tns) and set(a.idxs) == {i, j}
+                        and isinstance(b, Access) and set(b.idxs) == {j, k}):
+                    continue
+                sr = _SEMIRINGS[(m.agg, mul)]
+                # only A's stored entries are visited, which is exact when A's
+                # fill annihilates (*) into the identity of (+): -Inf for
+                # max-plus, +Inf for min-plus, false for or-and
+                # (src/symbolic/symbolic.jl:89-166)
+                fill = (a.tns.body if isinstance(a.tns, SwizzleArray) else a.tns).fill_value
+                want = {L.MAX_PLUS: -np.inf, L.MIN_PLUS: np.inf, L.OR_AND: False}[sr]
+                if not (fill == want or (sr == L.OR_AND and not fill)):
+                    raise FinchGBUnsupported(f"<<{m.agg}>>= over {a.tns!r} needs its fill {want}, not {fill}")
+                A = sparse_operand(a.tns, a.idxs, (i, j))
+                if A.orient == "csc":
+                    A = _csr_copy(a.tns, A)
+                if _is_dense(b.tns):
+                    B = dense_operand(b.tns, b.idxs, (j, k))
+                else:  # a sparse right operand: its dense copy in HBM, fill included
+                    bs = sparse_operand(b.tns, b.idxs, (j, k))
+                    bfill = (b.tns.body if isinstance(b.tns, SwizzleArray) else b.tns).fill_value
+                    B = dev.sparse_to_dense(bs, bfill)
+                if A.val is not None and A.val.dtype != B.dtype:
+                    raise FinchGBUnsupported(f"semiring product of {A.val.dtype} and {B.dtype}")
+                flags = L.ACCUMULATE if (out is not None and accumulate) else 0
+                C = None if out is None else dense_operand(out, (i, k), (i, k))
+                self.last_kernel = f"fgb_spmm_semiring[{sr}]"
+                C = dev.spmm_semiring(A, B, C, semiring=sr, flags=flags)
+                return dense_from_device(C, m.init if m.init is not None else want)
         return None
 
     # -- C[i,k] += A[i,j] * B[j,k] with both sparse: a sparse result (Gustavson)

@@ -170,6 +170,14 @@ FGB_API int fgb_narrow_index(fgb_ctx* ctx, const int64_t* src, int32_t* dst, int
 FGB_API int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr, int32_t* out_idx,
                   void* out_val, void* stream);
 
+/* Dense copy of a sparse matrix: out (row-major nrows x ncols, leading
+ * dimension ld, elements of A's val_t; one byte 0/1 for a Pattern) holds
+ * the stored entries of A and *fill (one host element of val_t) elsewhere
+ * -- the copy into Tensor(Dense(Dense(Element(fill))), A) that
+ * src/interface/copy.jl makes.  Synchronous. */
+FGB_API int fgb_sparse_to_dense(fgb_ctx* ctx, const fgb_sparse* A, const void* fill, void* out, int64_t ld,
+                                void* stream);
+
 /* Duplicate handling of fgb_coo_assemble: Julia's `combine` for fsparse. */
 typedef enum fgb_combine {
   FGB_COMBINE_ADD = 0, /* +  (the default; | for Bool values) */
@@ -222,6 +230,17 @@ FGB_API int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void
  * atomics. */
 FGB_API int fgb_spmm(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int64_t nk, void* C,
              int64_t ldc, int dtype, unsigned flags, void* stream);
+
+/* Semiring SpMM: C[i,k] <<add>>= mul(A[i,j], B[j,k]) over `semiring` (the
+ * fgb_spmv semirings), B row-major (ldb), C row-major (ldc).  MIN_PLUS and
+ * MAX_PLUS: values, B and C of `dtype` (F64, F32, I32, I64; integers wrap);
+ * OR_AND: Bool (or Pattern) A with Bool B and C; PLUS_TIMES is fgb_spmm.
+ * C starts at the semiring's identity unless FGB_ACCUMULATE.  A is CSR.
+ * Replaces `@einsum init=-Inf R[i,j] <<max>>= P[i,k] + Q[k,j]`
+ * (test/suites/interface_tests.jl:72-82) and its min-plus / or-and forms;
+ * results are exact (the reductions are order-free). */
+FGB_API int fgb_spmm_semiring(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* B, int64_t ldb,
+                              int64_t nk, void* C, int64_t ldc, int dtype, unsigned flags, void* stream);
 
 /* Schedule knobs of the load-balanced CSR SpMM (the autotuner's search
  * space).  CSR SpMM walks merge-path items of `path` steps (rows + stored
@@ -321,6 +340,16 @@ FGB_API int fgb_spgemm_symbolic(fgb_ctx* ctx, const fgb_sparse* A, const fgb_spa
                                 int64_t* c_ptr, int64_t* nnz_c, void* stream);
 FGB_API int fgb_spgemm_numeric(fgb_ctx* ctx, const fgb_sparse* A, const fgb_sparse* B, int dtype,
                                unsigned flags, fgb_sparse* C, void* stream);
+
+/* SpGEMM into a dense output: C (row-major A.nrows x B.ncols, leading
+ * dimension ldc, dtype F64/F32) = A * B for A, B of one orientation (each
+ * with its own ptr type and index base) -- the dense format Galley selects for a product
+ * whose estimated density passes one half
+ * (src/Galley/PhysicalOptimizer/format-selector.jl:27-65).  Each output sums
+ * its products in the order of k as fgb_spgemm_numeric does, so its values
+ * equal the sparse product's bit for bit (zero where nothing is stored). */
+FGB_API int fgb_spgemm_dense(fgb_ctx* ctx, const fgb_sparse* A, const fgb_sparse* B, int dtype, unsigned flags,
+                             void* C, int64_t ldc, void* stream);
 
 /* Elementwise ops of two same-shape CSR/CSC matrices (same orientation). */
 typedef enum {
@@ -589,6 +618,8 @@ typedef struct fgb_cg_options {
   int32_t chunk;         /* iterations per captured CUDA graph (even) */
   int32_t precision;     /* value type of the iteration SpMV: FGB_F64, FGB_F32 or FGB_BF16 */
   int64_t replace_every; /* FP64 residual replacement period in iterations (0 = only at the end) */
+  int32_t accumulate_fp64; /* 1: the FP32/BF16 SpMV widens its values and sums in FP64 (0: FP32 sums) */
+  int32_t reserved;
 } fgb_cg_options;
 
 typedef struct fgb_cg_result {
@@ -597,7 +628,7 @@ typedef struct fgb_cg_result {
   double true_rel_residual; /* ||b - A x|| / ||b|| at exit, FP64 */
   double seconds;           /* wall time of the solve */
   int32_t converged;
-  int32_t reserved;
+  int32_t compact_index;    /* 1: the iteration SpMV read 16-bit column offsets (a banded matrix) */
 } fgb_cg_result;
 
 /* Solves A x = b for SPD CSR A; x holds the initial guess and receives the

@@ -121,3 +121,21 @@ def test_non_sum_product_plans_go_to_the_kernel_matcher():
     assert g.estimator == "dc"
     with pytest.raises(ValueError):
         galley_scheduler(estimator="exact")
+
+
+@pytest.mark.parametrize("nnz,fmt,kind", [(2000, "sparse", "spgemm"), (60000, "dense", "spgemm_dense")])
+def test_spgemm_output_format_follows_estimated_density(nnz, fmt, kind):
+    """format-selector.jl:27-65: a product whose estimated density passes
+    one half is built dense, a sparse one as a sparse list."""
+    A, B = sparse(300, 300, nnz, 11), sparse(300, 300, nnz, 12)
+    q, p = plan_of(lazy(A) @ lazy(B))
+    assert [s.kind for s in p.steps] == [kind]
+    assert p.steps[0].fmt == fmt
+
+
+def test_select_output_format_thresholds():
+    from finchgb.galley import select_output_format
+
+    assert select_output_format(0.6 * 100 * 100, 100, 100, 8) == "dense"
+    assert select_output_format(0.4 * 100 * 100, 100, 100, 8) == "sparse"
+    assert select_output_format(0.9 * 4e5 * 1e5, 4e5, 1e5, 8) == "sparse"  # a dense copy above 3e10 cells

@@ -187,3 +187,44 @@ def test_einsum_sparse_times_sparse_is_spgemm(gpu_lib):
     C = F.einsum("C[i,j] += A[i,k] * B[k,j]", A=csc(Ad), B=csc(Bd))
     assert F.get_scheduler().last_kernel == "fgb_spgemm"
     assert np.array_equal(C.todense(), Ad @ Bd)
+
+
+@pytest.mark.parametrize("n,p,seed", [(3, 0.7, 0), (3, 0.7, 1), (40, 0.3, 2)])
+def test_einsum_max_plus_product(gpu_lib, n, p, seed):
+    """test/suites/interface_tests.jl:72-82 restated: P and Q are
+    Dense(SparseList(Element(-Inf))) with random integer-valued entries, and
+    `@einsum init=-Inf R[i,j] <<max>>= P[i,k] + Q[k,j]` equals the triple
+    loop R_ref[i,j] = max(R_ref[i,j], P[i,k] + Q[k,j]) exactly."""
+    rng = np.random.default_rng(seed)
+
+    def rand_tensor():
+        D = np.where(rng.random((n, n)) < p, rng.integers(-1000, 1000, (n, n)).astype(np.float64), -np.inf)
+        return D, F.Tensor(F.Dense(F.SparseList(F.Element(-np.inf))), D)
+
+    Pd, P = rand_tensor()
+    Qd, Q = rand_tensor()
+    R = F.einsum("R[i,j] <<max>>= P[i,k] + Q[k,j]", init=-np.inf, P=P, Q=Q)
+    R_ref = np.full((n, n), -np.inf)
+    for i in range(n):
+        for j in range(n):
+            for k in range(n):
+                R_ref[i, j] = max(R_ref[i, j], Pd[i, k] + Qd[k, j])
+    assert np.array_equal(R.todense(), R_ref)
+    # min-plus over a dense right operand, and or-and over Bool
+    Md = np.where(rng.random((n, n)) < p, rng.integers(0, 50, (n, n)).astype(np.float64), np.inf)
+    M = F.Tensor(F.Dense(F.SparseList(F.Element(np.inf))), Md)
+    X = rng.integers(0, 50, (n, 5)).astype(np.float64)
+    S = F.einsum("S[i,j] <<min>>= M[i,k] + X[k,j]", init=np.inf, M=M, X=dense2(X))
+    assert np.array_equal(S.todense(), np.min(Md[:, :, None] + X[None, :, :], axis=1))
+    Bd = rng.random((n, n)) < p
+    Bt = F.Tensor(F.Dense(F.SparseList(F.Element(False))), Bd)
+    Y = rng.random((n, 4)) < 0.5
+    O = F.einsum("O[i,j] |= B[i,k] & Y[k,j]", B=Bt, Y=dense2(Y))
+    assert np.array_equal(O.todense().astype(bool), (Bd.astype(int) @ Y.astype(int)) > 0)
+
+
+def test_einsum_max_plus_needs_the_annihilating_fill(gpu_lib):
+    D = np.array([[1.0, 0.0], [0.0, 2.0]])
+    P = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), D)  # fill 0 is not max-plus's annihilator
+    with pytest.raises(F.FinchGBUnsupported):
+        F.einsum("R[i,j] <<max>>= P[i,k] + Q[k,j]", init=-np.inf, P=P, Q=dense2(D))

@@ -66,3 +66,40 @@ def test_cg_finch_program_matches_native(gpu_lib):
     Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
     xn, res = cg.cg_solve(Ad, torch.from_numpy(b).cuda(), precision="f64", chunk=2)
     np.testing.assert_allclose(x.todense(), xn.cpu().numpy(), rtol=0, atol=1e-8)
+
+
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+def test_cg_fp64_accumulation_equals_fp64(gpu_lib, precision):
+    """Poisson values (4, -1) are exact in FP32 and BF16: widened to FP64 and
+    summed in FP64, the low-precision SpMV gives the FP64 iterates bit for
+    bit, so the solve takes the FP64 iteration count; the banded matrix is
+    read through 16-bit column offsets."""
+    A = poisson2d(64)
+    b = np.random.default_rng(5).uniform(-1, 1, A.nrows)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    x64, r64 = cg.cg_solve(Ad, bd, precision="f64", chunk=16, replace_every=64)
+    xl, rl = cg.cg_solve(Ad, bd, precision=precision, accumulate="f64", chunk=16, replace_every=64)
+    assert r64.compact_index and rl.compact_index
+    assert rl.iterations == r64.iterations and torch.equal(xl, x64)
+    assert rl.converged and true_residual(A, xl.cpu().numpy(), b) <= 1.2e-10
+
+
+def test_cg_wide_matrix_keeps_the_int32_index(gpu_lib):
+    """Columns farther than 32,767 from the diagonal: no compact index, same
+    tolerance reached (a diagonally dominant SPD matrix with far couplings)."""
+    n = 70000
+    rng = np.random.default_rng(9)
+    far = rng.integers(0, n, 2000)
+    rows = np.concatenate([np.arange(n), np.arange(n - 1), np.arange(1, n), far, (far + 40000) % n])
+    cols = np.concatenate([np.arange(n), np.arange(1, n), np.arange(n - 1), (far + 40000) % n, far])
+    vals = np.concatenate([np.full(n, 6.0), np.full(2 * (n - 1), -1.0), np.full(4000, -0.5)])
+    from finchgb.workloads import coo_to_csr
+
+    A = coo_to_csr(n, n, rows + 1, cols + 1, vals)
+    b = rng.uniform(-1, 1, n)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    for precision in ("f64", "f32"):
+        x, res = cg.cg_solve(Ad, torch.from_numpy(b).cuda(), precision=precision, rtol=1e-10, chunk=8)
+        assert res.converged and not res.compact_index
+        assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10

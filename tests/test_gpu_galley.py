@@ -76,3 +76,31 @@ def test_sparse_times_dense_matrix(gpu_lib):
     kinds = [st.kind for st in g.last_plan.steps]
     assert kinds in (["spmm", "spmm"], ["spgemm", "spmm"])
     np.testing.assert_allclose(host(out), Ah @ Bh @ D, rtol=1e-11, atol=1e-11)
+
+
+@pytest.mark.parametrize("nnz", [1500, 40000])
+def test_spgemm_format_selection_on_device(gpu_lib, nnz):
+    """A sparse product runs as a sparse-list SpGEMM, a dense-ish one into a
+    dense array; both equal the dense product exactly (small integers), and
+    the dense build equals the sparse SpGEMM's values bit for bit."""
+    (A, Ah), (B, Bh) = sparse(250, 200, nnz, 21, ints=True), sparse(200, 230, nnz, 22, ints=True)
+    g = galley_scheduler()
+    C = compute(lazy(A) @ lazy(B), ctx=g)
+    kinds = [s.kind for s in g.last_plan.steps]
+    assert kinds == (["spgemm_dense"] if nnz == 40000 else ["spgemm"])
+    assert np.array_equal(host(C), Ah @ Bh)
+    from finchgb import device as dev
+    from finchgb.scheduler import sparse_operand
+
+    Ad = sparse_operand(A, ("i", "j"), ("i", "j"))
+    Bd = sparse_operand(B, ("i", "j"), ("i", "j"))
+    D = dev.spgemm_dense(Ad, Bd).cpu().numpy()
+    S = dev.spgemm(Ad, Bd)
+    ptr, idx, val = S.to_host()
+    Sd = np.zeros_like(D)
+    f = np.repeat(np.arange(S.ncols if S.orient == "csc" else S.nrows), np.diff(ptr))
+    if S.orient == "csc":
+        Sd[idx - 1, f] = val
+    else:
+        Sd[f, idx - 1] = val
+    assert D.tobytes() == Sd.tobytes()
