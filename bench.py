@@ -637,7 +637,8 @@ def run_gpu(args):
         # the plugin API from host tensors (transfer + matcher + per-call SpMM + host result)
         line["e2e_api"], C_api = e2e_api(A_h, B_h, nbytes, steps=max(3, min(args.steps, 8)))
         line["e2e_api"]["max_rel_err_vs_fp64"] = spmm_fp64_error(A_h, B_h, C_api)["max_rel_err_vs_fp64"]
-        line["gpu_launches"] += line["e2e_api"]["steps"] * (16 + slabs * 2 + 2)
+        # per call: 2 index narrowings, the 16-kernel schedule build, 4 slabs x 2 bands, 2 fix-ups
+        line["gpu_launches"] += (line["e2e_api"]["steps"] + 1) * (2 + 16 + 4 * 2 + 2)
         del C_api
     line["cpu_baseline"] = None
     if rank == 0 and not args.skip_cpu_baseline:

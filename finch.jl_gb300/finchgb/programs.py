@@ -202,7 +202,7 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
     """Runs a matched program on the device; returns {name: tensor} of the
     outputs, or None if no graph program matches.  adjacency_rows(t) gives
     the CSR of a matrix tensor whose row i lists the j with t[i, j] stored."""
-    from .tensors import Tensor, dense_from_device, pair_from_device
+    from .tensors import dense_from_device
     from .scheduler import FinchGBUnsupported, Scalar, _device_vector
 
     m = match_bfs_round(prog)

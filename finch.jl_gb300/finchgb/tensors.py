@@ -192,12 +192,16 @@ class Tensor:
             self.data = np.ascontiguousarray(arr)
         elif self.kind == "csc":
             assert arr.ndim == 2
-            b = csc_from_dense(np.where(arr != fill, arr, 0) if arr.dtype != np.bool_ else arr)
-            if isinstance(fmt.lvl.lvl, Pattern):
-                b.val = None
-            else:
-                b.val = b.val.astype(self.dtype)
-            self.buf = b
+            # stored: every entry that differs from the fill (a 0 is stored when the fill is not 0)
+            mask = arr != fill
+            cols, rows = np.nonzero(mask.T)
+            lengths = np.bincount(cols, minlength=arr.shape[1]).astype(np.int64)
+            ptr = np.empty(arr.shape[1] + 1, dtype=np.int64)
+            ptr[0] = 1
+            np.cumsum(lengths, out=ptr[1:])
+            ptr[1:] += 1
+            val = None if isinstance(fmt.lvl.lvl, Pattern) else arr[rows, cols].astype(self.dtype)
+            self.buf = SparseBuffers(arr.shape[0], arr.shape[1], ptr, rows.astype(np.int64) + 1, val, "csc")
         elif self.kind == "sparse1":
             assert arr.ndim == 1
             nz = np.flatnonzero(arr != fill)
@@ -233,9 +237,9 @@ class Tensor:
                 out["f0"] = self.ddata[0].cpu().numpy()
                 out["f1"] = self.ddata[1].cpu().numpy()
                 return out
-            if self.data is None:
-                self.data = self.ddata.cpu().numpy()
-            return self.data
+            if self.data is not None:
+                return self.data
+            return self.ddata.cpu().numpy()  # read back each time: kernels may have updated it
         if self.kind == "coo":
             out = np.full(self.shape, self.fill_value, dtype=self.dtype)
             I, J, V = self.coo
@@ -466,6 +470,7 @@ def transfer(device, t):
         src = np.ascontiguousarray(t.data)
         tt = torch.from_numpy(src if src.dtype != np.bool_ else src.astype(np.uint8))
         t.ddata = tt.to(torch.device("cuda", idx))
+        t.data = None  # the HBM copy is the tensor now (kernels may update it in place)
         return t
     if t.kind == "coo":  # assembled in HBM: sort, fold duplicates, build ptr
         I, J, V = t.coo

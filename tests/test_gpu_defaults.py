@@ -1,6 +1,7 @@
 """Per-call SpMM and SDDMM with no schedule given.  Large problems (B or Y
 larger than 64 MB, at least 2^20 entries) take the virtual-row slab
-schedules built for the call, bit-identical to asking for them explicitly.
+schedules built for the call (for SpMM with two column bands),
+bit-identical to asking for them explicitly.
 While the stream is being captured into a CUDA graph those schedules, whose
 build reads sizes back, are not taken: the capture succeeds and replays the
 same product within tolerance."""
@@ -28,7 +29,7 @@ def test_spmm_default_is_the_slab_schedule_and_capture_safe(gpu_lib, big):
     A = upload(big)
     B = torch.randn((big.ncols, 32), dtype=torch.float32, device="cuda")  # 77 MB
     C_def = to_host(dev.spmm(A, B))
-    assert np.array_equal(C_def, to_host(dev.spmm(A, B, lanes=8, path=128, variant=3)))
+    assert np.array_equal(C_def, to_host(dev.spmm(A, B, lanes=8, path=128, variant=3, bands=2)))
     C = torch.empty((big.nrows, 32), dtype=torch.float32, device="cuda")
     g = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
