@@ -366,17 +366,22 @@ def suite_block(A_h, Ad) -> dict:
 
 def cg_lines(P, Pd, bd) -> dict:
     """CG to a true relative residual of 1e-10: FP64, and FP32/BF16-valued
-    SpMVs summed in FP32 or (values widened) in FP64.  Per-iteration bytes:
-    the SpMV's ptr, index (2-byte offsets when compact) and values, p and q,
-    and the updates' r, q, x, p traffic (80 bytes per row)."""
+    SpMVs summed in FP32, (values widened) in FP64, or with the whole
+    iteration in pairs of FP32 numbers.  Per-iteration bytes: the SpMV's ptr,
+    index (2-byte offsets when compact) and values, p and q, and the updates'
+    r, q, x, p traffic (80 bytes per row)."""
     from finchgb import cg
 
     lines = {}
-    for prec, acc in (("f64", "f64"), ("f32", "f32"), ("bf16", "f32"), ("f32", "f64"), ("bf16", "f64")):
+    for prec, acc in (("f64", "f64"), ("f32", "f32"), ("bf16", "f32"), ("f32", "f64"), ("bf16", "f64"),
+                      ("f32", "pair"), ("bf16", "pair")):
         x, res = cg.cg_solve(Pd, bd, precision=prec, rtol=1e-10, max_iter=60_000, accumulate=acc)
         vb = {"f64": 8, "f32": 4, "bf16": 2}[prec]
         ib = 2 if res.compact_index else 4
-        per_it = P.nnz * (ib + vb) + 4 * (P.nrows + 1) + 80 * P.nrows
+        # vectors per row: SpMV p, q; r update q, r, r; x/p update p, r, x, x, p
+        # (8-byte elements: FP64 or pairs); FP32 sums add p's FP32 copy (write
+        # and read)
+        per_it = P.nnz * (ib + vb) + 4 * (P.nrows + 1) + 80 * P.nrows + (8 * P.nrows if acc == "f32" else 0)
         ms_it = 1e3 * res.seconds / max(res.iterations, 1)
         key = prec if prec == "f64" else f"{prec}_values_{acc}_sums"
         lines[key] = {"seconds": round(res.seconds, 4), "iterations": res.iterations,
@@ -438,7 +443,7 @@ def run_gpu(args):
     slabs = -(-NK // (4 * plan_lanes))
     if plan is None and lanes == 0 and path == 0 and variant == 0:
         variant = 3  # the library's default for a B far larger than L2
-    vrow = variant in (2, 3, 4)
+    vrow = variant in (2, 3, 4, 5)
     if plan is None and vrow:
         # schedule built per call: count, 5 scans (2 kernels each), fill, a
         # 3-kernel radix sort and the gather, then the slab x band launches
@@ -990,7 +995,20 @@ def serve_layout(plan, mats, arena_floats):
     return virt % arena_floats, dep
 
 
-def serve_run(mode, mats, partners, plan, arena, window, arrivals=None, batch=128):
+def serve_tune(mats, partners):
+    """The serving autotuner on the library: per-class SpMV shapes, applied
+    to every server of the run (both modes compute rows the same way at a
+    given shape)."""
+    from finchgb.server import Server
+
+    with Server(mode="batched", pool_bytes=64 << 20, max_inflight=64) as srv:
+        for A in mats + partners:
+            srv.register(A)
+        t = srv.tune(reps=3)
+    return t, Server.shapes(t)
+
+
+def serve_run(mode, mats, partners, plan, arena, window, arrivals=None, batch=128, tuning=None):
     """Runs the request plan through a server; returns (seconds, latencies, stats).
 
     The FgbRequest records (pointers into a pinned arena) are built before the
@@ -1006,6 +1024,8 @@ def serve_run(mode, mats, partners, plan, arena, window, arrivals=None, batch=12
     with Server(mode=mode, pool_bytes=4 << 30, max_inflight=min(window, 4096)) as srv:
         ids = [srv.register(A) for A in mats]
         pids = [srv.register(B) for B in partners]
+        if tuning is not None:
+            srv.set_tuning(tuning)
         reqs = (L.FgbRequest * len(plan))()
         for i, (op, k, nk) in enumerate(plan):
             A = mats[k]
@@ -1137,7 +1157,7 @@ def _serve_plan(rng, n_req, mats, partners):
     return plan
 
 
-def serve_check(mats, partners, n: int = 48) -> dict:
+def serve_check(mats, partners, n: int = 48, tuning=None) -> dict:
     """Served results against the FP64 oracle: n mixed requests through the
     batched server; SpMV/SpMM as |got - fp64| / sum|terms|, masked multiply
     (one product per entry) exact."""
@@ -1152,6 +1172,8 @@ def serve_check(mats, partners, n: int = 48) -> dict:
     with Server(mode="batched", pool_bytes=1 << 30, max_inflight=256) as srv:
         ids = [srv.register(A) for A in mats]
         pids = [srv.register(B) for B in partners]
+        if tuning is not None:
+            srv.set_tuning(tuning)
         todo = []
         for q in range(n):
             op = ("spmv", "spmm", "masked_mul")[q % 3]
@@ -1193,7 +1215,8 @@ def served_block(min_seconds: float = 1.0) -> dict:
     requests each), then Poisson arrivals at the same rates for both modes
     (half and nine tenths of the per-call capacity) and at half the batched
     capacity for the batched mode, p50/p99 of each; clocks sampled; a sample
-    of served results against the FP64 oracle."""
+    of served results against the FP64 oracle.  Every server uses the SpMV
+    shapes the serving autotuner picked for the library's size classes."""
     import torch
 
     mats, partners = serve_library()
@@ -1208,14 +1231,16 @@ def served_block(min_seconds: float = 1.0) -> dict:
         return {"p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3)}
 
+    tuning, shapes = serve_tune(mats, partners)
+    out["spmv_shapes"] = shapes
     with ClockSampler(torch.cuda.current_device()) as clk:
         cap = {}
         for mode, n0 in (("batched", 400_000), ("per_call", 40_000)):
             plan = _serve_plan(rng, n0, mats, partners)
-            dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
+            dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, tuning=tuning)
             if dt < min_seconds:  # too short: again with enough requests
                 plan = _serve_plan(rng, int(n0 * 1.3 * min_seconds / dt), mats, partners)
-                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window)
+                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, tuning=tuning)
             cap[mode] = len(plan) / dt
             out[mode] = {"closed_loop": {"ops_per_s": round(cap[mode], 1), "requests": len(plan),
                                          "seconds": round(dt, 3), **lat_stats(lat),
@@ -1229,11 +1254,11 @@ def served_block(min_seconds: float = 1.0) -> dict:
             plan = _serve_plan(rng, n_req, mats, partners)
             arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
             for mode in modes:
-                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr)
+                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr, tuning=tuning)
                 out[mode][f"poisson_{name}"] = {"rate_per_s": round(lam, 1), "requests": n_req,
                                                 "seconds": round(dt, 3), **lat_stats(lat)}
     out["clocks"] = clk.summary()
-    out["oracle_check"] = serve_check(mats, partners)
+    out["oracle_check"] = serve_check(mats, partners, tuning=tuning)
     return out
 
 

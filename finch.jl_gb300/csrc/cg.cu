@@ -1,25 +1,38 @@
-// Conjugate gradients for SPD CSR systems with a low-precision SpMV and FP64
-// everything else, the Finch-expressed solver
+// Conjugate gradients for SPD CSR systems, the Finch-expressed solver
 //
 //   q = A p          @einsum q[i] += A[i,j] * p[j]
 //   alpha = rr / p.q @einsum s[] += p[i] * q[i]
 //   x += alpha p;  r -= alpha q;  rr' = r.r;  p = r + (rr'/rr) p
 //
-// run on the GPU.  The iteration SpMV reads FP32 or BF16 values (or FP64),
-// converts p to FP32 per product and accumulates in FP32 (or, when asked,
-// widens the values to FP64 and accumulates in FP64); x, r, p, q, the dot
-// products and the updates are FP64.  A matrix whose columns lie within
-// 32,767 of the diagonal is read through 16-bit column offsets j - i.  Accuracy is won back by reliable
-// updates: every `replace_every` iterations, and whenever the recursive
-// residual reaches the tolerance, the true residual r = b - A x is recomputed
-// with the FP64 matrix and replaces the recursive one (residual replacement
-// keeping the search direction), and the solve stops only when that true
-// residual is below rtol * ||b||.
+// run on the GPU in one of four arithmetic modes:
+//   FP64          values, sums, vectors and updates in FP64;
+//   FP32 sums     FP32 or BF16 values times an FP32 copy of p, summed in
+//                 FP32; x, r, p, q, dots and updates FP64;
+//   FP64 sums     FP32 or BF16 values widened to FP64 and summed in FP64;
+//   pair sums     FP32 or BF16 values, and everything per row or per stored
+//                 entry -- the SpMV sums, x, r, p, q, the dot products and
+//                 updates -- in pairs of FP32 numbers (an unevaluated sum
+//                 hi + lo with about 48 significant bits: Dekker's exact
+//                 product through an FMA and Knuth's TwoSum, in the
+//                 double-single arithmetic of Bailey's DSFUN and the QD
+//                 library of Hida, Li and Bailey).  GB300 runs FP32 far
+//                 faster than FP64, whose narrow pipe bounds the FP64 modes
+//                 (an FP64 convert costs about as much as an FP64 FMA), so
+//                 this mode executes no FP64 instruction per row or entry.
+// A matrix whose columns lie within 32,767 of the diagonal is read through
+// 16-bit column offsets j - i.  Accuracy is won back by reliable updates:
+// every `replace_every` iterations, and whenever the recursive residual
+// reaches the tolerance, the true residual r = b - A x is recomputed with
+// the FP64 matrix in FP64 and replaces the recursive one (residual
+// replacement keeping the search direction while the two residuals agree
+// within a factor of two, restarting it from the new residual otherwise),
+// and the solve stops only when that true residual is below rtol * ||b||.
 //
 // One iteration is three kernels -- SpMV fused with the p.q partials; the r
 // update (every block folds the p.q partials itself) fused with the r.r
 // partials; the x and p updates fused with the folds -- so no scalar ever
-// leaves the device, and p is read once by the updates.  Every partial is folded in a fixed order: the solve is
+// leaves the device, and p is read once by the updates.  Partials are FP64
+// and folded by one warp per block in a fixed order: the solve is
 // deterministic.  A chunk of iterations is captured once in a CUDA graph and
 // replayed; the host reads the residual history once per chunk.
 #include <chrono>
@@ -53,15 +66,66 @@ __device__ __forceinline__ T cg_block_sum(T v, T* sh) {
   return v;  // valid in thread 0
 }
 
-// Every block folds the same partials in the same order.
-__device__ __forceinline__ double fold_parts(const double* __restrict__ part, int nparts, double* sh) {
+// The partials folded by one warp: lane l sums l, l + 32, ..., then a fixed
+// shuffle tree, so every block folds them in the same order and the other
+// warps spend no FP64 instruction on it.  Call from warp 0; every lane of
+// it gets the sum.
+__device__ __forceinline__ double warp_fold(const double* __restrict__ part, int nparts) {
   double s = 0.0;
-  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
-  s = cg_block_sum(s, sh);
+  for (int i = threadIdx.x & 31; i < nparts; i += 32) s += part[i];
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  return s;
+}
+
+// ---- pairs of FP32 numbers (hi + lo, |lo| <= ulp(hi) / 2)
+// The intrinsics keep every operation a separately rounded IEEE operation.
+__device__ __forceinline__ float2 two_sum(float a, float b) {  // Knuth: s + e == a + b exactly
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 quick_two_sum(float a, float b) {  // Dekker, |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {  // the accurate pair sum
+  float2 s = two_sum(a.x, b.x);
+  const float2 t = two_sum(a.y, b.y);
+  s = quick_two_sum(s.x, __fadd_rn(s.y, t.x));
+  return quick_two_sum(s.x, __fadd_rn(s.y, t.y));
+}
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {  // exact hi product by FMA
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e));
+  return quick_two_sum(p, e);
+}
+__device__ __forceinline__ float2 ff_mul_f(float a, float2 b) {  // a float times a pair
+  const float p = __fmul_rn(a, b.x);
+  return quick_two_sum(p, __fmaf_rn(a, b.y, __fmaf_rn(a, b.x, -p)));
+}
+__device__ __forceinline__ float2 ff_from_double(double d) {
+  const float hi = __double2float_rn(d);
+  return make_float2(hi, __double2float_rn(d - (double)hi));
+}
+__device__ __forceinline__ double ff_to_double(float2 v) { return (double)v.x + (double)v.y; }
+
+__device__ __forceinline__ float2 ff_block_sum(float2 v, float2* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1)
+    v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)));
   __syncthreads();
-  if (threadIdx.x == 0) sh[32] = s;
+  if (lane == 0) sh[w] = v;
   __syncthreads();
-  return sh[32];
+  v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : make_float2(0.f, 0.f);
+  if (w == 0) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1)
+      v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)));
+  }
+  return v;  // valid in thread 0
 }
 
 template <class VT>
@@ -78,19 +142,21 @@ __device__ __forceinline__ int64_t cg_col(const IX* __restrict__ ix, int64_t k, 
 }
 
 // q = A p (one row per thread, j ascending) and the block partial of p.q.
-// ACC = float: values converted to FP32 and p rounded to FP32 per product;
-// ACC = double: values (FP64, FP32 or BF16) widened to FP64 and the products
-// summed in FP64 -- with the FP64 values, the FP64 SpMV.
+// ACC = float: values converted to FP32 times p32, the FP32 copy of p that
+// the p update writes, summed in FP32; ACC = double: values (FP64, FP32 or
+// BF16) widened to FP64 and the products summed in FP64 -- with the FP64
+// values, the FP64 SpMV.
 template <class VT, class ACC, class PtrT, class IX>
 __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
     int64_t n, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
-    int base, const double* __restrict__ p, double* __restrict__ q, double* __restrict__ part) {
+    int base, const double* __restrict__ p, const float* __restrict__ p32, double* __restrict__ q,
+    double* __restrict__ part) {
   __shared__ double sh[33];
   double dot = 0.0;
   auto term = [&](int64_t k, int64_t row, ACC acc) -> ACC {
     const int64_t j = cg_col(idx, k, row, base);
     if constexpr (sizeof(ACC) == 4)
-      return __fmaf_rn(cg_val(val, k), (float)__ldg(p + j), acc);
+      return __fmaf_rn(cg_val(val, k), __ldg(p32 + j), acc);
     else if constexpr (sizeof(VT) == 8)
       return __fma_rn((double)__ldg((const double*)val + k), __ldg(p + j), acc);
     else
@@ -123,6 +189,37 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
   if (threadIdx.x == 0) part[blockIdx.x] = dot;
 }
 
+// The pair-sum SpMV: q = A p and the block partial of p.q, all in pairs;
+// the partial leaves the block as one FP64 number.
+template <class VT, class PtrT, class IX>
+__global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
+    int64_t n, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
+    int base, const float2* __restrict__ p, float2* __restrict__ q, double* __restrict__ part) {
+  __shared__ float2 sh[32];
+  float2 dot = make_float2(0.f, 0.f);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+    const int64_t i2 = i + stride;
+    const bool two = i2 < n;
+    const int64_t a0 = ld_ptr(ptr, i) - base, a1 = ld_ptr(ptr, i + 1) - base;
+    const int64_t b0 = two ? ld_ptr(ptr, i2) - base : 0, b1 = two ? ld_ptr(ptr, i2 + 1) - base : 0;
+    float2 acc_a = make_float2(0.f, 0.f), acc_b = make_float2(0.f, 0.f);
+    const int64_t la = a1 - a0, lb = b1 - b0;
+    for (int64_t t = 0; t < (la > lb ? la : lb); ++t) {
+      if (t < la) acc_a = ff_add(acc_a, ff_mul_f(cg_val(val, a0 + t), __ldg(p + cg_col(idx, a0 + t, i, base))));
+      if (t < lb) acc_b = ff_add(acc_b, ff_mul_f(cg_val(val, b0 + t), __ldg(p + cg_col(idx, b0 + t, i2, base))));
+    }
+    q[i] = acc_a;
+    dot = ff_add(dot, ff_mul(__ldg(p + i), acc_a));
+    if (two) {
+      q[i2] = acc_b;
+      dot = ff_add(dot, ff_mul(__ldg(p + i2), acc_b));
+    }
+  }
+  dot = ff_block_sum(dot, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = ff_to_double(dot);
+}
+
 // The compact index of a banded matrix: off[k] = j - i for the stored
 // entries of row i, and *bad set when some |j - i| does not fit 16 bits.
 template <class PtrT>
@@ -141,15 +238,27 @@ __global__ void cg_offsets(int64_t n, const PtrT* __restrict__ ptr, const int* _
   }
 }
 
-// alpha = rr[slot] / (p.q);  r -= alpha q;  partials of r.r.  (x += alpha p
-// waits for the p update, which reads p anyway: one pass over p less.)
+// alpha = rr[slot] / (p.q), formed once per block by thread 0 (a vanished
+// curvature, p.q == 0, only happens once r is exactly zero).
+__device__ __forceinline__ double cg_alpha(const double* __restrict__ part_pq, int nparts,
+                                           const double* __restrict__ rr, int slot) {
+  const double pq = warp_fold(part_pq, nparts);
+  return pq != 0.0 ? rr[slot] / pq : 0.0;
+}
+
+// alpha;  r -= alpha q;  partials of r.r.  (x += alpha p waits for the p
+// update, which reads p anyway: one pass over p less.)
 __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_r(
     int64_t n, double* __restrict__ r, const double* __restrict__ q, const double* __restrict__ part_pq,
     int nparts, const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
   __shared__ double sh[33];
-  const double pq = fold_parts(part_pq, nparts, sh);
-  // a vanished curvature (p.q == 0) only happens once r is exactly zero
-  const double alpha = pq != 0.0 ? rr[slot] / pq : 0.0;
+  __shared__ double s_alpha;
+  if (threadIdx.x < 32) {
+    const double a = cg_alpha(part_pq, nparts, rr, slot);
+    if (threadIdx.x == 0) s_alpha = a;
+  }
+  __syncthreads();
+  const double alpha = s_alpha;
   double acc = 0.0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -180,16 +289,28 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_r(
 
 // alpha as cg_update_r formed it (the same fold of the p.q partials);
 // x += alpha p; rr' = fold(r.r partials); p = r + (rr' / rr[slot_in]) p;
-// rr[slot_out] = rr'.  x's update is the one of the plain loop, bit for bit.
+// rr[slot_out] = rr'; p32 (when given) = p rounded to FP32, the FP32-sum
+// SpMV's operand.  x's update is the one of the plain loop, bit for bit.
 __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xp(
     int64_t n, double* __restrict__ x, const double* __restrict__ r, double* __restrict__ p,
-    const double* __restrict__ part_pq, int nparts_pq, const double* __restrict__ part_rr, int nparts,
-    double* __restrict__ rr, int slot_in, int slot_out, double* __restrict__ hist, int64_t it) {
-  __shared__ double sh[33];
-  const double pq = fold_parts(part_pq, nparts_pq, sh);
-  const double alpha = pq != 0.0 ? rr[slot_in] / pq : 0.0;
-  const double rr_new = fold_parts(part_rr, nparts, sh);
-  const double beta = rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0;
+    float* __restrict__ p32, const double* __restrict__ part_pq, int nparts_pq,
+    const double* __restrict__ part_rr, int nparts, double* __restrict__ rr, int slot_in, int slot_out,
+    double* __restrict__ hist, int64_t it) {
+  __shared__ double s_ab[2];
+  if (threadIdx.x < 32) {
+    const double a = cg_alpha(part_pq, nparts_pq, rr, slot_in);
+    const double rr_new = warp_fold(part_rr, nparts);
+    if (threadIdx.x == 0) {
+      s_ab[0] = a;
+      s_ab[1] = rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0;
+      if (blockIdx.x == 0) {  // slot_out != slot_in: no block reads it here
+        rr[slot_out] = rr_new;
+        hist[it] = rr_new;
+      }
+    }
+  }
+  __syncthreads();
+  const double alpha = s_ab[0], beta = s_ab[1];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
@@ -203,17 +324,98 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xp(
 #pragma unroll
     for (int u = 0; u < CG_ILP; ++u) {
       x[i + u * stride] = __fma_rn(alpha, pv[u], xv[u]);
-      p[i + u * stride] = __fma_rn(beta, pv[u], rv[u]);
+      const double pn = __fma_rn(beta, pv[u], rv[u]);
+      p[i + u * stride] = pn;
+      if (p32) p32[i + u * stride] = __double2float_rn(pn);
     }
   }
   for (; i < n; i += stride) {
     const double pi = p[i];
     x[i] = __fma_rn(alpha, pi, x[i]);
-    p[i] = __fma_rn(beta, pi, r[i]);
+    const double pn = __fma_rn(beta, pi, r[i]);
+    p[i] = pn;
+    if (p32) p32[i] = __double2float_rn(pn);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {  // slot_out != slot_in: no block reads it here
-    rr[slot_out] = rr_new;
-    hist[it] = rr_new;
+}
+
+// The pair-sum r update: r -= alpha q in pairs, partials of r.r.
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cgp_update_r(
+    int64_t n, float2* __restrict__ r, const float2* __restrict__ q, const double* __restrict__ part_pq,
+    int nparts, const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
+  __shared__ float2 sh[32];
+  __shared__ float2 s_na;
+  if (threadIdx.x < 32) {
+    const double a = cg_alpha(part_pq, nparts, rr, slot);
+    if (threadIdx.x == 0) s_na = ff_from_double(-a);
+  }
+  __syncthreads();
+  const float2 na = s_na;
+  float2 acc = make_float2(0.f, 0.f);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
+    float2 qv[CG_ILP], rv[CG_ILP];
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      qv[u] = q[i + u * stride];
+      rv[u] = r[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      const float2 ri = ff_add(rv[u], ff_mul(na, qv[u]));
+      r[i + u * stride] = ri;
+      acc = ff_add(acc, ff_mul(ri, ri));
+    }
+  }
+  for (; i < n; i += stride) {
+    const float2 ri = ff_add(r[i], ff_mul(na, q[i]));
+    r[i] = ri;
+    acc = ff_add(acc, ff_mul(ri, ri));
+  }
+  acc = ff_block_sum(acc, sh);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = ff_to_double(acc);
+}
+
+// The pair-sum x and p updates (alpha, beta formed in FP64 as above).
+__global__ void __launch_bounds__(CG_UPD_THREADS, 1) cgp_update_xp(
+    int64_t n, float2* __restrict__ x, const float2* __restrict__ r, float2* __restrict__ p,
+    const double* __restrict__ part_pq, int nparts_pq, const double* __restrict__ part_rr, int nparts,
+    double* __restrict__ rr, int slot_in, int slot_out, double* __restrict__ hist, int64_t it) {
+  __shared__ float2 s_ab[2];
+  if (threadIdx.x < 32) {
+    const double a = cg_alpha(part_pq, nparts_pq, rr, slot_in);
+    const double rr_new = warp_fold(part_rr, nparts);
+    if (threadIdx.x == 0) {
+      s_ab[0] = ff_from_double(a);
+      s_ab[1] = ff_from_double(rr[slot_in] != 0.0 ? rr_new / rr[slot_in] : 0.0);
+      if (blockIdx.x == 0) {
+        rr[slot_out] = rr_new;
+        hist[it] = rr_new;
+      }
+    }
+  }
+  __syncthreads();
+  const float2 alpha = s_ab[0], beta = s_ab[1];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + (CG_ILP - 1) * stride < n; i += CG_ILP * stride) {
+    float2 pv[CG_ILP], rv[CG_ILP], xv[CG_ILP];
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      pv[u] = p[i + u * stride];
+      rv[u] = r[i + u * stride];
+      xv[u] = x[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < CG_ILP; ++u) {
+      x[i + u * stride] = ff_add(xv[u], ff_mul(alpha, pv[u]));
+      p[i + u * stride] = ff_add(rv[u], ff_mul(beta, pv[u]));
+    }
+  }
+  for (; i < n; i += stride) {
+    const float2 pi = p[i];
+    x[i] = ff_add(x[i], ff_mul(alpha, pi));
+    p[i] = ff_add(r[i], ff_mul(beta, pi));
   }
 }
 
@@ -246,15 +448,34 @@ __global__ void __launch_bounds__(CG_THREADS) cg_residual(
   }
 }
 
-// out[slot] = fold(part); optionally p = r (restart of the direction).
-__global__ void __launch_bounds__(CG_THREADS) cg_fold_set(const double* __restrict__ part, int nparts,
-                                                          double* __restrict__ out, int slot) {
-  __shared__ double sh[33];
-  const double s = fold_parts(part, nparts, sh);
+// out[slot] = fold(part).
+__global__ void cg_fold_set(const double* __restrict__ part, int nparts, double* __restrict__ out, int slot) {
+  const double s = warp_fold(part, nparts);  // launched with one warp
   if (threadIdx.x == 0) out[slot] = s;
 }
 
-__global__ void cg_copy(int64_t n, const double* __restrict__ src, double* __restrict__ dst) {
+// p = r (a restart of the search direction), with p's FP32 copy when given.
+__global__ void cg_copy(int64_t n, const double* __restrict__ src, double* __restrict__ dst,
+                        float* __restrict__ dst32) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    dst[i] = src[i];
+    if (dst32) dst32[i] = __double2float_rn(src[i]);
+  }
+}
+
+// FP64 vector <-> pairs (the pair mode's entry to and exit from FP64).
+__global__ void cgp_from_f64(int64_t n, const double* __restrict__ src, float2* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = ff_from_double(src[i]);
+}
+__global__ void cgp_to_f64(int64_t n, const float2* __restrict__ src, double* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = ff_to_double(src[i]);
+}
+__global__ void cgp_copy(int64_t n, const float2* __restrict__ src, float2* __restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     dst[i] = src[i];
@@ -263,54 +484,72 @@ __global__ void cg_copy(int64_t n, const double* __restrict__ src, double* __res
 struct CgBuffers {
   double *r = nullptr, *p = nullptr, *q = nullptr, *part_a = nullptr, *part_b = nullptr,
          *part_c = nullptr, *rr = nullptr, *bb = nullptr, *hist = nullptr;
+  float* p32 = nullptr;                      // FP32-sum mode: p rounded to FP32
+  float2 *r2 = nullptr, *p2 = nullptr, *q2 = nullptr, *x2 = nullptr;  // pair mode
 };
+
+enum CgMode { CG_F32_SUMS = 0, CG_F64_SUMS = 1, CG_PAIR_SUMS = 2 };
 
 // The SpMV's own grid: at most `grid` blocks and no more than fit the SMs at
 // once (its two rows per thread take more registers than the updates).
-template <class VT, class ACC, class PtrT, class IX>
-static int dot_grid_t(int grid, int sms) {
-  static const int occ = [] {  // once per process (one device model); thread-safe
-    int o = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cg_spmv_dot<VT, ACC, PtrT, IX>, CG_THREADS, 0);
-    return o > 0 ? o : 1;
-  }();
-  return std::max(1, std::min(grid, occ * sms));
+template <class K>
+static int occupancy_grid(K kernel, int grid, int sms) {
+  int o = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, CG_THREADS, 0);
+  return std::max(1, std::min(grid, (o > 0 ? o : 1) * sms));
 }
 
-// The iteration SpMV: value type (precision), accumulation (FP64 for the
-// FP64 matrix or when asked) and index form (16-bit offsets when compact).
-template <class VT, class ACC, class PtrT, class IX>
-static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int grid, int sms, const double* p, double* q,
-                      double* part, cudaStream_t s, bool launch) {
-  const int g = dot_grid_t<VT, ACC, PtrT, IX>(grid, sms);
-  if (launch)
-    cg_spmv_dot<VT, ACC, PtrT, IX><<<g, CG_THREADS, 0, s>>>(A->nrows, (const PtrT*)A->ptr, ix, (const VT*)A->val,
-                                                           A->index_base, p, q, part);
-  return g;
+// The iteration SpMV of one mode, value type and index form.
+template <class VT, class PtrT, class IX>
+static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int sms, const CgBuffers& b,
+                      cudaStream_t s, bool launch) {
+  const int64_t n = A->nrows;
+  const PtrT* ptr = (const PtrT*)A->ptr;
+  const VT* val = (const VT*)A->val;
+  const int base = A->index_base;
+  if constexpr (sizeof(VT) == 8) {  // the FP64 matrix: FP64 sums
+    static const int g0 = occupancy_grid(cg_spmv_dot<VT, double, PtrT, IX>, 1 << 30, 1);
+    const int g = std::max(1, std::min(grid, g0 * sms));
+    if (launch) cg_spmv_dot<VT, double, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, nullptr, b.q, b.part_a);
+    return g;
+  } else {
+    if (mode == CG_PAIR_SUMS) {
+      static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX>, 1 << 30, 1);
+      const int g = std::max(1, std::min(grid, g0 * sms));
+      if (launch) cgp_spmv_dot<VT, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
+      return g;
+    }
+    if (mode == CG_F64_SUMS) {
+      static const int g0 = occupancy_grid(cg_spmv_dot<VT, double, PtrT, IX>, 1 << 30, 1);
+      const int g = std::max(1, std::min(grid, g0 * sms));
+      if (launch) cg_spmv_dot<VT, double, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, nullptr, b.q, b.part_a);
+      return g;
+    }
+    static const int g0 = occupancy_grid(cg_spmv_dot<VT, float, PtrT, IX>, 1 << 30, 1);
+    const int g = std::max(1, std::min(grid, g0 * sms));
+    if (launch) cg_spmv_dot<VT, float, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, b.p32, b.q, b.part_a);
+    return g;
+  }
 }
 
 template <class PtrT, class IX>
-static int spmv_dot_ix(const fgb_sparse* A, const IX* ix, int precision, bool acc64, int grid, int sms,
-                       const double* p, double* q, double* part, cudaStream_t s, bool launch) {
-  if (precision == FGB_F64)
-    return spmv_dot_t<double, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
-  if (precision == FGB_BF16)
-    return acc64 ? spmv_dot_t<__nv_bfloat16, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch)
-                 : spmv_dot_t<__nv_bfloat16, float, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
-  return acc64 ? spmv_dot_t<float, double, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch)
-               : spmv_dot_t<float, float, PtrT, IX>(A, ix, grid, sms, p, q, part, s, launch);
+static int spmv_dot_ix(const fgb_sparse* A, const IX* ix, int precision, int mode, int grid, int sms,
+                       const CgBuffers& b, cudaStream_t s, bool launch) {
+  if (precision == FGB_F64) return spmv_dot_t<double, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
+  if (precision == FGB_BF16) return spmv_dot_t<__nv_bfloat16, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
+  return spmv_dot_t<float, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
 }
 
 // Launches (launch = true) or sizes (false) the iteration SpMV; returns its grid.
-static int spmv_dot(const fgb_sparse* A, const int16_t* off, int precision, bool acc64, int grid, int sms,
-                    const double* p, double* q, double* part, cudaStream_t s, bool launch) {
+static int spmv_dot(const fgb_sparse* A, const int16_t* off, int precision, int mode, int grid, int sms,
+                    const CgBuffers& b, cudaStream_t s, bool launch) {
   const bool i32 = A->ptr_t == FGB_I32;
   if (off)
-    return i32 ? spmv_dot_ix<int32_t, int16_t>(A, off, precision, acc64, grid, sms, p, q, part, s, launch)
-               : spmv_dot_ix<int64_t, int16_t>(A, off, precision, acc64, grid, sms, p, q, part, s, launch);
+    return i32 ? spmv_dot_ix<int32_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch)
+               : spmv_dot_ix<int64_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch);
   const int* idx = (const int*)A->idx;
-  return i32 ? spmv_dot_ix<int32_t, int>(A, idx, precision, acc64, grid, sms, p, q, part, s, launch)
-             : spmv_dot_ix<int64_t, int>(A, idx, precision, acc64, grid, sms, p, q, part, s, launch);
+  return i32 ? spmv_dot_ix<int32_t, int>(A, idx, precision, mode, grid, sms, b, s, launch)
+             : spmv_dot_ix<int64_t, int>(A, idx, precision, mode, grid, sms, b, s, launch);
 }
 
 template <class PtrT>
@@ -343,6 +582,10 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   const int precision = opt->precision;
   if (precision != FGB_F64 && precision != FGB_F32 && precision != FGB_BF16)
     return set_error(FGB_EINVAL, "fgb_cg_solve: precision must be F64, F32 or BF16");
+  if (opt->accumulate < FGB_CG_SUM_F32 || opt->accumulate > FGB_CG_SUM_PAIR)
+    return set_error(FGB_EINVAL, "fgb_cg_solve: accumulate must be FGB_CG_SUM_F32, _F64 or _PAIR");
+  if (precision == FGB_F64 && opt->accumulate == FGB_CG_SUM_PAIR)
+    return set_error(FGB_EINVAL, "fgb_cg_solve: pair sums take FP32 or BF16 values");
   const fgb_sparse* Ait = A64;
   if (precision != FGB_F64) {
     if (!Alow) return set_error(FGB_EINVAL, "fgb_cg_solve: low-precision matrix missing");
@@ -370,7 +613,9 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   cudaGraphExec_t exec = nullptr;
   CgBuffers bufs;
   int16_t* off = nullptr;  // the compact index (16-bit column offsets), when it fits
-  const bool acc64 = precision == FGB_F64 || opt->accumulate_fp64 != 0;
+  const int mode = precision == FGB_F64 ? CG_F64_SUMS : opt->accumulate;
+  const bool pair = mode == CG_PAIR_SUMS;
+  bool pair_live = false;  // x2 holds the iterate (x is refreshed from it)
   int64_t hist_cap = 0;
   const int grid = grid_for(n, CG_THREADS, ctx->num_sms, 8);  // full occupancy: streaming kernels
   const bool i32 = A64->ptr_t == FGB_I32;  // ptr width of the FP64 matrix
@@ -384,11 +629,29 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev, 0);
     const size_t vec = sizeof(double) * n;
     hist_cap = opt->max_iter + chunk;
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&bufs.r, vec * 3 + sizeof(double) * (3 * grid + 4 + hist_cap), s);
+    // FP64 r, p, q (pair mode: r only, for the replacements), the pair
+    // vectors or p's FP32 copy, then partials, scalars and the history
+    const size_t f64_bytes = vec * (pair ? 1 : 3);
+    const size_t extra = pair ? sizeof(float2) * n * 4 : (mode == CG_F32_SUMS ? sizeof(float) * n : 0);
+    const size_t extra_off = (f64_bytes + 255) & ~size_t(255);
+    const size_t tail_off = (extra_off + extra + 255) & ~size_t(255);
+    char* base_ptr = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&base_ptr, tail_off + sizeof(double) * (3 * grid + 4 + hist_cap), s);
     if (e != cudaSuccess) { fail(FGB_ENOMEM, "setup", e); break; }
-    bufs.p = bufs.r + n;
-    bufs.q = bufs.p + n;
-    bufs.part_a = bufs.q + n;
+    bufs.r = (double*)base_ptr;
+    if (!pair) {
+      bufs.p = bufs.r + n;
+      bufs.q = bufs.p + n;
+    }
+    if (pair) {
+      bufs.r2 = (float2*)(base_ptr + extra_off);
+      bufs.p2 = bufs.r2 + n;
+      bufs.q2 = bufs.p2 + n;
+      bufs.x2 = bufs.q2 + n;
+    } else if (mode == CG_F32_SUMS) {
+      bufs.p32 = (float*)(base_ptr + extra_off);
+    }
+    bufs.part_a = (double*)(base_ptr + tail_off);
     bufs.part_b = bufs.part_a + grid;
     bufs.part_c = bufs.part_b + grid;
     bufs.rr = bufs.part_c + grid;  // [0], [1]: r.r slots; [2]: b.b
@@ -396,9 +659,15 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     // r = b - A x0, rr[0] = r.r, bb = b.b, p = r
     if (i32) launch_residual<int32_t>(A64, grid, x, b, bufs.r, bufs.part_a, bufs.part_b, s);
     else launch_residual<int64_t>(A64, grid, x, b, bufs.r, bufs.part_a, bufs.part_b, s);
-    cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
-    cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_b, grid, bufs.rr, 2);
-    cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p);
+    cg_fold_set<<<1, 32, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
+    cg_fold_set<<<1, 32, 0, s>>>(bufs.part_b, grid, bufs.rr, 2);
+    if (pair) {
+      cgp_from_f64<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.r2);
+      cgp_from_f64<<<grid, CG_THREADS, 0, s>>>(n, x, bufs.x2);
+      cgp_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r2, bufs.p2);
+    } else {
+      cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p, bufs.p32);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) { fail(FGB_ECUDA, "setup kernels", e); break; }
     double rr_bb[3];
     if ((e = cudaMemcpyAsync(rr_bb, bufs.rr, sizeof(rr_bb), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -410,6 +679,7 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
       res->true_rel_residual = bnorm > 0 ? sqrt(rr_bb[0]) / bnorm : 0.0;
       break;
     }
+    pair_live = pair;
     // The compact index: 16-bit column offsets j - i when the matrix is
     // banded that tightly (built once; the int32 index otherwise).
     if (n > 0 && Ait->nnz > 0) {
@@ -432,14 +702,21 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     // one chunk of iterations, captured once (slots alternate; chunk is even)
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { fail(FGB_ECUDA, "capture", e); break; }
     const int grid_upd = grid_for(n, CG_UPD_THREADS, ctx->num_sms, 1);  // <= grid partial slots
-    const int grid_dot = spmv_dot(Ait, off, precision, acc64, grid, ctx->num_sms, nullptr, nullptr, nullptr, s, false);
+    const int grid_dot = spmv_dot(Ait, off, precision, mode, grid, ctx->num_sms, bufs, s, false);
     for (int t = 0; t < chunk; ++t) {
       const int si = t & 1, so = si ^ 1;
-      spmv_dot(Ait, off, precision, acc64, grid, ctx->num_sms, bufs.p, bufs.q, bufs.part_a, s, true);
-      cg_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
-                                                     bufs.part_b);
-      cg_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.part_a, grid_dot, bufs.part_b,
-                                                      grid_upd, bufs.rr, si, so, bufs.hist, t);
+      spmv_dot(Ait, off, precision, mode, grid, ctx->num_sms, bufs, s, true);
+      if (pair) {
+        cgp_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r2, bufs.q2, bufs.part_a, grid_dot, bufs.rr, si,
+                                                        bufs.part_b);
+        cgp_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.x2, bufs.r2, bufs.p2, bufs.part_a, grid_dot,
+                                                         bufs.part_b, grid_upd, bufs.rr, si, so, bufs.hist, t);
+      } else {
+        cg_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
+                                                       bufs.part_b);
+        cg_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.p32, bufs.part_a, grid_dot,
+                                                        bufs.part_b, grid_upd, bufs.rr, si, so, bufs.hist, t);
+      }
     }
     e = cudaStreamEndCapture(s, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -460,18 +737,24 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
         // the next chunk); the search direction is kept.  If p has vanished
         // (the recursive residual reached zero), p.q = 0 gives alpha = 0 and
         // the next update rebuilds p from the replaced residual.
+        if (pair) cgp_to_f64<<<grid, CG_THREADS, 0, s>>>(n, bufs.x2, x);
         if (i32) launch_residual<int32_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
         else launch_residual<int64_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
-        cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
+        cg_fold_set<<<1, 32, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
+        if (pair) cgp_from_f64<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.r2);
         double rr_true = 0;
         if ((e = cudaMemcpyAsync(&rr_true, bufs.rr, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess) { fail(FGB_ECUDA, "replacement sync", e); break; }
         res->replacements++;
         since_replace = 0;
-        // When the recursive residual has drifted far below the true one, the
-        // kept direction no longer matches r: restart it from the replaced r.
-        if (hist[chunk - 1] < 1e-6 * rr_true) {
-          cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p);
+        // When the recursive residual has drifted below half the true one
+        // (an iteration operator rounded to FP32 or BF16 leaves such a gap),
+        // the kept direction no longer matches r: the next step would take
+        // alpha = r.r / p.Ap, far above r.p / p.Ap, and the iteration would
+        // diverge.  Restart the direction from the replaced r.
+        if (hist[chunk - 1] < 0.25 * rr_true) {
+          if (pair) cgp_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r2, bufs.p2);
+          else cg_copy<<<grid, CG_THREADS, 0, s>>>(n, bufs.r, bufs.p, bufs.p32);
           if ((e = cudaGetLastError()) != cudaSuccess) { fail(FGB_ECUDA, "restart", e); break; }
         }
         res->true_rel_residual = sqrt(rr_true) / (bnorm > 0 ? bnorm : 1.0);
@@ -483,11 +766,12 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     }
     res->iterations = it;
   } while (0);
+  if (pair_live && rc == FGB_OK) cgp_to_f64<<<grid, CG_THREADS, 0, s>>>(n, bufs.x2, x);  // the solution
   if (rc == FGB_OK && !res->converged && res->iterations >= opt->max_iter) {
     // report the true residual reached
     if (i32) launch_residual<int32_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
     else launch_residual<int64_t>(A64, grid, x, b, bufs.r, bufs.part_a, nullptr, s);
-    cg_fold_set<<<1, CG_THREADS, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
+    cg_fold_set<<<1, 32, 0, s>>>(bufs.part_a, grid, bufs.rr, 0);
     double rr_true = 0, bb = 0;
     cudaMemcpyAsync(&rr_true, bufs.rr, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(&bb, bufs.rr + 2, sizeof(double), cudaMemcpyDeviceToHost, s);

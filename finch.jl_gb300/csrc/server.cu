@@ -60,7 +60,20 @@ struct __align__(16) DevMatrix {
   const int32_t* idx;
   const float* val;
   int32_t nrows, ncols, base, nnz;
+  int32_t lanes;  // SpMV lanes per row (a power of two <= 32), from the matrix's size class
+  int32_t rpi;    // rows per work item, from the matrix's size class
 };
+
+// Size classes of registered matrices by mean stored entries per row:
+// class 0 holds means below 1, class c >= 1 means in [2^(c-1), 2^c), the
+// last class everything above.  Each class has its own serving shape.
+constexpr int SRV_CLASSES = 10;
+inline int size_class(int64_t nnz, int64_t nrows) {
+  const double mean = nrows > 0 ? (double)nnz / (double)nrows : 0.0;
+  int c = 0;
+  while (c < SRV_CLASSES - 1 && mean >= (double)(int64_t(1) << c)) ++c;
+  return c;
+}
 
 struct __align__(16) DevSlot {
   int32_t op, matrix, matrix_b, nk;
@@ -106,9 +119,12 @@ struct SrvArgs {
   unsigned int* done_items;         // per slot
   unsigned int* exit_epoch;         // device word: the last launch told to exit
   unsigned long long* done_count;   // device counter: completion records written
-  unsigned int epoch;               // this launch
+  const unsigned int* epoch_word;   // device word: this launch's number (bumped before each launch)
   uint64_t idle_ns;
 };
+
+// The graph node before every launch of the device loop: a new launch number.
+__global__ void serve_bump_epoch_k(unsigned int* epoch_word) { *epoch_word += 1u; }
 
 __device__ __forceinline__ uint64_t globaltimer() {
   uint64_t t;
@@ -126,14 +142,19 @@ __device__ __forceinline__ void st_release_sys(volatile uint64_t* p, uint64_t v)
   asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// y[r] = sum_j A[r,j] x[j]; returns y[r] in every lane
-__device__ float srv_spmv_row(const DevMatrix& A, const float* __restrict__ x, int r, int lane) {
-  const int q0 = __ldg(A.ptr + r) - A.base, q1 = __ldg(A.ptr + r + 1) - A.base;
+// y[r] = sum_j A[r,j] x[j] over the G lanes of one row group (gl = lane in
+// the group; a row of r < 0 contributes nothing but still takes part in the
+// shuffles); returns y[r] in every lane of the group.  Lanes stride the
+// row's entries by G and the partial sums fold by xor over the group: a
+// fixed order for each G.
+__device__ float srv_spmv_row(const DevMatrix& A, const float* __restrict__ x, int r, int gl, int G) {
   float acc = 0.f;
-  for (int q = q0 + lane; q < q1; q += 32)
-    acc = __fmaf_rn(__ldg(A.val + q), __ldcg(x + (__ldg(A.idx + q) - A.base)), acc);
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+  if (r >= 0) {
+    const int q0 = __ldg(A.ptr + r) - A.base, q1 = __ldg(A.ptr + r + 1) - A.base;
+    for (int q = q0 + gl; q < q1; q += G)
+      acc = __fmaf_rn(__ldg(A.val + q), __ldcg(x + (__ldg(A.idx + q) - A.base)), acc);
+  }
+  for (int m = G >> 1; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
   return acc;
 }
 
@@ -192,11 +213,13 @@ __device__ void srv_process(const SrvArgs& a, const DevSlot& s, const DevItem& i
     // one value per row: staged so that the block stores whole lines (the
     // output may live in host memory, where scattered 4-byte stores are slow)
     __shared__ float s_y[SRV_YCHUNK];
+    const int G = A.lanes, per = 32 / G, sub = lane / G, gl = lane % G;  // 32 / G rows per warp at once
     for (int r0 = (int)it.row_begin; r0 < (int)it.row_end; r0 += SRV_YCHUNK) {
       const int n = min(SRV_YCHUNK, (int)it.row_end - r0);
-      for (int k = warp; k < n; k += SRV_THREADS / 32) {
-        const float y = srv_spmv_row(A, s.in, r0 + k, lane);
-        if (lane == 0) s_y[k] = y;
+      for (int k0 = warp * per; k0 < n; k0 += (SRV_THREADS / 32) * per) {
+        const int k = k0 + sub;
+        const float y = srv_spmv_row(A, s.in, k < n ? r0 + k : -1, gl, G);
+        if (k < n && gl == 0) s_y[k] = y;
       }
       __syncthreads();
       for (int k = threadIdx.x; k < n; k += SRV_THREADS) s.out[r0 + k] = s_y[k];
@@ -221,6 +244,7 @@ __device__ void srv_process(const SrvArgs& a, const DevSlot& s, const DevItem& i
 // leaves.  The host relaunches when it sees the kernel finished with work
 // outstanding; a kernel never keeps running on a few blocks.
 __global__ void __launch_bounds__(SRV_THREADS, 5) serve_loop_k(SrvArgs a) {
+  const unsigned epoch = *(volatile const unsigned*)a.epoch_word;  // set by the node before this launch
   __shared__ unsigned long long s_item;
   __shared__ unsigned s_take;
   __shared__ int s_exit;
@@ -251,14 +275,14 @@ __global__ void __launch_bounds__(SRV_THREADS, 5) serve_loop_k(SrvArgs a) {
         }
         cached_pub = ld_acquire_sys(&a.host->published);
         if (cached_pub > cur) continue;
-        if (a.host->stop || *(volatile unsigned*)a.exit_epoch >= a.epoch) { exit_now = 1; break; }
+        if (a.host->stop || *(volatile unsigned*)a.exit_epoch >= epoch) { exit_now = 1; break; }
         const uint64_t now = globaltimer();
         if (cur != last_cur) {  // another block claimed an item: not idle
           last_cur = cur;
           idle_since = now;
         }
         if (now - idle_since > a.idle_ns) {
-          atomicMax(a.exit_epoch, a.epoch);
+          atomicMax(a.exit_epoch, epoch);
           exit_now = 1;
           break;
         }
@@ -459,7 +483,15 @@ struct fgb_server {
   cudaStream_t copy_stream = nullptr, kernel_stream = nullptr;
   cudaEvent_t kernel_done = nullptr;
   bool kernel_launched = false;
-  unsigned loop_epoch = 0;         // launches of the device loop so far
+  // the device loop's launch (epoch bump + loop kernel) and the stage launch,
+  // each captured once into a graph that the dispatcher replays; the stage
+  // node's grid and arguments are updated per group before its replay
+  cudaGraphExec_t loop_exec = nullptr, stage_exec = nullptr;
+  cudaGraph_t loop_graph = nullptr, stage_graph = nullptr;
+  cudaGraphNode_t stage_node = nullptr;
+  // serving shape per size class: SpMV lanes per row and rows per work item
+  int32_t class_lanes[SRV_CLASSES] = {};
+  int32_t class_rpi[SRV_CLASSES] = {};
   // host bookkeeping
   std::vector<DevMatrix> mats;
   std::mutex mu;
@@ -517,7 +549,7 @@ SrvArgs make_args(fgb_server* s) {
   a.done_items = s->d_done;
   a.exit_epoch = (unsigned*)(s->d_next + 2);
   a.done_count = s->d_next + 3;
-  a.epoch = s->loop_epoch;
+  a.epoch_word = (const unsigned*)(s->d_next + 4);
   a.idle_ns = (uint64_t)s->cfg.idle_exit_us * 1000ull;
   return a;
 }
@@ -556,7 +588,7 @@ void run_per_call(fgb_server* s, std::vector<uint64_t>& batch, std::unique_lock<
     if (t.in_bytes) e = cudaMemcpyAsync(s->pool + t.in_off, r.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
     if (e == cudaSuccess && t.n_items > 0) {
       serve_one_k<<<(unsigned)t.n_items, SRV_THREADS, 0, s->copy_stream>>>(make_args(s), slot, (int)t.rows,
-                                                                           s->cfg.rows_per_item);
+                                                                           s->mats[r.matrix].rpi);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && !t.out_mapped)
@@ -641,7 +673,7 @@ void worker_main(fgb_server* s) {
         rq.item0 = t.item0;
         rq.slot = t.slot;
         rq.rows = (int32_t)t.rows;
-        rq.rows_per_item = s->cfg.rows_per_item;
+        rq.rows_per_item = s->mats[t.req.matrix].rpi;
         rq.pad = 0;
         max_chunks = std::max<uint64_t>(max_chunks, (rq.bytes + STAGE_CHUNK - 1) / STAGE_CHUNK);
         n_new += t.n_items;
@@ -652,8 +684,15 @@ void worker_main(fgb_server* s) {
       if (e == cudaSuccess) {
         StageArgs g{s->stage_dev, (uint32_t)first, (uint32_t)STAGE_CAP, s->d_slots, s->d_items,
                     (unsigned*)(s->d_next + 1), s->host_dev, publish_to};
-        serve_stage_k<<<dim3((unsigned)max_chunks, (unsigned)admitted.size()), STAGE_THREADS, 0, s->copy_stream>>>(g);
-        e = cudaGetLastError();
+        // the captured stage launch, with this group's grid and arguments
+        void* args[] = {&g};
+        cudaKernelNodeParams kp{};
+        kp.func = (void*)serve_stage_k;
+        kp.gridDim = dim3((unsigned)max_chunks, (unsigned)admitted.size());
+        kp.blockDim = dim3(STAGE_THREADS);
+        kp.kernelParams = args;
+        e = cudaGraphExecKernelNodeSetParams(s->stage_exec, s->stage_node, &kp);
+        if (e == cudaSuccess) e = cudaGraphLaunch(s->stage_exec, s->copy_stream);
       }
       if (e != cudaSuccess) {
         fail_worker(s, FGB_ECUDA, "stage launch", e);
@@ -675,10 +714,8 @@ void worker_main(fgb_server* s) {
       const bool running = s->kernel_launched && cudaEventQuery(s->kernel_done) == cudaErrorNotReady;
       if (!running) {
         cudaGetLastError();
-        const int grid = s->ctx->num_sms * s->cfg.blocks_per_sm;
-        ++s->loop_epoch;
-        serve_loop_k<<<grid, SRV_THREADS, 0, s->kernel_stream>>>(make_args(s));
-        cudaError_t e = cudaGetLastError();
+        // the captured relaunch: a new launch number, then the loop kernel
+        cudaError_t e = cudaGraphLaunch(s->loop_exec, s->kernel_stream);
         if (e == cudaSuccess) e = cudaEventRecord(s->kernel_done, s->kernel_stream);
         if (e != cudaSuccess) fail_worker(s, FGB_ECUDA, "serve_loop_k launch", e);
         s->kernel_launched = true;
@@ -814,6 +851,37 @@ int fgb_server_create(fgb_ctx* ctx, const fgb_server_config* cfg_in, fgb_server*
   s->slot_seq.assign(cfg.max_inflight, 0);
   s->slot_done_seq.assign(cfg.max_inflight, 0);
   s->stage_pub.assign(STAGE_CAP, 0);
+  for (int c = 0; c < SRV_CLASSES; ++c) {
+    s->class_lanes[c] = 32;
+    s->class_rpi[c] = cfg.rows_per_item;
+  }
+  // capture the two launches the dispatcher replays (nothing runs here)
+  {
+    const int grid = ctx->num_sms * cfg.blocks_per_sm;
+    cudaError_t ge = cudaStreamBeginCapture(s->kernel_stream, cudaStreamCaptureModeThreadLocal);
+    if (ge == cudaSuccess) {
+      serve_bump_epoch_k<<<1, 1, 0, s->kernel_stream>>>((unsigned*)(s->d_next + 4));
+      serve_loop_k<<<grid, SRV_THREADS, 0, s->kernel_stream>>>(make_args(s));
+      ge = cudaStreamEndCapture(s->kernel_stream, &s->loop_graph);
+    }
+    if (ge == cudaSuccess) ge = cudaGraphInstantiate(&s->loop_exec, s->loop_graph, 0);
+    if (ge == cudaSuccess) ge = cudaStreamBeginCapture(s->copy_stream, cudaStreamCaptureModeThreadLocal);
+    if (ge == cudaSuccess) {
+      StageArgs g0{s->stage_dev, 0u, (uint32_t)STAGE_CAP, s->d_slots, s->d_items, (unsigned*)(s->d_next + 1),
+                   s->host_dev, 0ull};
+      serve_stage_k<<<dim3(1, 1), STAGE_THREADS, 0, s->copy_stream>>>(g0);
+      ge = cudaStreamEndCapture(s->copy_stream, &s->stage_graph);
+    }
+    size_t nn = 1;
+    if (ge == cudaSuccess) ge = cudaGraphGetNodes(s->stage_graph, &s->stage_node, &nn);
+    if (ge == cudaSuccess) ge = cudaGraphInstantiate(&s->stage_exec, s->stage_graph, 0);
+    if (ge != cudaSuccess) {
+      set_error(FGB_ECUDA, "fgb_server_create: graphs: %s", cudaGetErrorString(ge));
+      cudaGetLastError();
+      fgb_server_destroy(s);
+      return FGB_ECUDA;
+    }
+  }
   s->worker = std::thread(worker_main, s);
   *out = s;
   return FGB_OK;
@@ -829,8 +897,9 @@ int fgb_server_register(fgb_server* s, const fgb_sparse* A, int32_t* id) {
   std::lock_guard<std::mutex> lk(s->mu);
   if ((int)s->mats.size() >= SRV_MAX_MATRICES) return set_error(FGB_ENOMEM, "fgb_server_register: matrix table full");
   if (A->nnz > INT32_MAX) return set_error(FGB_EUNSUPPORTED, "fgb_server_register: too many entries");
+  const int c = size_class(A->nnz, A->nrows);
   DevMatrix m{(const int32_t*)A->ptr, (const int32_t*)A->idx, (const float*)A->val, (int32_t)A->nrows,
-              (int32_t)A->ncols, A->index_base, (int32_t)A->nnz};
+              (int32_t)A->ncols, A->index_base, (int32_t)A->nnz, s->class_lanes[c], s->class_rpi[c]};
   FGB_CUDA_TRY(cudaMemcpy(s->d_mats + s->mats.size(), &m, sizeof(m), cudaMemcpyHostToDevice));
   *id = (int32_t)s->mats.size();
   s->mats.push_back(m);
@@ -884,7 +953,7 @@ static int submit_locked(fgb_server* s, const fgb_request* r, const MappedBufs& 
   Ticket t;
   t.req = *r;
   t.rows = A.nrows;
-  t.n_items = (A.nrows + s->cfg.rows_per_item - 1) / s->cfg.rows_per_item;
+  t.n_items = (A.nrows + A.rpi - 1) / A.rpi;
   t.in_bytes = req_in_bytes(s, *r);
   t.out_bytes = req_out_bytes(s, *r, A.nnz);
   // a page-locked output is written by the device in place (no copy back);
@@ -971,6 +1040,144 @@ int fgb_server_wait_batch(fgb_server* s, const uint64_t* tickets, int32_t n, int
   return FGB_OK;
 }
 
+}  // extern "C"
+
+// Applies per-class shapes to the table and every registered matrix; the
+// caller holds s->mu and the server is idle.
+static int apply_shapes(fgb_server* s, const int32_t* lanes, const int32_t* rpi) {
+  for (int c = 0; c < SRV_CLASSES; ++c) {
+    s->class_lanes[c] = lanes[c];
+    s->class_rpi[c] = rpi[c];
+  }
+  for (size_t k = 0; k < s->mats.size(); ++k) {
+    DevMatrix& m = s->mats[k];
+    const int c = size_class(m.nnz, m.nrows);
+    m.lanes = lanes[c];
+    m.rpi = rpi[c];
+  }
+  if (!s->mats.empty())
+    FGB_CUDA_TRY(cudaMemcpy(s->d_mats, s->mats.data(), sizeof(DevMatrix) * s->mats.size(), cudaMemcpyHostToDevice));
+  return FGB_OK;
+}
+
+static bool server_idle(const fgb_server* s) { return s->queue.empty() && s->n_inflight == 0; }
+
+extern "C" {
+
+int fgb_server_tune(fgb_server* s, int32_t reps, fgb_server_tuning* out) {
+  if (!s || !out) return set_error(FGB_EINVAL, "fgb_server_tune: null argument");
+  if (reps <= 0) reps = 3;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (!server_idle(s)) return set_error(FGB_EBUSY, "fgb_server_tune: requests are in flight");
+  *out = fgb_server_tuning{};
+  static const int kLanes[] = {2, 4, 8, 16, 32};
+  static const int kRpi[] = {32, 64, 128, 256};
+  constexpr int kSample = 8;
+  int64_t max_rows = 1, max_cols = 1;
+  for (const DevMatrix& m : s->mats) {
+    max_rows = std::max<int64_t>(max_rows, m.nrows);
+    max_cols = std::max<int64_t>(max_cols, m.ncols);
+  }
+  DevMatrix* tmp = nullptr;
+  float *x = nullptr, *y = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc((void**)&tmp, sizeof(DevMatrix) * kSample);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&x, sizeof(float) * max_cols);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&y, sizeof(float) * max_rows);
+  if (e == cudaSuccess) e = cudaMemset(x, 0, sizeof(float) * max_cols);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  int32_t lanes[SRV_CLASSES], rpi[SRV_CLASSES];
+  for (int c = 0; c < SRV_CLASSES; ++c) {
+    lanes[c] = s->class_lanes[c];
+    rpi[c] = s->class_rpi[c];
+  }
+  for (int c = 0; c < SRV_CLASSES && e == cudaSuccess; ++c) {
+    std::vector<DevMatrix> sample;
+    int count = 0;
+    for (const DevMatrix& m : s->mats)
+      if (size_class(m.nnz, m.nrows) == c) {
+        ++count;
+        if ((int)sample.size() < kSample) sample.push_back(m);
+      }
+    fgb_server_class_shape& o = out->cls[c];
+    o.matrices = count;
+    o.ms = o.ms_default = -1.0;
+    o.lanes = lanes[c];
+    o.rows_per_item = rpi[c];
+    if (sample.empty()) continue;
+    // the class's sample as SpMV requests through the serving kernel, at one shape
+    auto time_shape = [&](int G, int R, double* ms) -> cudaError_t {
+      std::vector<DevMatrix> t = sample;
+      for (DevMatrix& m : t) {
+        m.lanes = G;
+        m.rpi = R;
+      }
+      cudaError_t ce = cudaMemcpyAsync(tmp, t.data(), sizeof(DevMatrix) * t.size(), cudaMemcpyHostToDevice, st);
+      SrvArgs a = make_args(s);
+      a.mats = tmp;
+      for (int rep = -1; rep < reps && ce == cudaSuccess; ++rep) {  // rep -1: warm-up
+        if (rep == 0) ce = cudaEventRecord(e0, st);
+        for (int k = 0; k < (int)t.size() && ce == cudaSuccess; ++k) {
+          const DevSlot slot{FGB_REQ_SPMV, k, -1, 0, x, y, (int32_t)((t[k].nrows + R - 1) / R), 0, 0};
+          if (slot.n_items > 0) serve_one_k<<<(unsigned)slot.n_items, SRV_THREADS, 0, st>>>(a, slot, t[k].nrows, R);
+          ce = cudaGetLastError();
+        }
+      }
+      if (ce == cudaSuccess) ce = cudaEventRecord(e1, st);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float f = 0.f;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&f, e0, e1);
+      *ms = f / reps;
+      return ce;
+    };
+    double best = -1.0;
+    for (int G : kLanes) {
+      for (int R : kRpi) {
+        double ms = 0;
+        if ((e = time_shape(G, R, &ms)) != cudaSuccess) break;
+        if (best < 0 || ms < best) {
+          best = ms;
+          lanes[c] = G;
+          rpi[c] = R;
+        }
+      }
+      if (e != cudaSuccess) break;
+    }
+    if (e == cudaSuccess) e = time_shape(32, s->cfg.rows_per_item, &o.ms_default);
+    o.ms = best;
+    o.lanes = lanes[c];
+    o.rows_per_item = rpi[c];
+  }
+  int rc = FGB_OK;
+  if (e != cudaSuccess) rc = set_error(FGB_ECUDA, "fgb_server_tune: %s", cudaGetErrorString(e));
+  if (rc == FGB_OK) rc = apply_shapes(s, lanes, rpi);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  cudaFree(tmp);
+  cudaFree(x);
+  cudaFree(y);
+  return rc;
+}
+
+int fgb_server_set_tuning(fgb_server* s, const fgb_server_tuning* t) {
+  if (!s || !t) return set_error(FGB_EINVAL, "fgb_server_set_tuning: null argument");
+  int32_t lanes[SRV_CLASSES], rpi[SRV_CLASSES];
+  for (int c = 0; c < SRV_CLASSES; ++c) {
+    const int G = t->cls[c].lanes, R = t->cls[c].rows_per_item;
+    if (G < 1 || G > 32 || (G & (G - 1)) || R < 1 || R > (1 << 16))
+      return set_error(FGB_EINVAL, "fgb_server_set_tuning: class %d: lanes %d, rows per item %d", c, G, R);
+    lanes[c] = G;
+    rpi[c] = R;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (!server_idle(s)) return set_error(FGB_EBUSY, "fgb_server_set_tuning: requests are in flight");
+  return apply_shapes(s, lanes, rpi);
+}
+
 int fgb_server_stats_get(fgb_server* s, fgb_server_stats* out) {
   if (!s || !out) return set_error(FGB_EINVAL, "fgb_server_stats_get: null argument");
   std::lock_guard<std::mutex> lk(s->mu);
@@ -992,6 +1199,10 @@ int fgb_server_destroy(fgb_server* s) {
   if (s->host) s->host->stop = 1;
   if (s->kernel_stream) cudaStreamSynchronize(s->kernel_stream);  // the loop exits on stop
   if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
+  if (s->loop_exec) cudaGraphExecDestroy(s->loop_exec);
+  if (s->stage_exec) cudaGraphExecDestroy(s->stage_exec);
+  if (s->loop_graph) cudaGraphDestroy(s->loop_graph);
+  if (s->stage_graph) cudaGraphDestroy(s->stage_graph);
   if (s->kernel_done) cudaEventDestroy(s->kernel_done);
   if (s->kernel_stream) cudaStreamDestroy(s->kernel_stream);
   if (s->copy_stream) cudaStreamDestroy(s->copy_stream);

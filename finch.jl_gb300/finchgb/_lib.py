@@ -51,7 +51,7 @@ class FgbSddmmTuning(ctypes.Structure):
 
 class FgbCgOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("max_iter", c_int64), ("chunk", c_int32),
-                ("precision", c_int32), ("replace_every", c_int64), ("accumulate_fp64", c_int32),
+                ("precision", c_int32), ("replace_every", c_int64), ("accumulate", c_int32),
                 ("reserved", c_int32)]
 
 
@@ -90,6 +90,18 @@ class FgbServerStats(ctypes.Structure):
                 ("batches_published", c_uint64), ("pool_used", c_uint64), ("admit_ns", c_uint64),
                 ("scan_ns", c_uint64), ("finish_ns", c_uint64), ("iterations", c_uint64),
                 ("queue_ns", c_uint64), ("service_ns", c_uint64)]
+
+
+SERVER_CLASSES = 10  # FGB_SERVER_CLASSES
+
+
+class FgbServerClassShape(ctypes.Structure):
+    _fields_ = [("matrices", c_int32), ("lanes", c_int32), ("rows_per_item", c_int32), ("reserved", c_int32),
+                ("ms", c_double), ("ms_default", c_double)]
+
+
+class FgbServerTuning(ctypes.Structure):
+    _fields_ = [("cls", FgbServerClassShape * SERVER_CLASSES)]
 
 
 class FgbSparse(ctypes.Structure):
@@ -181,6 +193,8 @@ SIGNATURES: dict[str, tuple] = {
                                         POINTER(c_int32)]),
     "fgb_server_wait_batch": (c_int, [c_void_p, POINTER(c_uint64), c_int32, c_int32,
                                       POINTER(c_double)]),
+    "fgb_server_tune": (c_int, [c_void_p, c_int32, POINTER(FgbServerTuning)]),
+    "fgb_server_set_tuning": (c_int, [c_void_p, POINTER(FgbServerTuning)]),
     "fgb_server_stats_get": (c_int, [c_void_p, POINTER(FgbServerStats)]),
     "fgb_server_destroy": (c_int, [c_void_p]),
 }

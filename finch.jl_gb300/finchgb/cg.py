@@ -1,10 +1,11 @@
 """Conjugate gradients, two ways.
 
 `cg_solve` runs the native mixed-precision solver (fgb_cg_solve): the
-iteration SpMV reads FP32 or BF16 values with FP32 accumulation, the dot
-products and vector updates stay FP64, FP64 reliable updates of the residual
-bring the true residual to rtol, and chunks of iterations replay as CUDA
-graphs.
+iteration SpMV reads FP32 or BF16 values and sums them in FP32, in FP64, or
+-- with the whole iteration -- in pairs of FP32 numbers (about 48 bits, no
+FP64 arithmetic per row: the fast mode on GB300, whose FP64 rate is a small
+fraction of its FP32 rate); FP64 reliable updates of the residual bring the
+true residual to rtol, and chunks of iterations replay as CUDA graphs.
 
 `cg_finch` is the same algorithm written as Finch programs -- every step is an
 `@einsum` matched onto a kernel by the GB300 scheduler -- for readability and
@@ -22,6 +23,7 @@ from . import _lib as L
 from . import device as dev
 
 PRECISIONS = {"f64": L.F64, "f32": L.F32, "bf16": L.BF16}
+ACCUMULATE = {"f32": 0, "f64": 1, "pair": 2}  # FGB_CG_SUM_F32, _F64, _PAIR
 
 
 @dataclass
@@ -46,7 +48,9 @@ def cg_solve(A64: dev.DeviceSparse, b: torch.Tensor, x: torch.Tensor | None = No
              accumulate: str = "f32") -> tuple[torch.Tensor, CGResult]:
     """Solves A x = b (A SPD, CSR, FP64 values); returns (x, result).
     precision: the stored values of the iteration SpMV (f64, f32, bf16);
-    accumulate: its sums for f32/bf16 values, "f32" or "f64" (values widened)."""
+    accumulate: the arithmetic for f32/bf16 values: "f32" (FP32 SpMV sums),
+    "f64" (values widened, FP64 sums) or "pair" (pairs of FP32 numbers for the
+    SpMV sums, vectors, dots and updates)."""
     if A64.orient != "csr":
         raise ValueError("cg_solve needs a CSR matrix")
     if x is None:
@@ -54,7 +58,7 @@ def cg_solve(A64: dev.DeviceSparse, b: torch.Tensor, x: torch.Tensor | None = No
     prec = PRECISIONS[precision]
     if prec != L.F64 and Alow is None:
         Alow = low_precision_copy(A64, precision)
-    opts = L.FgbCgOptions(rtol, max_iter, chunk, prec, replace_every, 1 if accumulate == "f64" else 0, 0)
+    opts = L.FgbCgOptions(rtol, max_iter, chunk, prec, replace_every, ACCUMULATE[accumulate], 0)
     res = L.FgbCgResult()
     da = A64.desc()
     dl = None if prec == L.F64 else ctypes.byref(Alow.desc())

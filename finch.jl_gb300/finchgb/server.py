@@ -102,6 +102,23 @@ class Server:
         L.check(rc, "fgb_server_wait")
         return lat.value
 
+    def tune(self, reps: int = 3) -> L.FgbServerTuning:
+        """Runs the serving autotuner (fgb_server_tune) on the registered
+        matrices and applies its choice; returns the per-class shapes."""
+        t = L.FgbServerTuning()
+        L.call("fgb_server_tune", self.h, reps, ctypes.byref(t))
+        return t
+
+    def set_tuning(self, t: L.FgbServerTuning):
+        """Applies per-class shapes (e.g. another server's tune() result)."""
+        L.call("fgb_server_set_tuning", self.h, ctypes.byref(t))
+
+    @staticmethod
+    def shapes(t: L.FgbServerTuning) -> list[dict]:
+        return [{"class": c, "matrices": x.matrices, "lanes": x.lanes, "rows_per_item": x.rows_per_item,
+                 "ms": round(x.ms, 4), "ms_default": round(x.ms_default, 4)}
+                for c, x in enumerate(t.cls) if x.matrices > 0]
+
     def stats(self) -> dict:
         s = L.FgbServerStats()
         L.call("fgb_server_stats_get", self.h, ctypes.byref(s))

@@ -249,15 +249,18 @@ FGB_API int fgb_spmm_semiring(fgb_ctx* ctx, int semiring, const fgb_sparse* A, c
  * lanes * vector-width, one launch per slab, so the gathered slab of B stays
  * L2-resident.  Zero fields take the defaults. */
 typedef struct fgb_spmm_tuning {
-  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variants 2 and 3: 2, 4 or 8) */
+  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variants 2-4: 2, 4 or 8) */
   int32_t variant; /* 0: B rows gathered into registers; 1: B rows staged into a
                       shared-memory ring by TMA tile::gather4 (fp32); 2: rows
                       cut into virtual rows of at most `path` entries, sorted
                       by length, one launch per column slab of 4 * lanes (fp32);
                       3: variant 2 with the gathers staged in shared memory by
-                      cp.async (more warps per SM; identical results) */
-  int64_t path;    /* merge-path item length (variants 2, 3: virtual-row length) */
-  int32_t bands;   /* variants 2, 3: cut A's columns into this many bands of
+                      cp.async (more warps per SM; identical results);
+                      4: variant 3 with each lane group's next virtual row's
+                      indices and values bulk-prefetched into L2 (identical
+                      results) */
+  int64_t path;    /* merge-path item length (variants 2-4: virtual-row length) */
+  int32_t bands;   /* variants 2-4: cut A's columns into this many bands of
                       consecutive columns (0 or 1: none, at most 8), each band's
                       entries in launches of their own, so a launch gathers from
                       1/bands of B's slab; a row's sum still runs over its
@@ -558,7 +561,7 @@ typedef enum {
 typedef struct fgb_server_config {
   size_t pool_bytes;     /* HBM budget for in-flight inputs/outputs (admission) */
   int32_t max_inflight;  /* request slots, <= 4096 */
-  int32_t rows_per_item; /* rows per work item (default 64) */
+  int32_t rows_per_item; /* rows per work item of every size class until tuned (default 64) */
   int32_t blocks_per_sm; /* persistent blocks per SM (default 4; capped one below occupancy) */
   int32_t idle_exit_us;  /* device loop exits after this long without work (default 20000) */
   int32_t mode;          /* fgb_serve_mode */
@@ -607,6 +610,37 @@ FGB_API int fgb_server_wait_batch(fgb_server* srv, const uint64_t* tickets, int3
 FGB_API int fgb_server_wait(fgb_server* srv, uint64_t ticket, int32_t timeout_ms,
                             double* latency_s);
 FGB_API int fgb_server_stats_get(fgb_server* srv, fgb_server_stats* out);
+
+/* Serving shapes per size class.  Registered matrices fall into classes by
+ * their mean stored entries per row (class 0: below 1; class c >= 1: in
+ * [2^(c-1), 2^c); the last class: everything above).  Each class has its
+ * SpMV lanes per row (a power of two <= 32; 32 / lanes rows per warp at
+ * once) and rows per work item (the unit the device loop claims). */
+#define FGB_SERVER_CLASSES 10
+typedef struct fgb_server_class_shape {
+  int32_t matrices;      /* registered matrices of the class (tune: output only) */
+  int32_t lanes;         /* SpMV lanes per row */
+  int32_t rows_per_item; /* rows per work item */
+  int32_t reserved;
+  double ms;             /* tune: time of the class's sample at the chosen shape (-1: none) */
+  double ms_default;     /* tune: the same sample at 32 lanes and the configured rows per item */
+} fgb_server_class_shape;
+typedef struct fgb_server_tuning {
+  fgb_server_class_shape cls[FGB_SERVER_CLASSES];
+} fgb_server_tuning;
+
+/* The serving autotuner (no counterpart in Finch): for every size class
+ * with registered matrices, times SpMV requests on up to 8 of them through
+ * the serving kernel itself at every shape (lanes 2..32, rows per item
+ * 32..256), reps timed runs each, keeps the fastest and applies it to the
+ * class (its matrices and later registrations).  Both modes compute a row
+ * the same way for a given shape, so batched and per-call results stay
+ * identical at the same shapes.  The server must be idle (FGB_EBUSY
+ * otherwise).  Synchronous; allocates its timing buffers. */
+FGB_API int fgb_server_tune(fgb_server* srv, int32_t reps, fgb_server_tuning* out);
+/* Applies shapes (lanes, rows_per_item per class; other fields ignored),
+ * e.g. those another server's fgb_server_tune chose.  Idle server only. */
+FGB_API int fgb_server_set_tuning(fgb_server* srv, const fgb_server_tuning* tuning);
 /* Stops the device loop (bounded) and frees everything. */
 FGB_API int fgb_server_destroy(fgb_server* srv);
 
@@ -618,9 +652,16 @@ typedef struct fgb_cg_options {
   int32_t chunk;         /* iterations per captured CUDA graph (even) */
   int32_t precision;     /* value type of the iteration SpMV: FGB_F64, FGB_F32 or FGB_BF16 */
   int64_t replace_every; /* FP64 residual replacement period in iterations (0 = only at the end) */
-  int32_t accumulate_fp64; /* 1: the FP32/BF16 SpMV widens its values and sums in FP64 (0: FP32 sums) */
+  int32_t accumulate;    /* arithmetic of an FP32/BF16-valued solve: FGB_CG_SUM_* */
   int32_t reserved;
 } fgb_cg_options;
+
+/* fgb_cg_options.accumulate (ignored for FP64 values, which sum in FP64) */
+#define FGB_CG_SUM_F32 0  /* SpMV: values times an FP32 copy of p, FP32 sums; vectors, dots, updates FP64 */
+#define FGB_CG_SUM_F64 1  /* SpMV: values widened to FP64, FP64 sums; vectors, dots, updates FP64 */
+#define FGB_CG_SUM_PAIR 2 /* SpMV sums, x, r, p, q, dots and updates in pairs of FP32 numbers
+                           * (hi + lo, about 48 significant bits), no FP64 arithmetic per row or
+                           * stored entry: the fast mode on GPUs whose FP64 rate is far below FP32 */
 
 typedef struct fgb_cg_result {
   int64_t iterations;       /* iterations run */
@@ -636,8 +677,8 @@ typedef struct fgb_cg_result {
  * replacement and the FP64 mode); Alow (same pattern) carries the FP32 or
  * BF16 values of the iteration SpMV (NULL when precision is FGB_F64).  The
  * loop is the Finch program `@einsum q[i] += A[i,j]*p[j]`,
- * `@einsum s[] += p[i]*q[i]` and the vector updates, with dot products and
- * updates in FP64 and FP64 reliable updates of the residual.
+ * `@einsum s[] += p[i]*q[i]` and the vector updates, in the arithmetic that
+ * opt->accumulate names, with FP64 reliable updates of the residual.
  * Synchronous with respect to `stream`. */
 FGB_API int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_sparse* Alow,
                          const double* b, double* x, const fgb_cg_options* opt,

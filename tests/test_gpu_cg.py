@@ -1,6 +1,7 @@
-"""Mixed-precision CG on the GPU: FP32/BF16-valued SpMV with FP64 dots,
-updates and reliable residual replacement reaches the same FP64 tolerance as
-FP64 CG; residuals are checked on the host in FP64 against the oracle's SpMV."""
+"""Mixed-precision CG on the GPU: FP32/BF16-valued SpMV summed in FP32, FP64
+or pairs of FP32 numbers, with FP64 reliable residual replacement, reaches
+the same FP64 tolerance as FP64 CG; residuals are checked on the host in FP64
+against the oracle's SpMV."""
 import numpy as np
 import pytest
 import torch
@@ -83,6 +84,52 @@ def test_cg_fp64_accumulation_equals_fp64(gpu_lib, precision):
     assert r64.compact_index and rl.compact_index
     assert rl.iterations == r64.iterations and torch.equal(xl, x64)
     assert rl.converged and true_residual(A, xl.cpu().numpy(), b) <= 1.2e-10
+
+
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+@pytest.mark.parametrize("N", [32, 96])
+def test_cg_pair_sums_reach_fp64_tolerance(gpu_lib, precision, N):
+    """Pair arithmetic (about 48 bits) for the SpMV sums, vectors, dots and
+    updates: the FP64 tolerance, and no more than a few percent more
+    iterations than FP64 CG, deterministically."""
+    A = poisson2d(N)
+    b = np.random.default_rng(N + 1).uniform(-1, 1, A.nrows)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    _, r64 = cg.cg_solve(Ad, bd, precision="f64", rtol=1e-10, chunk=16, replace_every=64)
+    x, res = cg.cg_solve(Ad, bd, precision=precision, accumulate="pair", rtol=1e-10, chunk=16,
+                         replace_every=64)
+    assert res.converged and res.true_rel_residual <= 1e-10
+    assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10
+    assert res.iterations <= int(1.05 * r64.iterations) + 16
+    x2, res2 = cg.cg_solve(Ad, bd, precision=precision, accumulate="pair", rtol=1e-10, chunk=16,
+                           replace_every=64)
+    assert torch.equal(x, x2) and res2.iterations == res.iterations
+
+
+def test_cg_pair_sums_wide_matrix_and_warm_start(gpu_lib):
+    """The int32 index path of the pair SpMV, a warm start that is already
+    converged (x untouched), and the option checks."""
+    n = 70000  # couplings 40,000 apart: no 16-bit column offsets
+    rng = np.random.default_rng(12)
+    far = rng.integers(0, n, 1000)
+    rows = np.concatenate([np.arange(n), np.arange(n - 1), np.arange(1, n), far, (far + 40000) % n])
+    cols = np.concatenate([np.arange(n), np.arange(1, n), np.arange(n - 1), (far + 40000) % n, far])
+    vals = np.concatenate([np.full(n, 2.5), np.full(2 * (n - 1), -1.0), np.full(2000, -0.1)])
+    from finchgb.workloads import coo_to_csr
+
+    A = coo_to_csr(n, n, rows + 1, cols + 1, vals)
+    b = rng.uniform(-1, 1, n)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    x, res = cg.cg_solve(Ad, bd, precision="f32", accumulate="pair", rtol=1e-10, chunk=8)
+    assert res.converged and not res.compact_index
+    assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10
+    x0 = x.clone()
+    x3, r3 = cg.cg_solve(Ad, bd, x=x0, precision="bf16", accumulate="pair", chunk=8)
+    assert r3.converged and r3.iterations == 0 and torch.equal(x3, x)
+    with pytest.raises(F.FinchGBError):  # FP64 values have no pair mode
+        cg.cg_solve(Ad, bd, precision="f64", accumulate="pair", chunk=8)
 
 
 def test_cg_wide_matrix_keeps_the_int32_index(gpu_lib):

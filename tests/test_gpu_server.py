@@ -56,10 +56,12 @@ def library(gpu_lib):
     return mats, partners
 
 
-def run(server_mode, mats, partners, reqs, batch=False, **kw):
+def run(server_mode, mats, partners, reqs, batch=False, tuning=None, **kw):
     with Server(mode=server_mode, **kw) as srv:
         ids = [srv.register(A) for A in mats]
         pids = [srv.register(B) for B in partners]
+        if tuning is not None:
+            srv.set_tuning(tuning)
         if batch:
             recs = [srv.request(op, ids[k], inp, out, matrix_b=pids[k] if kb >= 0 else -1, nk=nk)
                     for op, k, inp, out, kb, nk in reqs]
@@ -110,6 +112,51 @@ def test_same_alone_and_in_the_mix(library):
             want = val.astype(np.float64) * Db[fa, idx - 1]
             scale = np.abs(want)
         assert (np.abs(got.numpy().astype(np.float64) - want) <= 2e-5 * scale + 1e-30).all()
+
+
+def test_tuned_shapes_same_alone_and_in_the_mix(library):
+    """The autotuner picks a shape per size class; both modes then compute
+    every row at that shape, so results stay bit-identical between them and
+    within the tolerance of the oracle."""
+    mats, partners = library
+    with Server(mode="batched") as srv:
+        for A in mats + partners:
+            srv.register(A)
+        t = srv.tune(reps=2)
+        shapes = Server.shapes(t)
+    assert sum(x["matrices"] for x in shapes) == len(mats) + len(partners)
+    for x in shapes:
+        assert x["lanes"] in (2, 4, 8, 16, 32) and x["rows_per_item"] in (32, 64, 128, 256)
+        assert 0 < x["ms"] and 0 < x["ms_default"]
+    # and shapes unlike the default in every class, so each lane-group width runs
+    forced = L.FgbServerTuning()
+    for c in range(L.SERVER_CLASSES):
+        forced.cls[c].lanes, forced.cls[c].rows_per_item = (2, 4, 8, 16)[c % 4], (32, 256)[c % 2]
+    rng = np.random.default_rng(9)
+    for tuning in (t, forced):
+        reqs = make_requests(rng, mats, partners, 45)
+        run("batched", mats, partners, reqs, tuning=tuning)
+        mixed = [r[3].clone() for r in reqs]
+        for r in reqs:
+            r[3].fill_(float("nan"))
+        run("per_call", mats, partners, reqs, tuning=tuning)
+        for (op, k, inp, out, kb, nk), a in zip(reqs, mixed):
+            assert torch.equal(a, out)
+            if op == "spmv":
+                ptr, idx, val = host_csr(mats[k])
+                A = mats[k]
+                want = oracle.spmv_csr(0, A.nrows, A.ncols, ptr, idx, val.astype(np.float64),
+                                       inp.numpy().astype(np.float64))
+                scale = oracle.spmv_csr(0, A.nrows, A.ncols, ptr, idx, np.abs(val).astype(np.float64),
+                                        np.abs(inp.numpy()).astype(np.float64))
+                assert (np.abs(a.numpy().astype(np.float64) - want) <= 2e-5 * scale + 1e-30).all()
+    bad = L.FgbServerTuning()
+    for c in range(L.SERVER_CLASSES):
+        bad.cls[c].lanes, bad.cls[c].rows_per_item = 3, 64  # not a power of two
+    with Server(mode="batched") as srv:
+        with pytest.raises(L.FinchGBError) as e:
+            srv.set_tuning(bad)
+        assert e.value.status == L.EINVAL
 
 
 def test_admission_queues_when_pool_is_small(library):
