@@ -443,7 +443,7 @@ def run_gpu(args):
     slabs = -(-NK // (4 * plan_lanes))
     if plan is None and lanes == 0 and path == 0 and variant == 0:
         variant = 3  # the library's default for a B far larger than L2
-    vrow = variant in (2, 3, 4, 5)
+    vrow = variant in (2, 3, 4)
     if plan is None and vrow:
         # schedule built per call: count, 5 scans (2 kernels each), fill, a
         # 3-kernel radix sort and the gather, then the slab x band launches

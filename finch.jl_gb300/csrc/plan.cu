@@ -139,7 +139,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
         return fgb_panels_spmm(p->ctx, it->second, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
                                d.flags, &t, s);
       }
-      if (c.variant >= 2 && c.variant <= 5) {
+      if (c.variant == 2 || c.variant == 3) {
         auto it = p->vrows.find({c.path, c.bands});
         if (it == p->vrows.end()) {  // built outside capture (the timing pass comes first)
           VrowSchedule v;
@@ -158,7 +158,7 @@ int issue(fgb_plan* p, const Choice& c, cudaStream_t s, bool plan_ready) {
           p->partial_bytes = need;
         }
         return spmm_vrow(p->ctx, it->second, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out,
-                         (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s, (int)c.variant - 2);
+                         (d.flags & FGB_ACCUMULATE) ? 1 : 0, 4 * c.lanes, p->partial, s, c.variant == 3);
       }
       if (c.path > 0)
         return spmm_merge(p->ctx, &p->A, d.in0, d.ld_in0, d.k, d.out, d.ld_out, d.dtype,
@@ -358,7 +358,7 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   }
   p->choice = best;
   for (auto it = p->vrows.begin(); it != p->vrows.end();) {  // and the chosen schedule
-    const bool vrow_choice = p->d.op == FGB_PLAN_SPMM ? (best.variant >= 2 && best.variant <= 5)
+    const bool vrow_choice = p->d.op == FGB_PLAN_SPMM ? (best.variant == 2 || best.variant == 3)
                                                        : (best.variant == 3 || best.variant == 4);
     if (!vrow_choice || it->first != std::make_pair(best.path, best.bands)) {
       vrow_free(&it->second);

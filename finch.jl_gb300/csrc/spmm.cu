@@ -242,9 +242,9 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
     path = 128;
     bands = 2;
   }
-  if (variant >= 2 && variant <= 5) {  // virtual-row column slabs: schedule built for this call
+  if (variant == 2 || variant == 3) {  // virtual-row column slabs: schedule built for this call
     if (A->orient != FGB_CSR || dtype != FGB_F32 || (flags & FGB_FINCH_ORDER))
-      return set_error(FGB_EUNSUPPORTED, "fgb_spmm: variants 2-5 need CSR, F32 and no FGB_FINCH_ORDER");
+      return set_error(FGB_EUNSUPPORTED, "fgb_spmm: variants 2 and 3 need CSR, F32 and no FGB_FINCH_ORDER");
     if (A->nrows == 0 || nk == 0) return FGB_OK;
     // the schedule and partial sums come from the stream-ordered pool and go
     // back to it behind the launches (no device-wide synchronisation)
@@ -260,7 +260,7 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
       return set_error(FGB_ENOMEM, "fgb_spmm: partial sums (%zu bytes)", pb);
     }
     rc = spmm_vrow(ctx, v, A, B, ldb, nk, C, ldc, (flags & FGB_ACCUMULATE) ? 1 : 0, slab, part, s,
-                   variant - 2);
+                   variant == 3);
     if (part) cudaFreeAsync(part, s);
     vrow_free(&v, s);
     return rc;
@@ -289,12 +289,12 @@ extern "C" int fgb_spmm_ex(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int
   int64_t path = tune ? tune->path : 0;
   const int variant = tune ? tune->variant : 0;
   const int bands = tune ? tune->bands : 0;
-  if (variant < 0 || variant > 5) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0 to 5");
+  if (variant < 0 || variant > 3) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variant must be 0, 1, 2 or 3");
   if (bands < 0 || bands > 8) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: bands must be in [0, 8]");
   if (bands > 1 && variant < 2)
-    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: column bands need variants 2 to 5");
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: column bands need variant 2 or 3");
   if (variant >= 2 && lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8)
-    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variants 2-5 take lanes 2, 4 or 8");
+    return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: variants 2 and 3 take lanes 2, 4 or 8");
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: lanes must be 0, 2, 4, 8, 16 or 32");
   if (path < 0) return fgb::set_error(FGB_EINVAL, "fgb_spmm_ex: negative path");

@@ -54,14 +54,11 @@ int vrow_build(fgb_ctx* ctx, const fgb_sparse* A, int T, VrowSchedule* out, cuda
 void vrow_free(VrowSchedule* v, cudaStream_t s = nullptr);
 // partial: the long rows' partial sums (spmm_vrow_scratch_bytes).
 size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk);
-// slab: 8, 16 or 32 columns per launch.  gather: where a batch of B rows
-// waits -- in registers, or staged in shared memory by cp.async (more warps
-// per SM), optionally with each group's next virtual row prefetched to L2,
-// or with the next batch's indices loaded while this batch gathers.
-enum { VR_GATHER_REGS = 0, VR_GATHER_ASYNC = 1, VR_GATHER_ASYNC_PF = 2, VR_GATHER_ASYNC_PIPE = 3 };
+// slab: 8, 16 or 32 columns per launch.  async_gather: gathers staged in
+// shared memory by cp.async (more warps per SM) instead of in registers.
 int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
               int64_t nk, void* C, int64_t ldc, int accumulate, int slab, void* partial,
-              cudaStream_t s, int gather = VR_GATHER_REGS);
+              cudaStream_t s, bool async_gather = false);
 
 // SDDMM over the same virtual rows (sddmm_vrow.cu): F32 CSR, k <= 128, k % 4 == 0.
 // slab: columns of k per launch (0 = all of k), a multiple of 4.

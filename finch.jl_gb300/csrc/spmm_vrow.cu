@@ -320,24 +320,11 @@ __device__ __forceinline__ void cp_async16_keep(void* smem, const void* gmem, ui
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Bulk prefetch into L2 of the 16-byte aligned part of [p, p + bytes): the
-// ragged ends, which the plain loads fetch anyway, are left out so that the
-// prefetch never names an address outside the span.
-__device__ __forceinline__ void prefetch_l2_span(const void* p, uint64_t bytes) {
-  const uint64_t a = ((uint64_t)p + 15) & ~uint64_t(15), e = ((uint64_t)p + bytes) & ~uint64_t(15);
-  if (e > a) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
-}
-
 // ALL: every lane's 4 columns lie inside nk (nk a multiple of 4L), so no
 // lane is masked.  A full batch (NB entries left) runs without per-entry
 // predicates; ldb fits 32 bits, so a gather address is one 32x32->64
-// multiply-add.  MODE 1: when a group starts a virtual row, its first lane
-// asks L2 for the group's next virtual row's indices and values (one bulk
-// prefetch each), so the loads that feed the gathers meet L2, not DRAM.
-// MODE 2: the next batch's indices and values are loaded into registers
-// before this batch's gathers are issued, so their round trip overlaps the
-// gathers instead of preceding them.
-template <int L, int NB, int MINB, bool ALL, int MODE>
+// multiply-add.
+template <int L, int NB, int MINB, bool ALL>
 __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
     int64_t nv, const int4* __restrict__ vr, const int* __restrict__ idx,
     const float* __restrict__ val, const float* __restrict__ B, int ldb, float* __restrict__ C,
@@ -366,49 +353,18 @@ __global__ void __launch_bounds__(VR_THREADS, MINB) spmm_vrow_async_k(
     const int len = rec.z;
     const int* ix = idx + rec.y;
     const float* vx = val + rec.y;
-    if (MODE == 1 && sl == 0 && v + ngroups < nv) {
-      const int4 nx = __ldg(vr + v + ngroups);
-      prefetch_l2_span(idx + nx.y, 4 * (uint64_t)nx.z);
-      prefetch_l2_span(val + nx.y, 4 * (uint64_t)nx.z);
-    }
     float4 acc = vrow_init(rec, C, ldc, col, active);
-    int jn[PER];
-    float an[PER];
-    if (MODE == 2) {
-#pragma unroll
-      for (int q = 0; q < PER; ++q) {
-        const int p = sl + L * q;
-        jn[q] = 0;
-        an[q] = 0.f;
-        if (p < len) {
-          jn[q] = ld_stream_i32(ix + p, pol_stream) - base;
-          an[q] = ld_stream_f32(vx + p, pol_stream);
-        }
-      }
-    }
     for (int t = 0; t < len; t += NB) {
       int j[PER];
       float a[PER];
 #pragma unroll
       for (int q = 0; q < PER; ++q) {
         const int p = t + sl + L * q;
-        if (MODE == 2) {
-          j[q] = jn[q];
-          a[q] = an[q];
-          const int pn = p + NB;  // the next batch's entry of this lane
-          jn[q] = 0;
-          an[q] = 0.f;
-          if (pn < len) {
-            jn[q] = ld_stream_i32(ix + pn, pol_stream) - base;
-            an[q] = ld_stream_f32(vx + pn, pol_stream);
-          }
-        } else {
-          j[q] = 0;
-          a[q] = 0.f;
-          if (p < len) {
-            j[q] = ld_stream_i32(ix + p, pol_stream) - base;
-            a[q] = ld_stream_f32(vx + p, pol_stream);
-          }
+        j[q] = 0;
+        a[q] = 0.f;
+        if (p < len) {
+          j[q] = ld_stream_i32(ix + p, pol_stream) - base;
+          a[q] = ld_stream_f32(vx + p, pol_stream);
         }
       }
       if (t + NB <= len && active) {  // full batch
@@ -654,16 +610,16 @@ void vrow_free(VrowSchedule* v, cudaStream_t s) {
   if (v) *v = VrowSchedule{};
 }
 
-template <int L, int NB, int MINB, bool ASYNC, int MODE = 0, bool ALL = false>
+template <int L, int NB, int MINB, bool ASYNC, bool ALL = false>
 static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const float* B,
                        int64_t ldb, int64_t nk, float* C, int64_t ldc, int accumulate, float* partial,
                        cudaStream_t s) {
   if constexpr (ASYNC) {
     if (!ALL && nk % (4 * L) == 0)  // no masked lanes: the unmasked build
-      return launch_vrow<L, NB, MINB, true, MODE, true>(ctx, v, A, B, ldb, nk, C, ldc, accumulate, partial, s);
+      return launch_vrow<L, NB, MINB, true, true>(ctx, v, A, B, ldb, nk, C, ldc, accumulate, partial, s);
   }
   auto kern = [] {
-    if constexpr (ASYNC) return spmm_vrow_async_k<L, NB, MINB, ALL, MODE>;
+    if constexpr (ASYNC) return spmm_vrow_async_k<L, NB, MINB, ALL>;
     else return spmm_vrow_k<L, NB, MINB>;
   }();
   using LdT = std::conditional_t<ASYNC, int, int64_t>;
@@ -718,8 +674,7 @@ size_t spmm_vrow_scratch_bytes(const VrowSchedule& v, int64_t nk) {
 
 int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const void* B, int64_t ldb,
               int64_t nk, void* C, int64_t ldc, int accumulate, int slab, void* partial,
-              cudaStream_t s, int gather) {
-  const bool async_gather = gather != VR_GATHER_REGS;
+              cudaStream_t s, bool async_gather) {
   if (A->val_t != FGB_F32 || A->idx_t != FGB_I32)
     return set_error(FGB_EUNSUPPORTED, "spmm vrow: F32 values and int32 indices only");
   if (nk % 4 || ldb % 4 || ldc % 4 || (uintptr_t)B % 16 || (uintptr_t)C % 16)
@@ -730,15 +685,7 @@ int spmm_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A, const vo
   float* part = (float*)partial;
   if (async_gather && ldb > INT32_MAX)
     return set_error(FGB_EUNSUPPORTED, "spmm vrow: cp.async gathers need a leading dimension below 2^31");
-  if (gather == VR_GATHER_ASYNC_PF) {
-    if (slab == 8) return launch_vrow<2, 8, 6, true, 1>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-    if (slab == 16) return launch_vrow<4, 8, 6, true, 1>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-    if (slab == 32) return launch_vrow<8, 8, 6, true, 1>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  } else if (gather == VR_GATHER_ASYNC_PIPE) {
-    if (slab == 8) return launch_vrow<2, 8, 6, true, 2>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-    if (slab == 16) return launch_vrow<4, 8, 6, true, 2>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-    if (slab == 32) return launch_vrow<8, 8, 6, true, 2>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
-  } else if (async_gather) {  // 32 KB of gather slots per block: 6 blocks (48 warps) per SM
+  if (async_gather) {  // 32 KB of gather slots per block: 6 blocks (48 warps) per SM
     if (slab == 8) return launch_vrow<2, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
     if (slab == 16) return launch_vrow<4, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);
     if (slab == 32) return launch_vrow<8, 8, 6, true>(ctx, v, A, b, ldb, nk, c, ldc, accumulate, part, s);

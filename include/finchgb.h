@@ -249,18 +249,15 @@ FGB_API int fgb_spmm_semiring(fgb_ctx* ctx, int semiring, const fgb_sparse* A, c
  * lanes * vector-width, one launch per slab, so the gathered slab of B stays
  * L2-resident.  Zero fields take the defaults. */
 typedef struct fgb_spmm_tuning {
-  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variants 2-4: 2, 4 or 8) */
+  int32_t lanes;   /* 2, 4, 8, 16 or 32 (variants 2 and 3: 2, 4 or 8) */
   int32_t variant; /* 0: B rows gathered into registers; 1: B rows staged into a
                       shared-memory ring by TMA tile::gather4 (fp32); 2: rows
                       cut into virtual rows of at most `path` entries, sorted
                       by length, one launch per column slab of 4 * lanes (fp32);
                       3: variant 2 with the gathers staged in shared memory by
-                      cp.async (more warps per SM; identical results);
-                      4: variant 3 with each lane group's next virtual row's
-                      indices and values bulk-prefetched into L2 (identical
-                      results) */
-  int64_t path;    /* merge-path item length (variants 2-4: virtual-row length) */
-  int32_t bands;   /* variants 2-4: cut A's columns into this many bands of
+                      cp.async (more warps per SM; identical results) */
+  int64_t path;    /* merge-path item length (variants 2, 3: virtual-row length) */
+  int32_t bands;   /* variants 2, 3: cut A's columns into this many bands of
                       consecutive columns (0 or 1: none, at most 8), each band's
                       entries in launches of their own, so a launch gathers from
                       1/bands of B's slab; a row's sum still runs over its

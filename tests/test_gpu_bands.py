@@ -46,9 +46,6 @@ def test_spmm_bands(gpu_lib, nk):
                                                            bands=bands)))
                 C2 = to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=2, bands=bands))
                 assert np.array_equal(C1, C2)
-                for v in (4, 5):  # L2 prefetch, register pipeline: no change in arithmetic
-                    assert np.array_equal(C1, to_host(dev.spmm(A, Bd, lanes=lanes, path=T, variant=v,
-                                                               bands=bands)))
                 assert np.array_equal(C1[short], flat[short])
 
 
@@ -67,7 +64,7 @@ def test_spmm_bands_accumulate_strides_empty(gpu_lib):
     B48 = np.ascontiguousarray(Bfull[:, :48])
     want = oracle.spmm_csr(500, 300, r.ptr, r.idx, r.val, B48, C=np.ascontiguousarray(C0[:, :48]),
                            init=False)
-    for bands, variant in ((2, 3), (4, 3), (8, 3), (4, 2), (4, 4), (2, 5)):
+    for bands, variant in ((2, 3), (4, 3), (8, 3), (4, 2)):
         Cd = to_dev(C0)
         dev.spmm(A, to_dev(Bfull)[:, :48], Cd[:, :48], flags=L.ACCUMULATE, lanes=8, path=16, variant=variant,
                  bands=bands)
@@ -78,7 +75,7 @@ def test_spmm_bands_accumulate_strides_empty(gpu_lib):
         assert_close(Cw, oracle.spmm_csr(500, 300, r.ptr, r.idx, r.val, B48), spmm_scale(r, B48), np.float32)
         assert not Cw[np.diff(r.ptr) == 0].any()  # empty rows written as zeros
     empty = upload(csr_from_dense(np.zeros((40, 30), dtype=np.float32)))
-    for variant in (2, 3, 4, 5):
+    for variant in (2, 3):
         Ce = dev.spmm(empty, to_dev(rng.standard_normal((30, 16)).astype(np.float32)), variant=variant, bands=4)
         assert not to_host(Ce).any()
 
@@ -89,7 +86,7 @@ def test_spmm_bands_rejects(gpu_lib):
     A = upload(r)
     Bd = to_dev(rng.standard_normal((100, 32)).astype(np.float32))
     for kw in ({"variant": 3, "bands": 9}, {"variant": 3, "bands": -1}, {"variant": 0, "bands": 2},
-               {"variant": 6}):
+               {"variant": 4}):
         with pytest.raises(L.FinchGBError) as e:
             dev.spmm(A, Bd, lanes=8, path=64, **kw)
         assert e.value.status == L.EINVAL
