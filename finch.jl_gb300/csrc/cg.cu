@@ -101,10 +101,6 @@ __device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {  // exact hi prod
   e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e));
   return quick_two_sum(p, e);
 }
-__device__ __forceinline__ float2 ff_mul_f(float a, float2 b) {  // a float times a pair
-  const float p = __fmul_rn(a, b.x);
-  return quick_two_sum(p, __fmaf_rn(a, b.y, __fmaf_rn(a, b.x, -p)));
-}
 __device__ __forceinline__ float2 ff_from_double(double d) {
   const float hi = __double2float_rn(d);
   return make_float2(hi, __double2float_rn(d - (double)hi));
@@ -189,6 +185,20 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
   if (threadIdx.x == 0) part[blockIdx.x] = dot;
 }
 
+// One product a * p[j] added to a row's running pair sum (h, l): TwoSum on
+// the high parts, the product's exact error (an FMA) and p's low part
+// folded into l in FP32, so each entry costs 11 FP32 operations; (h, l) is
+// normalised once per row.  l's own rounding keeps the sum within about
+// 2^-48 of the sum of |terms| (Dekker's pair addition without the
+// per-term renormalisation).
+__device__ __forceinline__ void ff_row_term(float& h, float& l, float a, float2 pj) {
+  const float ph = __fmul_rn(a, pj.x);
+  const float pe = __fmaf_rn(a, pj.y, __fmaf_rn(a, pj.x, -ph));
+  const float2 s = two_sum(h, ph);
+  h = s.x;
+  l = __fadd_rn(l, __fadd_rn(s.y, pe));
+}
+
 // The pair-sum SpMV: q = A p and the block partial of p.q, all in pairs;
 // the partial leaves the block as one FP64 number.
 template <class VT, class PtrT, class IX>
@@ -203,12 +213,13 @@ __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
     const bool two = i2 < n;
     const int64_t a0 = ld_ptr(ptr, i) - base, a1 = ld_ptr(ptr, i + 1) - base;
     const int64_t b0 = two ? ld_ptr(ptr, i2) - base : 0, b1 = two ? ld_ptr(ptr, i2 + 1) - base : 0;
-    float2 acc_a = make_float2(0.f, 0.f), acc_b = make_float2(0.f, 0.f);
+    float ha = 0.f, la_ = 0.f, hb = 0.f, lb_ = 0.f;
     const int64_t la = a1 - a0, lb = b1 - b0;
     for (int64_t t = 0; t < (la > lb ? la : lb); ++t) {
-      if (t < la) acc_a = ff_add(acc_a, ff_mul_f(cg_val(val, a0 + t), __ldg(p + cg_col(idx, a0 + t, i, base))));
-      if (t < lb) acc_b = ff_add(acc_b, ff_mul_f(cg_val(val, b0 + t), __ldg(p + cg_col(idx, b0 + t, i2, base))));
+      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), __ldg(p + cg_col(idx, a0 + t, i, base)));
+      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), __ldg(p + cg_col(idx, b0 + t, i2, base)));
     }
+    const float2 acc_a = two_sum(ha, la_), acc_b = two_sum(hb, lb_);  // l may exceed h after cancellation
     q[i] = acc_a;
     dot = ff_add(dot, ff_mul(__ldg(p + i), acc_a));
     if (two) {

@@ -61,7 +61,7 @@ struct __align__(16) DevMatrix {
   const float* val;
   int32_t nrows, ncols, base, nnz;
   int32_t lanes;  // SpMV lanes per row (a power of two <= 32), from the matrix's size class
-  int32_t rpi;    // rows per work item, from the matrix's size class
+  int32_t rpi;    // rows per work item of per-call launches, from the matrix's size class
 };
 
 // Size classes of registered matrices by mean stored entries per row:
@@ -539,6 +539,14 @@ size_t req_out_bytes(const fgb_server* s, const fgb_request& r, int64_t nnz) {
   return sizeof(float) * (size_t)nnz;
 }
 
+// Rows per work item of a request on A: the class's tuned value for the
+// per-call launches (where it sets the grid, so the latency), the configured
+// one for the batched loop (where it sets how many items are staged and
+// claimed).  Items only split rows; a row's sum is the same either way.
+int item_rows(const fgb_server* s, const DevMatrix& A) {
+  return s->cfg.mode == FGB_SERVE_PER_CALL ? A.rpi : s->cfg.rows_per_item;
+}
+
 SrvArgs make_args(fgb_server* s) {
   SrvArgs a;
   a.mats = s->d_mats;
@@ -588,7 +596,7 @@ void run_per_call(fgb_server* s, std::vector<uint64_t>& batch, std::unique_lock<
     if (t.in_bytes) e = cudaMemcpyAsync(s->pool + t.in_off, r.input, t.in_bytes, cudaMemcpyHostToDevice, s->copy_stream);
     if (e == cudaSuccess && t.n_items > 0) {
       serve_one_k<<<(unsigned)t.n_items, SRV_THREADS, 0, s->copy_stream>>>(make_args(s), slot, (int)t.rows,
-                                                                           s->mats[r.matrix].rpi);
+                                                                           item_rows(s, s->mats[r.matrix]));
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && !t.out_mapped)
@@ -673,7 +681,7 @@ void worker_main(fgb_server* s) {
         rq.item0 = t.item0;
         rq.slot = t.slot;
         rq.rows = (int32_t)t.rows;
-        rq.rows_per_item = s->mats[t.req.matrix].rpi;
+        rq.rows_per_item = item_rows(s, s->mats[t.req.matrix]);
         rq.pad = 0;
         max_chunks = std::max<uint64_t>(max_chunks, (rq.bytes + STAGE_CHUNK - 1) / STAGE_CHUNK);
         n_new += t.n_items;
@@ -953,7 +961,7 @@ static int submit_locked(fgb_server* s, const fgb_request* r, const MappedBufs& 
   Ticket t;
   t.req = *r;
   t.rows = A.nrows;
-  t.n_items = (A.nrows + A.rpi - 1) / A.rpi;
+  t.n_items = (A.nrows + item_rows(s, A) - 1) / item_rows(s, A);
   t.in_bytes = req_in_bytes(s, *r);
   t.out_bytes = req_out_bytes(s, *r, A.nnz);
   // a page-locked output is written by the device in place (no copy back);

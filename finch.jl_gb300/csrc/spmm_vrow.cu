@@ -625,7 +625,10 @@ static int launch_vrow(fgb_ctx* ctx, const VrowSchedule& v, const fgb_sparse* A,
   using LdT = std::conditional_t<ASYNC, int, int64_t>;
   const size_t smem = ASYNC ? sizeof(float4) * NB * VR_THREADS : 0;
   static const int occ = [&] {  // once per process (one device model); thread-safe
-    if (ASYNC) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (ASYNC) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, VR_THREADS, smem);
     return o > 0 ? o : 1;

@@ -558,7 +558,8 @@ typedef enum {
 typedef struct fgb_server_config {
   size_t pool_bytes;     /* HBM budget for in-flight inputs/outputs (admission) */
   int32_t max_inflight;  /* request slots, <= 4096 */
-  int32_t rows_per_item; /* rows per work item of every size class until tuned (default 64) */
+  int32_t rows_per_item; /* rows per work item (default 64): the batched loop's, and per-call
+                          * launches' until fgb_server_tune sets them per size class */
   int32_t blocks_per_sm; /* persistent blocks per SM (default 4; capped one below occupancy) */
   int32_t idle_exit_us;  /* device loop exits after this long without work (default 20000) */
   int32_t mode;          /* fgb_serve_mode */
@@ -617,7 +618,8 @@ FGB_API int fgb_server_stats_get(fgb_server* srv, fgb_server_stats* out);
 typedef struct fgb_server_class_shape {
   int32_t matrices;      /* registered matrices of the class (tune: output only) */
   int32_t lanes;         /* SpMV lanes per row */
-  int32_t rows_per_item; /* rows per work item */
+  int32_t rows_per_item; /* rows per work item of per-call launches (the batched
+                          * loop keeps the configured value: items only split rows) */
   int32_t reserved;
   double ms;             /* tune: time of the class's sample at the chosen shape (-1: none) */
   double ms_default;     /* tune: the same sample at 32 lanes and the configured rows per item */
@@ -630,9 +632,9 @@ typedef struct fgb_server_tuning {
  * with registered matrices, times SpMV requests on up to 8 of them through
  * the serving kernel itself at every shape (lanes 2..32, rows per item
  * 32..256), reps timed runs each, keeps the fastest and applies it to the
- * class (its matrices and later registrations).  Both modes compute a row
- * the same way for a given shape, so batched and per-call results stay
- * identical at the same shapes.  The server must be idle (FGB_EBUSY
+ * class (its matrices and later registrations).  Both modes sum a row the
+ * same way for given lanes, so batched and per-call results stay identical
+ * under the same tuning.  The server must be idle (FGB_EBUSY
  * otherwise).  Synchronous; allocates its timing buffers. */
 FGB_API int fgb_server_tune(fgb_server* srv, int32_t reps, fgb_server_tuning* out);
 /* Applies shapes (lanes, rows_per_item per class; other fields ignored),
