@@ -14,6 +14,7 @@ Lower layers:
 """
 from . import _lib
 from ._lib import FinchGBError
+from .algebra import AbstractAlgebra, DefaultAlgebra
 from .fileio import FinchExtensionError, fread, fwrite
 from .device import DeviceSparse, context, ewise, ewise_reduce, sddmm, spmm, spmv
 from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, reduce, tensordot
@@ -24,7 +25,7 @@ from .tensors import (GPU, Dense, Element, Pattern, SparseByteMap, SparseCOO, Sp
 from .galley import GalleyScheduler, galley_scheduler
 
 __all__ = [
-    "SparseByteMap", "pattern", "set_fill_value",
+    "SparseByteMap", "pattern", "set_fill_value", "AbstractAlgebra", "DefaultAlgebra",
     "FinchGBError", "FinchGBUnsupported", "DeviceSparse", "context", "spmv", "spmm", "sddmm",
     "ewise", "ewise_reduce", "LazyTensor", "lazy", "compute", "einsum", "finch", "tensordot",
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",

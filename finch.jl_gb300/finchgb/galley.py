@@ -491,7 +491,7 @@ class GalleyScheduler(GB300Scheduler):
     hands every other plan to the single-kernel matcher.  `last_plan` holds
     the chosen steps and their estimated seconds."""
 
-    OPTIONS = ("finch_order", "verbose", "estimator")
+    OPTIONS = ("finch_order", "verbose", "estimator", "algebra")
 
     def __init__(self, estimator: str = "dc", verbose: bool = False, **kw):
         super().__init__(verbose=verbose, **kw)

@@ -26,6 +26,7 @@ import torch
 
 from . import _lib as L
 from . import device as dev
+from .algebra import AbstractAlgebra, DefaultAlgebra
 from .logic import (Access, Aggregate, EinsumPlan, LazyTensor, Literal, MapJoin, Node, Reorder,
                     flatten, indices_of, parse_einsum, parse_finch)
 from .tensors import (GPU, SwizzleArray, Tensor, dense_from_device, sparse_from_device, transfer)
@@ -165,15 +166,21 @@ class GB300Scheduler:
 
     `finch_order=True` evaluates float sums in Finch's serial order (one
     running value per output, j ascending), bit-identical to Finch's CPU
-    nest; otherwise lane-parallel reductions are used."""
+    nest; otherwise lane-parallel reductions are used.  `algebra` decides,
+    as Finch's algebra does, whether a sparse operand's fill may be skipped:
+    every kernel visits stored entries only, so a plan matches one only when
+    the fill annihilates the product (or, for sums of one operand, is the
+    identity of the sum)."""
 
     # the options that make two schedulers equal (src/scheduler/
     # LogicExecutor.jl:77-78 compares and hashes the options, not the state)
-    OPTIONS = ("finch_order", "verbose")
+    OPTIONS = ("finch_order", "verbose", "algebra")
 
-    def __init__(self, finch_order: bool = False, verbose: bool = False):
+    def __init__(self, finch_order: bool = False, verbose: bool = False,
+                 algebra: AbstractAlgebra | None = None):
         self.finch_order = finch_order
         self.verbose = verbose
+        self.algebra = algebra if algebra is not None else DefaultAlgebra()
         self.last_kernel = None
 
     def options(self) -> dict:
@@ -192,6 +199,16 @@ class GB300Scheduler:
 
     def __hash__(self):
         return hash((type(self).__name__, tuple(sorted(self.options().items()))))
+
+    def _skippable(self, t, op: str, kind: str = "annihilator") -> None:
+        """Refuses a sparse operand whose fill the algebra does not let the
+        kernel skip: op's annihilator (a product) or identity (a sum)."""
+        fill = (t.body if isinstance(t, SwizzleArray) else t).fill_value
+        test = self.algebra.isannihilator if kind == "annihilator" else self.algebra.isidentity
+        if not test(op, fill):
+            raise FinchGBUnsupported(
+                f"the fill {fill!r} of {t!r} is not the {kind} of {op!r} in {self.algebra!r}: the kernels "
+                f"skip unstored entries (declare it in an algebra of your own)")
 
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
@@ -218,6 +235,7 @@ class GB300Scheduler:
                         and set(a.idxs) == {i, j} and isinstance(x, Access) and _is_dense(x.tns)
                         and x.idxs == (j,)):
                     sr = _SEMIRINGS[(m.agg, mul)]
+                    self._skippable(a.tns, mul)
                     A = sparse_operand(a.tns, a.idxs, (i, j))
                     xv = dense_operand(x.tns, x.idxs, (j,))
                     flags = 0
@@ -250,6 +268,7 @@ class GB300Scheduler:
         for a, b in (args, args[::-1]):
             if (isinstance(a, Access) and _is_sparse(a.tns) and set(a.idxs) == {i, j}
                     and isinstance(b, Access) and _is_dense(b.tns) and set(b.idxs) == {j, k}):
+                self._skippable(a.tns, "*")
                 A = sparse_operand(a.tns, a.idxs, (i, j))
                 if A.orient == "csc":
                     A = _csr_copy(a.tns, A)
@@ -276,13 +295,10 @@ class GB300Scheduler:
                     continue
                 sr = _SEMIRINGS[(m.agg, mul)]
                 # only A's stored entries are visited, which is exact when A's
-                # fill annihilates (*) into the identity of (+): -Inf for
-                # max-plus, +Inf for min-plus, false for or-and
+                # fill annihilates the product: +-Inf for (+), false for (&)
                 # (src/symbolic/symbolic.jl:89-166)
-                fill = (a.tns.body if isinstance(a.tns, SwizzleArray) else a.tns).fill_value
+                self._skippable(a.tns, mul)
                 want = {L.MAX_PLUS: -np.inf, L.MIN_PLUS: np.inf, L.OR_AND: False}[sr]
-                if not (fill == want or (sr == L.OR_AND and not fill)):
-                    raise FinchGBUnsupported(f"<<{m.agg}>>= over {a.tns!r} needs its fill {want}, not {fill}")
                 A = sparse_operand(a.tns, a.idxs, (i, j))
                 if A.orient == "csc":
                     A = _csr_copy(a.tns, A)
@@ -316,6 +332,8 @@ class GB300Scheduler:
             a, b = b, a
         if set(a.idxs) != {i, j} or set(b.idxs) != {j, k}:
             return None
+        self._skippable(a.tns, "*")
+        self._skippable(b.tns, "*")
         A = sparse_operand(a.tns, a.idxs, (i, j))
         B = sparse_operand(b.tns, b.idxs, (j, k))
         if A.val is None or B.val is None:
@@ -361,6 +379,7 @@ class GB300Scheduler:
                 Y = a
         if A is None or X is None or Y is None:
             return None
+        self._skippable(A.tns, "*")
         Ad = sparse_operand(A.tns, A.idxs, (i, j))
         Xd = dense_operand(X.tns, X.idxs, (i, k))
         Yd = dense_operand(Y.tns, Y.idxs, (j, k))
@@ -381,6 +400,11 @@ class GB300Scheduler:
                 and _is_sparse(b.tns)):
             return None
         i, j = m.outs
+        # a product is stored where both are (each fill annihilates it); a
+        # sum where either is (each fill the identity of the sum)
+        kind = "annihilator" if m.core.op == "*" else "identity"
+        self._skippable(a.tns, m.core.op, kind)
+        self._skippable(b.tns, m.core.op, kind)
         Ad = sparse_operand(a.tns, a.idxs, (i, j))
         Bd = sparse_operand(b.tns, b.idxs, (i, j))
         if Ad.orient != Bd.orient:
@@ -406,6 +430,10 @@ class GB300Scheduler:
         others = [t for t in terms if t is not a]
         if others and set(others[0].idxs) != {i, j}:
             return None
+        if others:
+            self._skippable(a.tns, "*")
+        else:
+            self._skippable(a.tns, "+", "identity")
         Ad = sparse_operand(a.tns, a.idxs, (i, j))
         Bs = Bdn = None
         if others:
@@ -573,15 +601,22 @@ def compute(x, ctx: GB300Scheduler | None = None, verbose: bool = False):
     return sched(Reorder(x.node, x.idxs))
 
 
-def einsum(stmt: str, init=None, ctx: GB300Scheduler | None = None, **tensors):
+def _with_algebra(sched: GB300Scheduler, algebra: AbstractAlgebra | None) -> GB300Scheduler:
+    return sched if algebra is None or sched.algebra == algebra else sched.set_options(algebra=algebra)
+
+
+def einsum(stmt: str, init=None, ctx: GB300Scheduler | None = None, algebra: AbstractAlgebra | None = None,
+           **tensors):
     """@einsum (src/interface/einsum.jl:190-201):
 
         y = einsum("y[i] += A[i,j] * x[j]", A=A, x=x)
         y = einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x)
         s = einsum("s[] += r[i] * r[i]", r=r)
-    """
+
+    algebra: as Finch's `@finch algebra ...`, the properties that decide
+    whether unstored entries may be skipped (default: DefaultAlgebra)."""
     plan: EinsumPlan = parse_einsum(stmt, tensors, init)
-    return (ctx or _scheduler)(plan.logic())
+    return _with_algebra(ctx or _scheduler, algebra)(plan.logic())
 
 
 def _device_vector(t, dtype) -> torch.Tensor:
@@ -604,7 +639,8 @@ def _rows_of(t) -> dev.DeviceSparse:
     return A if A.orient == "csr" else _csr_copy(t, A)
 
 
-def finch(program: str, ctx: GB300Scheduler | None = None, **tensors) -> dict:
+def finch(program: str, ctx: GB300Scheduler | None = None, algebra: AbstractAlgebra | None = None,
+          **tensors) -> dict:
     """@finch over a loop program; returns {output name: tensor}.
 
     A program that initialises its output (`y .= 0`) gets a fresh result;
@@ -626,7 +662,7 @@ def finch(program: str, ctx: GB300Scheduler | None = None, **tensors) -> dict:
     prog = parse_finch(program)
     plan = parse_einsum(prog.stmt, tensors)
     name = plan.out_name
-    sched = ctx or GB300Scheduler(finch_order=True)
+    sched = _with_algebra(ctx or GB300Scheduler(finch_order=True), algebra)
     if name in prog.init:
         init = prog.init[name]
         if plan.op is not None and init != _identity_value(plan.op, init):

@@ -84,18 +84,23 @@ def test_einsum_elementwise_sparse(gpu_lib):
 
 
 def test_semiring_einsum(gpu_lib):
+    """Max- and min-plus SpMV over tensors whose fill (-Inf, +Inf)
+    annihilates +, so skipping unstored entries is Finch's own result; a fill
+    of 0 would make Finch fold 0 + q[k] for every unstored k, which no kernel
+    here does, so that program is refused."""
     rng = np.random.default_rng(2)
     P = np.where(rng.random((30, 30)) < 0.2, rng.integers(1, 9, (30, 30)), 0).astype(np.float64)
     q = rng.integers(0, 9, 30).astype(np.float64)
-    Pt = csc(P, 0.0)
-    R = F.einsum("R[i] <<max>>= P[i,k] + q[k]", P=Pt, q=vec(q))
+    R = F.einsum("R[i] <<max>>= P[i,k] + q[k]", P=csc(np.where(P != 0, P, -np.inf), -np.inf), q=vec(q))
     want = np.array([max([P[i, k] + q[k] for k in range(30) if P[i, k] != 0], default=-np.inf)
                      for i in range(30)])
     assert R.todense().tolist() == want.tolist()
-    Rmin = F.einsum("R[i] <<min>>= P[i,k] + q[k]", P=Pt, q=vec(q))
+    Rmin = F.einsum("R[i] <<min>>= P[i,k] + q[k]", P=csc(np.where(P != 0, P, np.inf), np.inf), q=vec(q))
     want = np.array([min([P[i, k] + q[k] for k in range(30) if P[i, k] != 0], default=np.inf)
                      for i in range(30)])
     assert Rmin.todense().tolist() == want.tolist()
+    with pytest.raises(F.FinchGBUnsupported):
+        F.einsum("R[i] <<max>>= P[i,k] + q[k]", P=csc(P, 0.0), q=vec(q))
     Bp = F.Tensor(F.Dense(F.SparseList(F.Pattern())), P != 0)
     f = vec((rng.random(30) < 0.3).astype(np.bool_))
     reach = F.einsum("y[i] |= A[i,j] & f[j]", A=Bp, f=f)
@@ -123,6 +128,17 @@ def test_lazy_spmm_sddmm_reduce(gpu_lib):
     np.testing.assert_allclose(cs.todense(), D.sum(axis=0), rtol=1e-12, atol=1e-12)
 
 
+class GraphAlgebra(F.DefaultAlgebra):
+    """typemax(Int32) is "no edge": declared an annihilator of +, as a Finch
+    program over Int32 weights must declare it (Finch's default algebra
+    treats only infinities as annihilators of +, src/symbolic/symbolic.jl)."""
+
+    def isannihilator(self, op, x):
+        if op == "+" and x == np.iinfo(np.int32).max:
+            return True
+        return super().isannihilator(op, x)
+
+
 def test_bellman_ford_in_einsum(gpu_lib):
     from finchgb.scheduler import get_scheduler
     from finchgb.workloads import random_graph
@@ -133,9 +149,11 @@ def test_bellman_ford_in_einsum(gpu_lib):
     A = F.Tensor.from_buffers(F.Dense(F.SparseList(F.Element(np.int32(2**31 - 1), np.int32))), g)
     x = vec(np.where(np.arange(n) == 0, 0, 2**30).astype(np.int32))
     xh = x.todense().copy()
+    with pytest.raises(F.FinchGBUnsupported):  # the default algebra cannot skip typemax
+        F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x)
     kernels = []
     for _ in range(10):
-        y = F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x)
+        y = F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x, algebra=GraphAlgebra())
         kernels.append(get_scheduler().last_kernel)
         x = F.einsum("x[i] = min(x[i], y[i])", x=x, y=y)
         yh = oracle.spmv_csc(oracle.SR_MINP, n, n, g.ptr, g.idx, g.val, xh)
