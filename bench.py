@@ -958,6 +958,28 @@ def suite_cg() -> list[dict]:
              "higher_is_better": False, **v} for k, v in cg_lines(A, Ad, bd).items()]
 
 
+def suite_cg_probe() -> list[dict]:
+    """Two 16-iteration chunks of CG on the 2048^2 Poisson matrix in FP64 and
+    in BF16 pair mode: a short run of the iteration kernels (for ncu)."""
+    import torch
+
+    from finchgb import cg
+    from finchgb import device as dev
+    from finchgb.workloads import poisson2d
+
+    A = poisson2d(2048)
+    b = np.random.default_rng(SEED + 4).uniform(-1, 1, A.nrows)
+    Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
+    bd = torch.from_numpy(b).cuda()
+    out = []
+    for prec, acc in (("f64", "f64"), ("bf16", "pair")):
+        _, res = cg.cg_solve(Ad, bd, precision=prec, accumulate=acc, rtol=1e-10, max_iter=32, chunk=16)
+        torch.cuda.synchronize()
+        out.append({"suite": "cg_probe", "variant": f"{prec}_{acc}", "iterations": res.iterations,
+                    "seconds": round(res.seconds, 4)})
+    return out
+
+
 def serve_library(n_mats: int = 4096, n_partners: int = 512):
     """4,096 resident CSR matrices, rows log-uniform in [64, 8192], square,
     density U[0.5%, 5%], FP32 N(0,1), generated on the device; the first
@@ -1340,7 +1362,7 @@ def run_suite(args):
     from finchgb import build
 
     build.build()
-    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm):
+    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm, suite_cg_probe):
         if args.suite_only and fn.__name__ not in args.suite_only.split(","):
             continue
         try:

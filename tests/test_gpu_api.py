@@ -151,10 +151,11 @@ def test_bellman_ford_in_einsum(gpu_lib):
     xh = x.todense().copy()
     with pytest.raises(F.FinchGBUnsupported):  # the default algebra cannot skip typemax
         F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x)
+    sched = get_scheduler().set_options(algebra=GraphAlgebra())
     kernels = []
     for _ in range(10):
-        y = F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x, algebra=GraphAlgebra())
-        kernels.append(get_scheduler().last_kernel)
+        y = F.einsum("y[i] <<min>>= A[i,j] + x[j]", A=A, x=x, ctx=sched)
+        kernels.append(sched.last_kernel)
         x = F.einsum("x[i] = min(x[i], y[i])", x=x, y=y)
         yh = oracle.spmv_csc(oracle.SR_MINP, n, n, g.ptr, g.idx, g.val, xh)
         xh = np.minimum(xh, yh)
