@@ -200,24 +200,31 @@ __device__ __forceinline__ void ff_row_term(float& h, float& l, float a, float2 
 }
 
 // The pair-sum SpMV: q = A p and the block partial of p.q, all in pairs;
-// the partial leaves the block as one FP64 number.
-template <class VT, class PtrT, class IX>
+// the partial leaves the block as one FP64 number.  IT: the row, entry and
+// column arithmetic (int32 when rows and entries stay below 2^31, which
+// halves the integer instructions per entry).
+template <class VT, class PtrT, class IX, class IT>
 __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
-    int64_t n, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
+    int64_t n64, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const float2* __restrict__ p, float2* __restrict__ q, double* __restrict__ part) {
   __shared__ float2 sh[32];
   float2 dot = make_float2(0.f, 0.f);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
-    const int64_t i2 = i + stride;
+  const IT n = (IT)n64;
+  const IT stride = (IT)gridDim.x * (IT)blockDim.x;
+  auto col = [&](IT k, IT row) -> IT {
+    if constexpr (sizeof(IX) == 2) return row + (IT)__ldg(idx + k);
+    else return (IT)__ldg(idx + k) - (IT)base;
+  };
+  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += 2 * stride) {
+    const IT i2 = i + stride;
     const bool two = i2 < n;
-    const int64_t a0 = ld_ptr(ptr, i) - base, a1 = ld_ptr(ptr, i + 1) - base;
-    const int64_t b0 = two ? ld_ptr(ptr, i2) - base : 0, b1 = two ? ld_ptr(ptr, i2 + 1) - base : 0;
+    const IT a0 = (IT)(ld_ptr(ptr, i) - base), a1 = (IT)(ld_ptr(ptr, i + 1) - base);
+    const IT b0 = two ? (IT)(ld_ptr(ptr, i2) - base) : 0, b1 = two ? (IT)(ld_ptr(ptr, i2 + 1) - base) : 0;
     float ha = 0.f, la_ = 0.f, hb = 0.f, lb_ = 0.f;
-    const int64_t la = a1 - a0, lb = b1 - b0;
-    for (int64_t t = 0; t < (la > lb ? la : lb); ++t) {
-      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), __ldg(p + cg_col(idx, a0 + t, i, base)));
-      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), __ldg(p + cg_col(idx, b0 + t, i2, base)));
+    const IT la = a1 - a0, lb = b1 - b0, lmax = la > lb ? la : lb;
+    for (IT t = 0; t < lmax; ++t) {
+      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), __ldg(p + col(a0 + t, i)));
+      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), __ldg(p + col(b0 + t, i2)));
     }
     const float2 acc_a = two_sum(ha, la_), acc_b = two_sum(hb, lb_);  // l may exceed h after cancellation
     q[i] = acc_a;
@@ -525,9 +532,20 @@ static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int
     return g;
   } else {
     if (mode == CG_PAIR_SUMS) {
-      static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX>, 1 << 30, 1);
+      // 32-bit index arithmetic while rows (two per thread, a grid-stride
+      // apart) and entries stay below 2^31
+      const bool i32 = n + 2 * (int64_t)grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
+      if (i32) {
+        static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int32_t>, 1 << 30, 1);
+        const int g = std::max(1, std::min(grid, g0 * sms));
+        if (launch)
+          cgp_spmv_dot<VT, PtrT, IX, int32_t><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
+        return g;
+      }
+      static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int64_t>, 1 << 30, 1);
       const int g = std::max(1, std::min(grid, g0 * sms));
-      if (launch) cgp_spmv_dot<VT, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
+      if (launch)
+        cgp_spmv_dot<VT, PtrT, IX, int64_t><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
       return g;
     }
     if (mode == CG_F64_SUMS) {
