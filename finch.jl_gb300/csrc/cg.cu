@@ -31,7 +31,8 @@
 // One iteration is three kernels -- SpMV fused with the p.q partials; the r
 // update (every block folds the p.q partials itself) fused with the r.r
 // partials; the x and p updates fused with the folds -- so no scalar ever
-// leaves the device, and p is read once by the updates.  Partials are FP64
+// leaves the device, and p is read once by the updates.  They are chained by
+// programmatic dependent launch.  Partials are FP64
 // and folded by one warp per block in a fixed order: the solve is
 // deterministic.  A chunk of iterations is captured once in a CUDA graph and
 // replayed; the host reads the residual history once per chunk.
@@ -49,6 +50,15 @@ constexpr int CG_ILP = 4;  // elements per thread in flight in the streaming upd
 // elements in flight (up to 64 registers): few partials, one load per thread
 // in each block's fold of the previous kernel's partials.
 constexpr int CG_UPD_THREADS = 1024;
+
+// The iteration kernels are chained by programmatic dependent launch: each
+// lets the next one launch as soon as it starts, and waits for the previous
+// one to complete (its writes visible) before touching any data.  Launched
+// without the attribute, the wait returns at once.
+__device__ __forceinline__ void cg_pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 template <class T>
 __device__ __forceinline__ T cg_block_sum(T v, T* sh) {
@@ -147,6 +157,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_spmv_dot(
     int64_t n, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const double* __restrict__ p, const float* __restrict__ p32, double* __restrict__ q,
     double* __restrict__ part) {
+  cg_pdl_enter();
   __shared__ double sh[33];
   double dot = 0.0;
   auto term = [&](int64_t k, int64_t row, ACC acc) -> ACC {
@@ -207,6 +218,7 @@ template <class VT, class PtrT, class IX, class IT>
 __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
     int64_t n64, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const float2* __restrict__ p, float2* __restrict__ q, double* __restrict__ part) {
+  cg_pdl_enter();
   __shared__ float2 sh[32];
   float2 dot = make_float2(0.f, 0.f);
   const IT n = (IT)n64;
@@ -269,6 +281,7 @@ __device__ __forceinline__ double cg_alpha(const double* __restrict__ part_pq, i
 __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_r(
     int64_t n, double* __restrict__ r, const double* __restrict__ q, const double* __restrict__ part_pq,
     int nparts, const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
+  cg_pdl_enter();
   __shared__ double sh[33];
   __shared__ double s_alpha;
   if (threadIdx.x < 32) {
@@ -314,6 +327,7 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xp(
     float* __restrict__ p32, const double* __restrict__ part_pq, int nparts_pq,
     const double* __restrict__ part_rr, int nparts, double* __restrict__ rr, int slot_in, int slot_out,
     double* __restrict__ hist, int64_t it) {
+  cg_pdl_enter();
   __shared__ double s_ab[2];
   if (threadIdx.x < 32) {
     const double a = cg_alpha(part_pq, nparts_pq, rr, slot_in);
@@ -360,6 +374,7 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cg_update_xp(
 __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cgp_update_r(
     int64_t n, float2* __restrict__ r, const float2* __restrict__ q, const double* __restrict__ part_pq,
     int nparts, const double* __restrict__ rr, int slot, double* __restrict__ part_rr) {
+  cg_pdl_enter();
   __shared__ float2 sh[32];
   __shared__ float2 s_na;
   if (threadIdx.x < 32) {
@@ -399,6 +414,7 @@ __global__ void __launch_bounds__(CG_UPD_THREADS, 1) cgp_update_xp(
     int64_t n, float2* __restrict__ x, const float2* __restrict__ r, float2* __restrict__ p,
     const double* __restrict__ part_pq, int nparts_pq, const double* __restrict__ part_rr, int nparts,
     double* __restrict__ rr, int slot_in, int slot_out, double* __restrict__ hist, int64_t it) {
+  cg_pdl_enter();
   __shared__ float2 s_ab[2];
   if (threadIdx.x < 32) {
     const double a = cg_alpha(part_pq, nparts_pq, rr, slot_in);
@@ -499,6 +515,21 @@ __global__ void cgp_copy(int64_t n, const float2* __restrict__ src, float2* __re
     dst[i] = src[i];
 }
 
+// A launch of an iteration kernel, chained to the previous one (pdl) or not.
+template <class... KArgs, class... Args>
+static void cg_launch(void (*kern)(KArgs...), int grid, int block, cudaStream_t s, bool pdl, Args... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = s;
+  cfg.attrs = pdl ? at : nullptr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, (KArgs)args...);  // errors surface at the capture's end
+}
+
 struct CgBuffers {
   double *r = nullptr, *p = nullptr, *q = nullptr, *part_a = nullptr, *part_b = nullptr,
          *part_c = nullptr, *rr = nullptr, *bb = nullptr, *hist = nullptr;
@@ -520,7 +551,7 @@ static int occupancy_grid(K kernel, int grid, int sms) {
 // The iteration SpMV of one mode, value type and index form.
 template <class VT, class PtrT, class IX>
 static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int sms, const CgBuffers& b,
-                      cudaStream_t s, bool launch) {
+                      cudaStream_t s, bool launch, bool pdl) {
   const int64_t n = A->nrows;
   const PtrT* ptr = (const PtrT*)A->ptr;
   const VT* val = (const VT*)A->val;
@@ -528,7 +559,9 @@ static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int
   if constexpr (sizeof(VT) == 8) {  // the FP64 matrix: FP64 sums
     static const int g0 = occupancy_grid(cg_spmv_dot<VT, double, PtrT, IX>, 1 << 30, 1);
     const int g = std::max(1, std::min(grid, g0 * sms));
-    if (launch) cg_spmv_dot<VT, double, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, nullptr, b.q, b.part_a);
+    if (launch)
+      cg_launch(cg_spmv_dot<VT, double, PtrT, IX>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base, (const double*)b.p,
+                (const float*)nullptr, b.q, b.part_a);
     return g;
   } else {
     if (mode == CG_PAIR_SUMS) {
@@ -539,46 +572,52 @@ static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int
         static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int32_t>, 1 << 30, 1);
         const int g = std::max(1, std::min(grid, g0 * sms));
         if (launch)
-          cgp_spmv_dot<VT, PtrT, IX, int32_t><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
+          cg_launch(cgp_spmv_dot<VT, PtrT, IX, int32_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+                    (const float2*)b.p2, b.q2, b.part_a);
         return g;
       }
       static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int64_t>, 1 << 30, 1);
       const int g = std::max(1, std::min(grid, g0 * sms));
       if (launch)
-        cgp_spmv_dot<VT, PtrT, IX, int64_t><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p2, b.q2, b.part_a);
+        cg_launch(cgp_spmv_dot<VT, PtrT, IX, int64_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+                  (const float2*)b.p2, b.q2, b.part_a);
       return g;
     }
     if (mode == CG_F64_SUMS) {
       static const int g0 = occupancy_grid(cg_spmv_dot<VT, double, PtrT, IX>, 1 << 30, 1);
       const int g = std::max(1, std::min(grid, g0 * sms));
-      if (launch) cg_spmv_dot<VT, double, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, nullptr, b.q, b.part_a);
+      if (launch)
+        cg_launch(cg_spmv_dot<VT, double, PtrT, IX>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base, (const double*)b.p,
+                  (const float*)nullptr, b.q, b.part_a);
       return g;
     }
     static const int g0 = occupancy_grid(cg_spmv_dot<VT, float, PtrT, IX>, 1 << 30, 1);
     const int g = std::max(1, std::min(grid, g0 * sms));
-    if (launch) cg_spmv_dot<VT, float, PtrT, IX><<<g, CG_THREADS, 0, s>>>(n, ptr, ix, val, base, b.p, b.p32, b.q, b.part_a);
+    if (launch)
+      cg_launch(cg_spmv_dot<VT, float, PtrT, IX>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base, (const double*)b.p,
+                (const float*)b.p32, b.q, b.part_a);
     return g;
   }
 }
 
 template <class PtrT, class IX>
 static int spmv_dot_ix(const fgb_sparse* A, const IX* ix, int precision, int mode, int grid, int sms,
-                       const CgBuffers& b, cudaStream_t s, bool launch) {
-  if (precision == FGB_F64) return spmv_dot_t<double, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
-  if (precision == FGB_BF16) return spmv_dot_t<__nv_bfloat16, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
-  return spmv_dot_t<float, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch);
+                       const CgBuffers& b, cudaStream_t s, bool launch, bool pdl) {
+  if (precision == FGB_F64) return spmv_dot_t<double, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch, pdl);
+  if (precision == FGB_BF16) return spmv_dot_t<__nv_bfloat16, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch, pdl);
+  return spmv_dot_t<float, PtrT, IX>(A, ix, mode, grid, sms, b, s, launch, pdl);
 }
 
 // Launches (launch = true) or sizes (false) the iteration SpMV; returns its grid.
 static int spmv_dot(const fgb_sparse* A, const int16_t* off, int precision, int mode, int grid, int sms,
-                    const CgBuffers& b, cudaStream_t s, bool launch) {
+                    const CgBuffers& b, cudaStream_t s, bool launch, bool pdl = false) {
   const bool i32 = A->ptr_t == FGB_I32;
   if (off)
-    return i32 ? spmv_dot_ix<int32_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch)
-               : spmv_dot_ix<int64_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch);
+    return i32 ? spmv_dot_ix<int32_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch, pdl)
+               : spmv_dot_ix<int64_t, int16_t>(A, off, precision, mode, grid, sms, b, s, launch, pdl);
   const int* idx = (const int*)A->idx;
-  return i32 ? spmv_dot_ix<int32_t, int>(A, idx, precision, mode, grid, sms, b, s, launch)
-             : spmv_dot_ix<int64_t, int>(A, idx, precision, mode, grid, sms, b, s, launch);
+  return i32 ? spmv_dot_ix<int32_t, int>(A, idx, precision, mode, grid, sms, b, s, launch, pdl)
+             : spmv_dot_ix<int64_t, int>(A, idx, precision, mode, grid, sms, b, s, launch, pdl);
 }
 
 template <class PtrT>
@@ -734,17 +773,20 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
     const int grid_dot = spmv_dot(Ait, off, precision, mode, grid, ctx->num_sms, bufs, s, false);
     for (int t = 0; t < chunk; ++t) {
       const int si = t & 1, so = si ^ 1;
-      spmv_dot(Ait, off, precision, mode, grid, ctx->num_sms, bufs, s, true);
+      // every launch after the chunk's first is chained to its predecessor
+      spmv_dot(Ait, off, precision, mode, grid, ctx->num_sms, bufs, s, true, t > 0);
       if (pair) {
-        cgp_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r2, bufs.q2, bufs.part_a, grid_dot, bufs.rr, si,
-                                                        bufs.part_b);
-        cgp_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.x2, bufs.r2, bufs.p2, bufs.part_a, grid_dot,
-                                                         bufs.part_b, grid_upd, bufs.rr, si, so, bufs.hist, t);
+        cg_launch(cgp_update_r, grid_upd, CG_UPD_THREADS, s, true, n, bufs.r2, (const float2*)bufs.q2,
+                  (const double*)bufs.part_a, grid_dot, (const double*)bufs.rr, si, bufs.part_b);
+        cg_launch(cgp_update_xp, grid_upd, CG_UPD_THREADS, s, true, n, bufs.x2, (const float2*)bufs.r2, bufs.p2,
+                  (const double*)bufs.part_a, grid_dot, (const double*)bufs.part_b, grid_upd, bufs.rr, si, so,
+                  bufs.hist, (int64_t)t);
       } else {
-        cg_update_r<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, bufs.r, bufs.q, bufs.part_a, grid_dot, bufs.rr, si,
-                                                       bufs.part_b);
-        cg_update_xp<<<grid_upd, CG_UPD_THREADS, 0, s>>>(n, x, bufs.r, bufs.p, bufs.p32, bufs.part_a, grid_dot,
-                                                        bufs.part_b, grid_upd, bufs.rr, si, so, bufs.hist, t);
+        cg_launch(cg_update_r, grid_upd, CG_UPD_THREADS, s, true, n, bufs.r, (const double*)bufs.q,
+                  (const double*)bufs.part_a, grid_dot, (const double*)bufs.rr, si, bufs.part_b);
+        cg_launch(cg_update_xp, grid_upd, CG_UPD_THREADS, s, true, n, x, (const double*)bufs.r, bufs.p, bufs.p32,
+                  (const double*)bufs.part_a, grid_dot, (const double*)bufs.part_b, grid_upd, bufs.rr, si, so,
+                  bufs.hist, (int64_t)t);
       }
     }
     e = cudaStreamEndCapture(s, &graph);
