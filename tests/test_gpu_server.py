@@ -159,6 +159,32 @@ def test_tuned_shapes_same_alone_and_in_the_mix(library):
         assert e.value.status == L.EINVAL
 
 
+def test_tune_edge_cases(library):
+    """No matrices: every class empty, nothing changes.  A per-call server
+    tunes too, and a matrix registered after tuning takes its class's
+    shape."""
+    mats, partners = library
+    with Server(mode="batched") as srv:
+        t = srv.tune(reps=1)
+        assert all(c.matrices == 0 for c in t.cls) and Server.shapes(t) == []
+    with Server(mode="per_call") as srv:
+        ids = [srv.register(A) for A in mats[:4]]
+        t = srv.tune(reps=1)
+        assert sum(x["matrices"] for x in Server.shapes(t)) == 4
+        late = srv.register(mats[4])  # registered after tuning: its class's tuned shape
+        rng = np.random.default_rng(3)
+        for k, mid in list(enumerate(ids)) + [(4, late)]:
+            A = mats[k]
+            x = torch.from_numpy(rng.standard_normal(A.ncols).astype(np.float32)).pin_memory()
+            y = torch.empty(A.nrows, dtype=torch.float32).pin_memory()
+            srv.wait(srv.submit("spmv", mid, x, y))
+            ptr, idx, val = host_csr(A)
+            want = oracle.spmv_csr(0, A.nrows, A.ncols, ptr, idx, val.astype(np.float64), x.numpy().astype(np.float64))
+            scale = oracle.spmv_csr(0, A.nrows, A.ncols, ptr, idx, np.abs(val).astype(np.float64),
+                                    np.abs(x.numpy()).astype(np.float64))
+            assert (np.abs(y.numpy().astype(np.float64) - want) <= 2e-5 * scale + 1e-30).all()
+
+
 def test_admission_queues_when_pool_is_small(library):
     mats, partners = library
     rng = np.random.default_rng(2)
