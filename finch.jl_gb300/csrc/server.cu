@@ -1070,6 +1070,34 @@ static int apply_shapes(fgb_server* s, const int32_t* lanes, const int32_t* rpi)
 
 static bool server_idle(const fgb_server* s) { return s->queue.empty() && s->n_inflight == 0; }
 
+// The device loop leaves by itself once it has been idle for idle_exit_us;
+// waits (bounded: that time plus a second) until it has, so that nothing
+// else runs on the SMs.  False if it is still running.
+static bool wait_loop_exit(const fgb_server* s) {
+  if (!s->kernel_launched) return true;
+  const auto limit = std::chrono::steady_clock::now() + std::chrono::microseconds(s->cfg.idle_exit_us) +
+                     std::chrono::seconds(1);
+  while (cudaEventQuery(s->kernel_done) == cudaErrorNotReady) {
+    if (std::chrono::steady_clock::now() > limit) return false;
+    std::this_thread::sleep_for(std::chrono::microseconds(200));
+  }
+  cudaGetLastError();
+  return true;
+}
+
+// Makes the server's device current for a call made on a host thread of the
+// caller's, and restores the caller's on the way out.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != device) cudaSetDevice(device);
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 extern "C" {
 
 int fgb_server_tune(fgb_server* s, int32_t reps, fgb_server_tuning* out) {
@@ -1077,6 +1105,8 @@ int fgb_server_tune(fgb_server* s, int32_t reps, fgb_server_tuning* out) {
   if (reps <= 0) reps = 3;
   std::lock_guard<std::mutex> lk(s->mu);
   if (!server_idle(s)) return set_error(FGB_EBUSY, "fgb_server_tune: requests are in flight");
+  if (!wait_loop_exit(s)) return set_error(FGB_EBUSY, "fgb_server_tune: the device loop has not exited");
+  DeviceScope dev(s->ctx->device);
   *out = fgb_server_tuning{};
   static const int kLanes[] = {2, 4, 8, 16, 32};
   static const int kRpi[] = {32, 64, 128, 256};

@@ -122,8 +122,8 @@ def flatten(n: Node) -> Node:
 
 _OPS = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.BitOr: "|", ast.BitAnd: "&",
         ast.Div: "/"}
-_LHS = re.compile(r"^\s*(\w+)\s*\[([\w\s,]*)\]\s*(<<\s*([\w+*|&]+)\s*>>=|\+=|\*=|\|=|&=|=)\s*(.+)$",
-                  re.S)
+_LHS = re.compile(r"^\s*(\w+)\s*\[([\w\s,]*)\]\s*(<<\s*([\w+*|&]+(?:\([^)]*\))?)\s*>>=|\+=|\*=|\|=|&=|=)"
+                  r"\s*(.+)$", re.S)
 _REDUCERS = {"+": "+", "*": "*", "|": "|", "&": "&", "min": "min", "max": "max", "or": "|",
              "and": "&"}
 
@@ -189,7 +189,14 @@ def parse_einsum(stmt: str, tensors: dict, init=None) -> EinsumPlan:
         raise SyntaxError(f"einsum: cannot parse {stmt!r}")
     name, idxs, assign, custom, rhs = m.groups()
     out_idxs = tuple(s.strip() for s in idxs.split(",") if s.strip())
-    if custom:
+    if custom and (custom == "overwrite" or custom.startswith("initwrite(")):
+        # overwrite(a, b) = b and initwrite(z)(a, b) = b (src/util/special_
+        # functions.jl): assignments, not reductions -- the `=` form, with
+        # initwrite's z as the output's initial value
+        op = None
+        if custom.startswith("initwrite(") and init is None:
+            init = ast.literal_eval(custom[len("initwrite("):-1].strip() or "0")
+    elif custom:
         op = _REDUCERS[custom]
     elif assign == "=":
         op = None

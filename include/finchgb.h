@@ -634,7 +634,9 @@ typedef struct fgb_server_tuning {
  * 32..256), reps timed runs each, keeps the fastest and applies it to the
  * class (its matrices and later registrations).  Both modes sum a row the
  * same way for given lanes, so batched and per-call results stay identical
- * under the same tuning.  The server must be idle (FGB_EBUSY
+ * under the same tuning.  A batched server first waits (bounded) for its
+ * device loop's idle exit, so the timings have the GPU to themselves.  The
+ * server must be idle (FGB_EBUSY
  * otherwise).  Synchronous; allocates its timing buffers. */
 FGB_API int fgb_server_tune(fgb_server* srv, int32_t reps, fgb_server_tuning* out);
 /* Applies shapes (lanes, rows_per_item per class; other fields ignored),
@@ -660,7 +662,10 @@ typedef struct fgb_cg_options {
 #define FGB_CG_SUM_F64 1  /* SpMV: values widened to FP64, FP64 sums; vectors, dots, updates FP64 */
 #define FGB_CG_SUM_PAIR 2 /* SpMV sums, x, r, p, q, dots and updates in pairs of FP32 numbers
                            * (hi + lo, about 48 significant bits), no FP64 arithmetic per row or
-                           * stored entry: the fast mode on GPUs whose FP64 rate is far below FP32 */
+                           * stored entry: the fast mode on GPUs whose FP64 rate is far below FP32.
+                           * Pairs keep FP32's exponent range: the squares of the residual's
+                           * entries must stay above FP32's smallest normal (about 1e-38) down to
+                           * the tolerance, so scale b accordingly */
 
 typedef struct fgb_cg_result {
   int64_t iterations;       /* iterations run */

@@ -75,3 +75,18 @@ def test_schedulers_compare_by_algebra():
     c = a.set_options(algebra=GraphAlgebra())
     assert c != a and c.algebra == GraphAlgebra() and c.finch_order == a.finch_order
     assert GraphAlgebra() != F.DefaultAlgebra() and hash(GraphAlgebra()) == hash(GraphAlgebra())
+
+
+def test_overwrite_and_initwrite_parse_as_assignments():
+    """overwrite(a, b) = b and initwrite(z)(a, b) = b (src/util/special_functions.jl)
+    are assignments: the `=` form, initwrite's z the initial value; a write
+    that would keep the last of a reduced index's values is refused."""
+    from finchgb.logic import parse_einsum
+
+    H = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), np.eye(3))
+    p = parse_einsum("J[i,j] <<overwrite>>= H[i,j] * H[i,j]", {"H": H})
+    assert p.op is None and p.init is None
+    p = parse_einsum("J[i,j] <<initwrite(0.0)>>= H[i,j]", {"H": H})
+    assert p.op is None and p.init == 0.0
+    with pytest.raises(ValueError):
+        parse_einsum("y[i] <<overwrite>>= H[i,j]", {"H": H}).logic()

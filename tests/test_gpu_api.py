@@ -79,6 +79,7 @@ def test_einsum_elementwise_sparse(gpu_lib):
     I = sprand_int(rng, 5, 5, 0.6).astype(np.float64)
     J = F.einsum("J[i,j] = H[i,j] * I[i,j]", H=csc(H), I=csc(I))
     assert J == H * I
+    assert F.einsum("J[i,j] <<overwrite>>= H[i,j] * I[i,j]", H=csc(H), I=csc(I)) == H * I
     K = F.compute(F.lazy(csc(H)) + F.lazy(csc(I)))
     assert K == H + I
 
