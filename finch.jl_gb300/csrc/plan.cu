@@ -384,6 +384,16 @@ int fgb_plan_create(fgb_ctx* ctx, const fgb_plan_desc* desc, int32_t tune_reps, 
   p->info.first_candidate_ms = first_ms;
   p->info.candidates = (int32_t)cands.size();
   p->info.from_cache = cached ? 1 : 0;
+  p->info.launches = 0;  // kernel nodes of the captured graph: the launches of one execute
+  size_t nn = 0;
+  if (p->graph && cudaGraphGetNodes(p->graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (cudaGraphGetNodes(p->graph, nodes.data(), &nn) == cudaSuccess)
+      for (size_t k = 0; k < nn; ++k) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++p->info.launches;
+      }
+  }
   *out = p;
   return FGB_OK;
 }

@@ -71,7 +71,7 @@ class FgbPlanInfo(ctypes.Structure):
     _fields_ = [("lanes", c_int32), ("bands", c_int32), ("path", c_int64),
                 ("tuned_ms", c_double), ("first_candidate_ms", c_double),
                 ("candidates", c_int32), ("from_cache", c_int32), ("panels", c_int32),
-                ("variant", c_int32)]
+                ("variant", c_int32), ("launches", c_int32), ("reserved", c_int32)]
 
 
 class FgbServerConfig(ctypes.Structure):

@@ -516,6 +516,9 @@ typedef struct fgb_plan_info {
   int32_t panels;            /* SpMM: column panels of the chosen schedule (1 = none) */
   int32_t variant;           /* SpMM: fgb_spmm_tuning.variant; SDDMM: 3 virtual rows, 4 the same
                                 with cp.async gathers */
+  int32_t launches;          /* kernel launches of one fgb_plan_execute (the captured graph's
+                                kernel nodes) */
+  int32_t reserved;
 } fgb_plan_info;
 
 /* Autotunes (tune_reps timed runs per schedule on these operands; 0 = use
