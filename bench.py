@@ -283,10 +283,51 @@ def e2e_api(A_h, B_h, nbytes: int, steps: int) -> dict:
             "timing": "host wall clock per call (synchronous), Finch's Int64 ptr/idx uploaded and narrowed"}, C
 
 
+def spmv_config1() -> dict:
+    """Configuration 1 in the default run: y[i] += A[i,j]*x[j], A 10,000^2
+    CSC (fsprand p = 0.001), FP64; the three device schedules replayed as
+    graphs, their results against the oracle's FP64 nest (Finch order
+    bit-exact), and Finch's serial nest timed on one core."""
+    import torch
+
+    import oracle
+    from finchgb import _lib as L
+    from finchgb import device as dev
+    from finchgb.workloads import fsprand
+
+    rng = np.random.default_rng(SEED + 1)
+    n = 10_000
+    A = fsprand(rng, n, n, 0.001)
+    x = rng.random(n)
+    Ad = dev.DeviceSparse.from_host(n, n, A.ptr, A.idx, A.val, orient="csc")
+    Ar = Ad.transposed_storage()
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    nbytes = 12 * A.nnz + 4 * (n + 1) + 16 * n
+    want = oracle.spmv_csc(oracle.SR_PT, n, n, A.ptr, A.idx, A.val, x)
+    scale = oracle.spmv_csc(oracle.SR_PT, n, n, A.ptr, A.idx, np.abs(A.val), np.abs(x))
+    out = {"metric": "spmv_latency_us", "unit": "us", "higher_is_better": False, "dtype": "f64",
+           "config": {"workload": "fsprand 10000x10000 p=0.001 CSC, x U[0,1), FP64", "nnz": int(A.nnz)},
+           "cpu_baseline": {"value": round(_cpu_time(lambda: oracle.spmv_csc(0, n, n, A.ptr, A.idx, A.val, x))
+                                           * 1e6, 3), "unit": "us", "cores": 1, "kind": "port",
+                            "sample": "whole matrix, Finch's serial CSC nest (oracle)"}}
+    for name, fn in (("csc_push_atomic", lambda: dev.spmv(Ad, xd, y)),
+                     ("csr_pull_finch_order", lambda: dev.spmv(Ar, xd, y, flags=L.FINCH_ORDER | L.FMA)),
+                     ("csr_pull", lambda: dev.spmv(Ar, xd, y))):
+        ms = _graph_ms(fn)
+        fn()
+        got = y.cpu().numpy()
+        err = float(np.max(np.abs(got - want) / (scale + 1e-300)))
+        out[name] = {"us": round(ms * 1e3, 3), "roofline": _roof(nbytes, ms), "max_rel_err_vs_fp64": err,
+                     "bit_exact_vs_finch_nest": bool(np.array_equal(got, want))}
+    return out
+
+
 def suite_block(A_h, Ad) -> dict:
-    """Compact lines for the other configurations: SDDMM (k = 64) on the
-    headline matrix, 20 Bellman-Ford min-plus rounds on the 4M-node graph,
-    and mixed-precision CG on the 2048^2 Poisson matrix."""
+    """Compact lines for the other configurations: the FP64 SpMV of
+    configuration 1, SDDMM (k = 64) on the headline matrix, 20 Bellman-Ford
+    min-plus rounds on the 4M-node graph, and CG on the 2048^2 Poisson
+    matrix in every arithmetic mode."""
     import torch
 
     import oracle
@@ -296,7 +337,7 @@ def suite_block(A_h, Ad) -> dict:
     from finchgb.plan import Plan
     from finchgb.workloads import poisson2d, random_graph
 
-    out = {}
+    out = {"spmv_fp64_10k": spmv_config1()}
     m = A_h.nrows
     rng = np.random.default_rng(SEED + 1)
     X = rng.standard_normal((m, 64), dtype=np.float32)
