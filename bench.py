@@ -720,7 +720,7 @@ def _timed_ms(fn, reps: int = 20, warm: int = 3) -> float:
 
 def _graph_ms(fn, reps: int = 200) -> float:
     """Device time per call with `reps` calls captured in one CUDA graph (the
-    launch-latency-free figure for microsecond kernels)."""
+    launch-latency-free figure for microsecond kernels), median of 5 replays."""
     import torch
 
     s = torch.cuda.Stream()
@@ -735,12 +735,15 @@ def _graph_ms(fn, reps: int = 200) -> float:
     torch.cuda.synchronize()
     g.replay()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    g.replay()
-    e1.record()
-    torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / reps
+    times = []
+    for _ in range(5):  # the median of 5 replays: one disturbed replay does not set the figure
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / reps)
+    return float(np.median(times))
 
 
 def _cpu_time(fn, min_seconds: float = 2.0, max_reps: int = 1000) -> float:

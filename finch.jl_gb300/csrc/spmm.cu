@@ -229,9 +229,9 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
   cudaStream_t s = pick_stream(ctx, stream);
   // No schedule given: a B far larger than L2 with many stored entries takes
   // the virtual-row slab schedule with cp.async gathers (32-column slabs,
-  // 128-entry virtual rows, two column bands; on the 1M x 1M Zipf matrix with
-  // k = 128, 1.39 ms per call with its schedule built, against 1.48 ms
-  // without bands and 2.1 ms for the best merge path).
+  // 256-entry virtual rows, two column bands; on the 1M x 1M Zipf matrix with
+  // k = 128, 1.38 ms per call with its schedule built, against 1.40 ms with
+  // 128-entry rows, 1.48 ms without bands and 2.1 ms for the best merge path).
   if (variant == 0 && lanes <= 0 && path <= 0 && A->orient == FGB_CSR && dtype == FGB_F32 &&
       A->val_t == FGB_F32 && A->idx_t == FGB_I32 && !(flags & FGB_FINCH_ORDER) && nk >= 32 && nk % 4 == 0 &&
       ldb % 4 == 0 && ldc % 4 == 0 && ldb <= INT32_MAX && (uintptr_t)B % 16 == 0 && (uintptr_t)C % 16 == 0 &&
@@ -239,7 +239,7 @@ int spmm_impl(fgb_ctx* ctx, const fgb_sparse* A, const void* B, int64_t ldb, int
       (double)A->ncols * (double)nk * 4.0 > 64.0 * 1024 * 1024 && !stream_capturing(s)) {
     variant = 3;
     lanes = 8;
-    path = 128;
+    path = 256;
     bands = 2;
   }
   if (variant == 2 || variant == 3) {  // virtual-row column slabs: schedule built for this call

@@ -29,7 +29,7 @@ def test_spmm_default_is_the_slab_schedule_and_capture_safe(gpu_lib, big):
     A = upload(big)
     B = torch.randn((big.ncols, 32), dtype=torch.float32, device="cuda")  # 77 MB
     C_def = to_host(dev.spmm(A, B))
-    assert np.array_equal(C_def, to_host(dev.spmm(A, B, lanes=8, path=128, variant=3, bands=2)))
+    assert np.array_equal(C_def, to_host(dev.spmm(A, B, lanes=8, path=256, variant=3, bands=2)))
     C = torch.empty((big.nrows, 32), dtype=torch.float32, device="cuda")
     g = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
