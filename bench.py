@@ -415,7 +415,7 @@ def cg_lines(P, Pd, bd) -> dict:
 
     lines = {}
     for prec, acc in (("f64", "f64"), ("f32", "f32"), ("bf16", "f32"), ("f32", "f64"), ("bf16", "f64"),
-                      ("f32", "pair"), ("bf16", "pair")):
+                      ("f32", "spmv_pair"), ("bf16", "spmv_pair"), ("f32", "pair"), ("bf16", "pair")):
         x, res = cg.cg_solve(Pd, bd, precision=prec, rtol=1e-10, max_iter=60_000, accumulate=acc)
         vb = {"f64": 8, "f32": 4, "bf16": 2}[prec]
         ib = 2 if res.compact_index else 4

@@ -4,11 +4,14 @@
 //   alpha = rr / p.q @einsum s[] += p[i] * q[i]
 //   x += alpha p;  r -= alpha q;  rr' = r.r;  p = r + (rr'/rr) p
 //
-// run on the GPU in one of four arithmetic modes:
+// run on the GPU in one of five arithmetic modes:
 //   FP64          values, sums, vectors and updates in FP64;
 //   FP32 sums     FP32 or BF16 values times an FP32 copy of p, summed in
 //                 FP32; x, r, p, q, dots and updates FP64;
 //   FP64 sums     FP32 or BF16 values widened to FP64 and summed in FP64;
+//   SpMV pairs    FP32 or BF16 values times p split into a pair of FP32
+//                 numbers by integer operations, each row summed as a pair;
+//                 x, r, p, q, dots and updates FP64;
 //   pair sums     FP32 or BF16 values, and everything per row or per stored
 //                 entry -- the SpMV sums, x, r, p, q, the dot products and
 //                 updates -- in pairs of FP32 numbers (an unevaluated sum
@@ -248,6 +251,69 @@ __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
   }
   dot = ff_block_sum(dot, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = ff_to_double(dot);
+}
+
+// p (FP64) as a pair of FP32 numbers with integer operations only, so the
+// SpMV below executes no FP64 instruction per entry: hi = p's top 24
+// significand bits (a truncation), lo = the remaining 29 bits rounded to
+// FP32, scaled by p's exponent.  |hi + lo - p| <= 2^-48 |p| for
+// 2^-102 <= |p| < 2^128; below that lo, then hi, flush to zero (and
+// beyond it hi is an infinity).
+__device__ __forceinline__ float2 split_f64(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int hw = (unsigned int)(b >> 32), lw = (unsigned int)b;
+  const int e = (int)((hw >> 20) & 0x7FFu) - 1023;
+  const unsigned int sign = hw & 0x80000000u;
+  if (e < -126) return make_float2(0.f, 0.f);
+  if (e > 127) return make_float2(__uint_as_float(sign | 0x7F800000u), 0.f);
+  const float hi = __uint_as_float(sign | ((unsigned int)(e + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+  float lo = __uint2float_rn(lw & 0x1FFFFFFFu);  // 29 bits, rounded to 24
+  if (e >= -74) {
+    lo = __fmul_rn(lo, __uint_as_float((unsigned int)(e + 75) << 23));  // 2^(e - 52)
+  } else {  // 2^(e - 52) below FP32's normal range: two exact steps
+    lo = __fmul_rn(__fmul_rn(lo, __uint_as_float((unsigned int)(e + 139) << 23)), 5.421010862427522e-20f);  // 2^-64
+  }
+  return make_float2(hi, sign ? -lo : lo);
+}
+
+// The SpMV of the pair-sum SpMV mode: FP64 p split into pairs as it is
+// gathered, each row summed as a pair (ff_row_term), q and the p.q partial
+// in FP64 -- the vectors, dots and updates stay FP64.
+template <class VT, class PtrT, class IX, class IT>
+__global__ void __launch_bounds__(CG_THREADS) cgs_spmv_dot(
+    int64_t n64, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
+    int base, const double* __restrict__ p, double* __restrict__ q, double* __restrict__ part) {
+  cg_pdl_enter();
+  __shared__ double sh[33];
+  double dot = 0.0;
+  const IT n = (IT)n64;
+  const IT stride = (IT)gridDim.x * (IT)blockDim.x;
+  auto col = [&](IT k, IT row) -> IT {
+    if constexpr (sizeof(IX) == 2) return row + (IT)__ldg(idx + k);
+    else return (IT)__ldg(idx + k) - (IT)base;
+  };
+  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += 2 * stride) {
+    const IT i2 = i + stride;
+    const bool two = i2 < n;
+    const IT a0 = (IT)(ld_ptr(ptr, i) - base), a1 = (IT)(ld_ptr(ptr, i + 1) - base);
+    const IT b0 = two ? (IT)(ld_ptr(ptr, i2) - base) : 0, b1 = two ? (IT)(ld_ptr(ptr, i2 + 1) - base) : 0;
+    float ha = 0.f, la_ = 0.f, hb = 0.f, lb_ = 0.f;
+    const IT la = a1 - a0, lb = b1 - b0, lmax = la > lb ? la : lb;
+    for (IT t = 0; t < lmax; ++t) {
+      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), split_f64(__ldg(p + col(a0 + t, i))));
+      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), split_f64(__ldg(p + col(b0 + t, i2))));
+    }
+    const double qa = ff_to_double(two_sum(ha, la_));
+    q[i] = qa;
+    dot = __fma_rn(__ldg(p + i), qa, dot);
+    if (two) {
+      const double qb = ff_to_double(two_sum(hb, lb_));
+      q[i2] = qb;
+      dot = __fma_rn(__ldg(p + i2), qb, dot);
+    }
+  }
+  dot = cg_block_sum(dot, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = dot;
 }
 
 // The compact index of a banded matrix: off[k] = j - i for the stored
@@ -537,7 +603,7 @@ struct CgBuffers {
   float2 *r2 = nullptr, *p2 = nullptr, *q2 = nullptr, *x2 = nullptr;  // pair mode
 };
 
-enum CgMode { CG_F32_SUMS = 0, CG_F64_SUMS = 1, CG_PAIR_SUMS = 2 };
+enum CgMode { CG_F32_SUMS = 0, CG_F64_SUMS = 1, CG_PAIR_SUMS = 2, CG_SPMV_PAIR = 3 };
 
 // The SpMV's own grid: at most `grid` blocks and no more than fit the SMs at
 // once (its two rows per thread take more registers than the updates).
@@ -581,6 +647,23 @@ static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int
       if (launch)
         cg_launch(cgp_spmv_dot<VT, PtrT, IX, int64_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
                   (const float2*)b.p2, b.q2, b.part_a);
+      return g;
+    }
+    if (mode == CG_SPMV_PAIR) {
+      const bool i32 = n + 2 * (int64_t)grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
+      if (i32) {
+        static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int32_t>, 1 << 30, 1);
+        const int g = std::max(1, std::min(grid, g0 * sms));
+        if (launch)
+          cg_launch(cgs_spmv_dot<VT, PtrT, IX, int32_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+                    (const double*)b.p, b.q, b.part_a);
+        return g;
+      }
+      static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int64_t>, 1 << 30, 1);
+      const int g = std::max(1, std::min(grid, g0 * sms));
+      if (launch)
+        cg_launch(cgs_spmv_dot<VT, PtrT, IX, int64_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+                  (const double*)b.p, b.q, b.part_a);
       return g;
     }
     if (mode == CG_F64_SUMS) {
@@ -650,9 +733,9 @@ extern "C" int fgb_cg_solve(fgb_ctx* ctx, const fgb_sparse* A64, const fgb_spars
   const int precision = opt->precision;
   if (precision != FGB_F64 && precision != FGB_F32 && precision != FGB_BF16)
     return set_error(FGB_EINVAL, "fgb_cg_solve: precision must be F64, F32 or BF16");
-  if (opt->accumulate < FGB_CG_SUM_F32 || opt->accumulate > FGB_CG_SUM_PAIR)
-    return set_error(FGB_EINVAL, "fgb_cg_solve: accumulate must be FGB_CG_SUM_F32, _F64 or _PAIR");
-  if (precision == FGB_F64 && opt->accumulate == FGB_CG_SUM_PAIR)
+  if (opt->accumulate < FGB_CG_SUM_F32 || opt->accumulate > FGB_CG_SUM_SPMV_PAIR)
+    return set_error(FGB_EINVAL, "fgb_cg_solve: accumulate must be FGB_CG_SUM_F32, _F64, _PAIR or _SPMV_PAIR");
+  if (precision == FGB_F64 && (opt->accumulate == FGB_CG_SUM_PAIR || opt->accumulate == FGB_CG_SUM_SPMV_PAIR))
     return set_error(FGB_EINVAL, "fgb_cg_solve: pair sums take FP32 or BF16 values");
   const fgb_sparse* Ait = A64;
   if (precision != FGB_F64) {

@@ -23,7 +23,7 @@ from . import _lib as L
 from . import device as dev
 
 PRECISIONS = {"f64": L.F64, "f32": L.F32, "bf16": L.BF16}
-ACCUMULATE = {"f32": 0, "f64": 1, "pair": 2}  # FGB_CG_SUM_F32, _F64, _PAIR
+ACCUMULATE = {"f32": 0, "f64": 1, "pair": 2, "spmv_pair": 3}  # FGB_CG_SUM_F32, _F64, _PAIR, _SPMV_PAIR
 
 
 @dataclass
@@ -49,8 +49,9 @@ def cg_solve(A64: dev.DeviceSparse, b: torch.Tensor, x: torch.Tensor | None = No
     """Solves A x = b (A SPD, CSR, FP64 values); returns (x, result).
     precision: the stored values of the iteration SpMV (f64, f32, bf16);
     accumulate: the arithmetic for f32/bf16 values: "f32" (FP32 SpMV sums),
-    "f64" (values widened, FP64 sums) or "pair" (pairs of FP32 numbers for the
-    SpMV sums, vectors, dots and updates)."""
+    "f64" (values widened, FP64 sums), "spmv_pair" (SpMV sums as pairs of FP32
+    numbers, vectors, dots and updates FP64) or "pair" (pairs of FP32 numbers
+    for the SpMV sums, vectors, dots and updates)."""
     if A64.orient != "csr":
         raise ValueError("cg_solve needs a CSR matrix")
     if x is None:

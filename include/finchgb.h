@@ -663,6 +663,9 @@ typedef struct fgb_cg_options {
 /* fgb_cg_options.accumulate (ignored for FP64 values, which sum in FP64) */
 #define FGB_CG_SUM_F32 0  /* SpMV: values times an FP32 copy of p, FP32 sums; vectors, dots, updates FP64 */
 #define FGB_CG_SUM_F64 1  /* SpMV: values widened to FP64, FP64 sums; vectors, dots, updates FP64 */
+#define FGB_CG_SUM_SPMV_PAIR 3 /* SpMV: values times p split into a pair of FP32 numbers (about 48 bits)
+                                * by integer operations, each row summed as a pair; vectors, dots and
+                                * updates FP64: no FP64 instruction per stored entry */
 #define FGB_CG_SUM_PAIR 2 /* SpMV sums, x, r, p, q, dots and updates in pairs of FP32 numbers
                            * (hi + lo, about 48 significant bits), no FP64 arithmetic per row or
                            * stored entry: the fast mode on GPUs whose FP64 rate is far below FP32.

@@ -86,23 +86,25 @@ def test_cg_fp64_accumulation_equals_fp64(gpu_lib, precision):
     assert rl.converged and true_residual(A, xl.cpu().numpy(), b) <= 1.2e-10
 
 
+@pytest.mark.parametrize("acc", ["pair", "spmv_pair"])
 @pytest.mark.parametrize("precision", ["f32", "bf16"])
 @pytest.mark.parametrize("N", [32, 96])
-def test_cg_pair_sums_reach_fp64_tolerance(gpu_lib, precision, N):
-    """Pair arithmetic (about 48 bits) for the SpMV sums, vectors, dots and
-    updates: the FP64 tolerance, and no more than a few percent more
-    iterations than FP64 CG, deterministically."""
+def test_cg_pair_sums_reach_fp64_tolerance(gpu_lib, precision, N, acc):
+    """Pair arithmetic (about 48 bits) for the SpMV sums (spmv_pair: FP64
+    vectors, dots and updates; pair: those too in pairs): the FP64
+    tolerance, and no more than a few percent more iterations than FP64
+    CG, deterministically."""
     A = poisson2d(N)
     b = np.random.default_rng(N + 1).uniform(-1, 1, A.nrows)
     Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
     bd = torch.from_numpy(b).cuda()
     _, r64 = cg.cg_solve(Ad, bd, precision="f64", rtol=1e-10, chunk=16, replace_every=64)
-    x, res = cg.cg_solve(Ad, bd, precision=precision, accumulate="pair", rtol=1e-10, chunk=16,
+    x, res = cg.cg_solve(Ad, bd, precision=precision, accumulate=acc, rtol=1e-10, chunk=16,
                          replace_every=64)
     assert res.converged and res.true_rel_residual <= 1e-10
     assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10
     assert res.iterations <= int(1.05 * r64.iterations) + 16
-    x2, res2 = cg.cg_solve(Ad, bd, precision=precision, accumulate="pair", rtol=1e-10, chunk=16,
+    x2, res2 = cg.cg_solve(Ad, bd, precision=precision, accumulate=acc, rtol=1e-10, chunk=16,
                            replace_every=64)
     assert torch.equal(x, x2) and res2.iterations == res.iterations
 
@@ -122,14 +124,16 @@ def test_cg_pair_sums_wide_matrix_and_warm_start(gpu_lib):
     b = rng.uniform(-1, 1, n)
     Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
     bd = torch.from_numpy(b).cuda()
-    x, res = cg.cg_solve(Ad, bd, precision="f32", accumulate="pair", rtol=1e-10, chunk=8)
-    assert res.converged and not res.compact_index
-    assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10
+    for acc in ("pair", "spmv_pair"):
+        x, res = cg.cg_solve(Ad, bd, precision="f32", accumulate=acc, rtol=1e-10, chunk=8)
+        assert res.converged and not res.compact_index
+        assert true_residual(A, x.cpu().numpy(), b) <= 1.2e-10
     x0 = x.clone()
     x3, r3 = cg.cg_solve(Ad, bd, x=x0, precision="bf16", accumulate="pair", chunk=8)
     assert r3.converged and r3.iterations == 0 and torch.equal(x3, x)
-    with pytest.raises(F.FinchGBError):  # FP64 values have no pair mode
-        cg.cg_solve(Ad, bd, precision="f64", accumulate="pair", chunk=8)
+    for acc in ("pair", "spmv_pair"):
+        with pytest.raises(F.FinchGBError):  # FP64 values have no pair mode
+            cg.cg_solve(Ad, bd, precision="f64", accumulate=acc, chunk=8)
 
 
 def test_cg_wide_matrix_keeps_the_int32_index(gpu_lib):
