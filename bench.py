@@ -1001,8 +1001,9 @@ def suite_cg() -> list[dict]:
 
 
 def suite_cg_probe() -> list[dict]:
-    """Two 16-iteration chunks of CG on the 2048^2 Poisson matrix in FP64 and
-    in BF16 pair mode: a short run of the iteration kernels (for ncu)."""
+    """Two 16-iteration chunks of CG on the 2048^2 Poisson matrix in FP64, in
+    BF16 pair mode and in BF16 SpMV-pair mode: a short run of the iteration
+    kernels (for ncu)."""
     import torch
 
     from finchgb import cg
@@ -1014,7 +1015,7 @@ def suite_cg_probe() -> list[dict]:
     Ad = dev.DeviceSparse.from_host(A.nrows, A.ncols, A.ptr, A.idx, A.val, orient="csr")
     bd = torch.from_numpy(b).cuda()
     out = []
-    for prec, acc in (("f64", "f64"), ("bf16", "pair")):
+    for prec, acc in (("f64", "f64"), ("bf16", "pair"), ("bf16", "spmv_pair")):
         _, res = cg.cg_solve(Ad, bd, precision=prec, accumulate=acc, rtol=1e-10, max_iter=32, chunk=16)
         torch.cuda.synchronize()
         out.append({"suite": "cg_probe", "variant": f"{prec}_{acc}", "iterations": res.iterations,
