@@ -239,7 +239,7 @@ class Tensor:
                 return out
             if self.data is not None:
                 return self.data
-            return self.ddata.cpu().numpy()  # read back each time: kernels may have updated it
+            return read_back(self.ddata)  # read back each time: kernels may have updated it
         if self.kind == "coo":
             out = np.full(self.shape, self.fill_value, dtype=self.dtype)
             I, J, V = self.coo
@@ -444,6 +444,26 @@ class GPU:
 
 def gpu(index: int = 0) -> GPU:
     return GPU(index)
+
+
+# Read-backs of at least this many bytes go through page-locked memory.
+_PINNED_READBACK = 1 << 20
+
+
+def read_back(d):
+    """A device array as a numpy array.  A large one is copied into
+    page-locked memory from torch's caching host allocator (the copy engine
+    writes it at link speed; a fresh pageable array is filled several times
+    slower) and returned as a view of it, so later read-backs of the same
+    size reuse the pinned block."""
+    import torch
+
+    if d.numel() * d.element_size() < _PINNED_READBACK:
+        return d.cpu().numpy()
+    h = torch.empty(d.shape, dtype=d.dtype, pin_memory=True)
+    h.copy_(d, non_blocking=True)
+    torch.cuda.current_stream(d.device).synchronize()
+    return h.numpy()
 
 
 def transfer(device, t):
