@@ -1279,7 +1279,8 @@ def served_block(min_seconds: float = 1.0) -> dict:
     batched server and of the plain per-call path (at least min_seconds of
     requests each), then Poisson arrivals at the same rates for both modes
     (half and nine tenths of the per-call capacity) and at half the batched
-    capacity for the batched mode, p50/p99 of each; clocks sampled; a sample
+    capacity for the batched mode, p50/p99 of the median of three runs;
+    clocks sampled; a sample
     of served results against the FP64 oracle.  Every server uses the SpMV
     shapes the serving autotuner picked for the library's size classes."""
     import torch
@@ -1319,9 +1320,17 @@ def served_block(min_seconds: float = 1.0) -> dict:
             plan = _serve_plan(rng, n_req, mats, partners)
             arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
             for mode in modes:
-                dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr, tuning=tuning)
+                # three runs of the same arrivals; the run with the median p99 is
+                # reported, every run's p99 beside it
+                runs = []
+                for _ in range(3):
+                    dt, lat, st = serve_run(mode, mats, partners, plan, arena, window, arrivals=arr, tuning=tuning)
+                    runs.append((float(np.percentile(lat, 99)), dt, lat))
+                runs.sort(key=lambda r: r[0])
+                _, dt, lat = runs[1]
                 out[mode][f"poisson_{name}"] = {"rate_per_s": round(lam, 1), "requests": n_req,
-                                                "seconds": round(dt, 3), **lat_stats(lat)}
+                                                "seconds": round(dt, 3), **lat_stats(lat),
+                                                "p99_ms_of_3_runs": [round(1e3 * r[0], 3) for r in runs]}
     out["clocks"] = clk.summary()
     out["oracle_check"] = serve_check(mats, partners, tuning=tuning)
     return out
