@@ -53,6 +53,9 @@ constexpr int CG_ILP = 4;  // elements per thread in flight in the streaming upd
 // elements in flight (up to 64 registers): few partials, one load per thread
 // in each block's fold of the previous kernel's partials.
 constexpr int CG_UPD_THREADS = 1024;
+// Rows in flight per thread in the pair SpMVs (32-bit index build): 4
+// measured slower than 2 (BF16 pair CG 0.694 against 0.637 s).
+constexpr int CG_PAIR_ROWS = 2;
 
 // The iteration kernels are chained by programmatic dependent launch: each
 // lets the next one launch as soon as it starts, and waits for the previous
@@ -217,7 +220,7 @@ __device__ __forceinline__ void ff_row_term(float& h, float& l, float a, float2 
 // the partial leaves the block as one FP64 number.  IT: the row, entry and
 // column arithmetic (int32 when rows and entries stay below 2^31, which
 // halves the integer instructions per entry).
-template <class VT, class PtrT, class IX, class IT>
+template <class VT, class PtrT, class IX, class IT, int R>
 __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
     int64_t n64, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const float2* __restrict__ p, float2* __restrict__ q, double* __restrict__ part) {
@@ -230,23 +233,40 @@ __global__ void __launch_bounds__(CG_THREADS) cgp_spmv_dot(
     if constexpr (sizeof(IX) == 2) return row + (IT)__ldg(idx + k);
     else return (IT)__ldg(idx + k) - (IT)base;
   };
-  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += 2 * stride) {
-    const IT i2 = i + stride;
-    const bool two = i2 < n;
-    const IT a0 = (IT)(ld_ptr(ptr, i) - base), a1 = (IT)(ld_ptr(ptr, i + 1) - base);
-    const IT b0 = two ? (IT)(ld_ptr(ptr, i2) - base) : 0, b1 = two ? (IT)(ld_ptr(ptr, i2 + 1) - base) : 0;
-    float ha = 0.f, la_ = 0.f, hb = 0.f, lb_ = 0.f;
-    const IT la = a1 - a0, lb = b1 - b0, lmax = la > lb ? la : lb;
-    for (IT t = 0; t < lmax; ++t) {
-      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), __ldg(p + col(a0 + t, i)));
-      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), __ldg(p + col(b0 + t, i2)));
+  // R rows (i, i + stride, ...) per thread in flight; the rows, and each
+  // row's products, in the plain loop's order, so q and the partial do not
+  // depend on R
+  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += R * stride) {
+    IT s0[R], len[R];
+    IT lmax = 0;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const IT row = i + (IT)u * stride;
+      s0[u] = 0;
+      len[u] = 0;
+      if (row < n) {
+        s0[u] = (IT)(ld_ptr(ptr, row) - base);
+        len[u] = (IT)(ld_ptr(ptr, row + 1) - base) - s0[u];
+      }
+      lmax = len[u] > lmax ? len[u] : lmax;
     }
-    const float2 acc_a = two_sum(ha, la_), acc_b = two_sum(hb, lb_);  // l may exceed h after cancellation
-    q[i] = acc_a;
-    dot = ff_add(dot, ff_mul(__ldg(p + i), acc_a));
-    if (two) {
-      q[i2] = acc_b;
-      dot = ff_add(dot, ff_mul(__ldg(p + i2), acc_b));
+    float h[R], l[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) h[u] = l[u] = 0.f;
+    for (IT t = 0; t < lmax; ++t) {
+#pragma unroll
+      for (int u = 0; u < R; ++u)
+        if (t < len[u])
+          ff_row_term(h[u], l[u], cg_val(val, s0[u] + t), __ldg(p + col(s0[u] + t, i + (IT)u * stride)));
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const IT row = i + (IT)u * stride;
+      if (row < n) {
+        const float2 acc = two_sum(h[u], l[u]);  // l may exceed h after cancellation
+        q[row] = acc;
+        dot = ff_add(dot, ff_mul(__ldg(p + row), acc));
+      }
     }
   }
   dot = ff_block_sum(dot, sh);
@@ -279,7 +299,7 @@ __device__ __forceinline__ float2 split_f64(double v) {
 // The SpMV of the pair-sum SpMV mode: FP64 p split into pairs as it is
 // gathered, each row summed as a pair (ff_row_term), q and the p.q partial
 // in FP64 -- the vectors, dots and updates stay FP64.
-template <class VT, class PtrT, class IX, class IT>
+template <class VT, class PtrT, class IX, class IT, int R>
 __global__ void __launch_bounds__(CG_THREADS) cgs_spmv_dot(
     int64_t n64, const PtrT* __restrict__ ptr, const IX* __restrict__ idx, const VT* __restrict__ val,
     int base, const double* __restrict__ p, double* __restrict__ q, double* __restrict__ part) {
@@ -292,24 +312,37 @@ __global__ void __launch_bounds__(CG_THREADS) cgs_spmv_dot(
     if constexpr (sizeof(IX) == 2) return row + (IT)__ldg(idx + k);
     else return (IT)__ldg(idx + k) - (IT)base;
   };
-  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += 2 * stride) {
-    const IT i2 = i + stride;
-    const bool two = i2 < n;
-    const IT a0 = (IT)(ld_ptr(ptr, i) - base), a1 = (IT)(ld_ptr(ptr, i + 1) - base);
-    const IT b0 = two ? (IT)(ld_ptr(ptr, i2) - base) : 0, b1 = two ? (IT)(ld_ptr(ptr, i2 + 1) - base) : 0;
-    float ha = 0.f, la_ = 0.f, hb = 0.f, lb_ = 0.f;
-    const IT la = a1 - a0, lb = b1 - b0, lmax = la > lb ? la : lb;
-    for (IT t = 0; t < lmax; ++t) {
-      if (t < la) ff_row_term(ha, la_, cg_val(val, a0 + t), split_f64(__ldg(p + col(a0 + t, i))));
-      if (t < lb) ff_row_term(hb, lb_, cg_val(val, b0 + t), split_f64(__ldg(p + col(b0 + t, i2))));
+  for (IT i = (IT)blockIdx.x * (IT)blockDim.x + (IT)threadIdx.x; i < n; i += R * stride) {
+    IT s0[R], len[R];
+    IT lmax = 0;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const IT row = i + (IT)u * stride;
+      s0[u] = 0;
+      len[u] = 0;
+      if (row < n) {
+        s0[u] = (IT)(ld_ptr(ptr, row) - base);
+        len[u] = (IT)(ld_ptr(ptr, row + 1) - base) - s0[u];
+      }
+      lmax = len[u] > lmax ? len[u] : lmax;
     }
-    const double qa = ff_to_double(two_sum(ha, la_));
-    q[i] = qa;
-    dot = __fma_rn(__ldg(p + i), qa, dot);
-    if (two) {
-      const double qb = ff_to_double(two_sum(hb, lb_));
-      q[i2] = qb;
-      dot = __fma_rn(__ldg(p + i2), qb, dot);
+    float h[R], l[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) h[u] = l[u] = 0.f;
+    for (IT t = 0; t < lmax; ++t) {
+#pragma unroll
+      for (int u = 0; u < R; ++u)
+        if (t < len[u])
+          ff_row_term(h[u], l[u], cg_val(val, s0[u] + t), split_f64(__ldg(p + col(s0[u] + t, i + (IT)u * stride))));
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const IT row = i + (IT)u * stride;
+      if (row < n) {
+        const double qv = ff_to_double(two_sum(h[u], l[u]));
+        q[row] = qv;
+        dot = __fma_rn(__ldg(p + row), qv, dot);
+      }
     }
   }
   dot = cg_block_sum(dot, sh);
@@ -633,36 +666,36 @@ static int spmv_dot_t(const fgb_sparse* A, const IX* ix, int mode, int grid, int
     if (mode == CG_PAIR_SUMS) {
       // 32-bit index arithmetic while rows (two per thread, a grid-stride
       // apart) and entries stay below 2^31
-      const bool i32 = n + 2 * (int64_t)grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
+      const bool i32 = n + (int64_t)CG_PAIR_ROWS * grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
       if (i32) {
-        static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int32_t>, 1 << 30, 1);
+        static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int32_t, CG_PAIR_ROWS>, 1 << 30, 1);
         const int g = std::max(1, std::min(grid, g0 * sms));
         if (launch)
-          cg_launch(cgp_spmv_dot<VT, PtrT, IX, int32_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+          cg_launch(cgp_spmv_dot<VT, PtrT, IX, int32_t, CG_PAIR_ROWS>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
                     (const float2*)b.p2, b.q2, b.part_a);
         return g;
       }
-      static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int64_t>, 1 << 30, 1);
+      static const int g0 = occupancy_grid(cgp_spmv_dot<VT, PtrT, IX, int64_t, 2>, 1 << 30, 1);
       const int g = std::max(1, std::min(grid, g0 * sms));
       if (launch)
-        cg_launch(cgp_spmv_dot<VT, PtrT, IX, int64_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+        cg_launch(cgp_spmv_dot<VT, PtrT, IX, int64_t, 2>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
                   (const float2*)b.p2, b.q2, b.part_a);
       return g;
     }
     if (mode == CG_SPMV_PAIR) {
-      const bool i32 = n + 2 * (int64_t)grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
+      const bool i32 = n + (int64_t)CG_PAIR_ROWS * grid * CG_THREADS < INT32_MAX && A->nnz < INT32_MAX;
       if (i32) {
-        static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int32_t>, 1 << 30, 1);
+        static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int32_t, CG_PAIR_ROWS>, 1 << 30, 1);
         const int g = std::max(1, std::min(grid, g0 * sms));
         if (launch)
-          cg_launch(cgs_spmv_dot<VT, PtrT, IX, int32_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+          cg_launch(cgs_spmv_dot<VT, PtrT, IX, int32_t, CG_PAIR_ROWS>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
                     (const double*)b.p, b.q, b.part_a);
         return g;
       }
-      static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int64_t>, 1 << 30, 1);
+      static const int g0 = occupancy_grid(cgs_spmv_dot<VT, PtrT, IX, int64_t, 2>, 1 << 30, 1);
       const int g = std::max(1, std::min(grid, g0 * sms));
       if (launch)
-        cg_launch(cgs_spmv_dot<VT, PtrT, IX, int64_t>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
+        cg_launch(cgs_spmv_dot<VT, PtrT, IX, int64_t, 2>, g, CG_THREADS, s, pdl, n, ptr, ix, val, base,
                   (const double*)b.p, b.q, b.part_a);
       return g;
     }
