@@ -4,7 +4,7 @@ ctypes wrapper around finch_oracle.c, a CPU restatement of the loop nests
 Finch.jl v1.2.12 generates for SpMV (CSC serial and CSR row-parallel), SpMM,
 SDDMM, two-finger elementwise merges and elementwise+reduce.  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may use it, and only
-as the checker.  The GPU library never calls it.
+to check or time against.  The GPU library never calls it.
 
 Sparse operands are passed in Finch's own layout: 1-based Int64 ptr/idx of a
 SparseList level and the Element values (numpy arrays).  bf16 values are

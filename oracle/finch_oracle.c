@@ -2,7 +2,7 @@
  * finch_oracle.c -- TEST INFRASTRUCTURE ONLY.  A CPU restatement, in plain
  * C, of the loop nests Finch.jl v1.2.12 generates for the sparse kernels the
  * GPU library replaces.  The tests, smoke() and the CPU-baseline leg of the
- * benchmark call it as the checker; the library never does.
+ * benchmark call it to check or time against; the library never does.
  *
  * All sparse inputs are Finch level buffers: 1-based Int64 ptr/idx of a
  * SparseList level (src/tensors/levels/sparse_list_levels.jl:37-53) and the
