@@ -110,23 +110,31 @@ class DeviceSparse:
     def from_host(cls, nrows: int, ncols: int, ptr, idx, val, orient: str = "csc", base: int = 1,
                   device: int | None = None, val_dtype: torch.dtype | None = None,
                   pinned: bool = False) -> "DeviceSparse":
-        """Uploads Finch level buffers (ptr/idx Int64 with `base`) to HBM."""
+        """Uploads level buffers (ptr/idx counted from `base`) to HBM: Finch's
+        Int64 buffers are narrowed to int32 on the device; int32 buffers
+        (scipy.sparse's usual width) are uploaded as they are."""
         ctx = context(device)
         dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-        ptr = np.ascontiguousarray(ptr, dtype=np.int64)
-        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        ptr, idx = np.asarray(ptr), np.asarray(idx)
         nnz = idx.size
         s = stream_ptr()
-        d_idx = torch.empty(nnz, dtype=torch.int32, device=dev)
-        if nnz:
-            tmp = torch.from_numpy(idx).to(dev, non_blocking=pinned)
-            L.call("fgb_narrow_index", ctx, tmp.data_ptr(), d_idx.data_ptr(), nnz, 0, s)
-        if nnz + base < 2**31 - 1:
+        if idx.dtype == np.int32:
+            d_idx = torch.from_numpy(np.ascontiguousarray(idx)).to(dev)
+        else:
+            idx = np.ascontiguousarray(idx, dtype=np.int64)
+            d_idx = torch.empty(nnz, dtype=torch.int32, device=dev)
+            if nnz:
+                tmp = torch.from_numpy(idx).to(dev, non_blocking=pinned)
+                L.call("fgb_narrow_index", ctx, tmp.data_ptr(), d_idx.data_ptr(), nnz, 0, s)
+        if ptr.dtype == np.int32:
+            d_ptr = torch.from_numpy(np.ascontiguousarray(ptr)).to(dev)
+        elif nnz + base < 2**31 - 1:
+            ptr = np.ascontiguousarray(ptr, dtype=np.int64)
             d_ptr = torch.empty(ptr.size, dtype=torch.int32, device=dev)
             tmp = torch.from_numpy(ptr).to(dev)
             L.call("fgb_narrow_index", ctx, tmp.data_ptr(), d_ptr.data_ptr(), ptr.size, 0, s)
         else:
-            d_ptr = torch.from_numpy(ptr).to(dev)
+            d_ptr = torch.from_numpy(np.ascontiguousarray(ptr, dtype=np.int64)).to(dev)
         d_val = None
         if val is not None:
             v = torch.as_tensor(np.ascontiguousarray(val))

@@ -100,7 +100,7 @@ def _findnz(t):
     else:
         b = t.host_buffers()
         f = np.repeat(np.arange(b.nfibers), np.diff(b.ptr))
-        inner = b.idx - 1
+        inner = np.asarray(b.idx, dtype=np.int64) - b.base
         I, J = (inner, f) if b.orient == "csc" else (f, inner)
         V = np.ones(b.nnz, dtype=np.bool_) if b.val is None else np.asarray(b.val)
         order = np.lexsort((I, J))
@@ -205,8 +205,8 @@ def _bsp_write(name: str, t) -> None:
         b = body.host_buffers()
         desc["format"] = "CSR" if swz else "CSC"
         desc["shape"] = list(map(int, t.shape if swz else body.shape))
-        arrays["pointers_to_1"] = np.asarray(b.ptr, dtype=np.int64) - 1
-        arrays["indices_1"] = np.asarray(b.idx, dtype=np.int64) - 1
+        arrays["pointers_to_1"] = np.asarray(b.ptr, dtype=np.int64) - b.base
+        arrays["indices_1"] = np.asarray(b.idx, dtype=np.int64) - b.base
         if b.val is not None:
             arrays["values"] = np.asarray(b.val)
     elif body.kind == "coo":

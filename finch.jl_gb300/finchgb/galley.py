@@ -120,7 +120,8 @@ def _body_degrees(body) -> tuple:
     if body.buf is not None:
         b = body.buf
         col = float(np.diff(b.ptr).max(initial=0))
-        row = float(np.bincount(np.asarray(b.idx) - 1, minlength=b.nrows).max(initial=0)) if b.nnz else 0.0
+        row = (float(np.bincount(np.asarray(b.idx, dtype=np.int64) - b.base, minlength=b.nrows).max(initial=0))
+               if b.nnz else 0.0)
         return (row, col) if b.orient == "csc" else (col, row)
     d = body.dsparse  # resident only: the fiber lengths are exact, the other side uniform
     ptr = d.ptr.cpu().numpy()

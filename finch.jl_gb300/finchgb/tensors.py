@@ -12,8 +12,11 @@ Mirrors the constructors of Finch.jl's levels and Tensor wrapper:
 (src/tensors/levels/{dense,sparse_list,sparse_coo,element,pattern}_levels.jl,
 src/tensors/tensors.jl:10-69, src/tensors/combinators/swizzle.jl:1-58,
 src/Finch.jl:188-258).  Host buffers use Finch's layout (1-based Int64
-ptr/idx).  `transfer(gpu(), t)` moves the level buffers into HBM once
-(narrowing idx to int32); tensors then stay resident across calls.
+ptr/idx).  `Tensor(A)` of a scipy.sparse matrix keeps A's own 0-based
+buffers, as Finch's Tensor(::SparseMatrixCSC) does, and `sparse(t)` gives
+a scipy.sparse matrix back (ext/SparseArraysExt.jl).  `transfer(gpu(), t)`
+moves the level buffers into HBM once (narrowing Int64 idx to int32);
+tensors then stay resident across calls.
 """
 from __future__ import annotations
 
@@ -152,6 +155,9 @@ class Tensor:
     """
 
     def __init__(self, fmt, arr=None, shape=None, _buf=None):
+        sp_in = _scipy_sparse(fmt) if arr is None and _buf is None else None
+        if sp_in is not None:  # Tensor(A): the scipy.sparse matrix's own buffers
+            fmt, _buf = _map_scipy(sp_in)
         self.fmt = fmt
         self.kind = _kind(fmt)
         self.fill_value = fmt.fill_value
@@ -180,6 +186,10 @@ class Tensor:
             assert arr.ndim == 1 and self.kind == "dense1", "tuple elements: Dense(Element((a, b))) vectors"
             self.shape = tuple(arr.shape)
             self.data = np.ascontiguousarray(arr)
+            return
+        sp_in = _scipy_sparse(arr)
+        if sp_in is not None and self.kind in ("csc", "coo") and not np.any(np.asarray(self.fill_value)):
+            self._from_scipy(sp_in)
             return
         arr = _as_array(arr, self.dtype)
         self.shape = tuple(arr.shape)
@@ -213,6 +223,30 @@ class Tensor:
             I, J = np.nonzero(arr != fill)
             order = np.lexsort((I, J))  # Finch sorts by reverse coordinates (column-major)
             self.coo = (I[order] + 1, J[order] + 1, arr[I[order], J[order]])
+
+    def _from_scipy(self, A):
+        """Tensor(fmt, A) for a scipy.sparse A and a zero fill: Finch's
+        dropfills! copy (src/interface/copy.jl:77-113) without a dense
+        intermediate.  Stored zeros are dropped, duplicates summed and
+        coordinates sorted; a canonical CSC A in the format's value type
+        keeps its own arrays (0-based, `base` 0)."""
+        if A.ndim != 2:
+            raise ValueError("Tensor from scipy.sparse: 2-D matrices only")
+        self.shape = tuple(map(int, A.shape))
+        if self.kind == "coo":
+            C = A.tocoo(copy=True)
+            C.sum_duplicates()
+            keep = C.data != 0
+            I, J, V = C.row[keep].astype(np.int64), C.col[keep].astype(np.int64), C.data[keep]
+            order = np.lexsort((I, J))  # Finch sorts by reverse coordinates (column-major)
+            self.coo = (I[order] + 1, J[order] + 1, V[order].astype(self.dtype))
+            return
+        C = _canonical_csc(A)
+        if not np.all(C.data):
+            C = C.copy()
+            C.eliminate_zeros()
+        val = None if isinstance(self.fmt.lvl.lvl, Pattern) else C.data.astype(self.dtype, copy=False)
+        self.buf = SparseBuffers(self.shape[0], self.shape[1], C.indptr, C.indices, val, "csc", base=0)
 
     # -- constructors from level buffers (zero-copy on the host)
     @classmethod
@@ -314,11 +348,73 @@ class Tensor:
 def _stored_mask(buf: SparseBuffers) -> np.ndarray:
     mask = np.zeros((buf.nrows, buf.ncols), dtype=bool)
     f = np.repeat(np.arange(buf.nfibers), np.diff(buf.ptr))
+    c = np.asarray(buf.idx, dtype=np.int64) - buf.base
     if buf.orient == "csc":
-        mask[buf.idx - 1, f] = True
+        mask[c, f] = True
     else:
-        mask[f, buf.idx - 1] = True
+        mask[f, c] = True
     return mask
+
+
+def _scipy_sparse(x):
+    """x when it is a scipy.sparse matrix or array, else None."""
+    try:
+        import scipy.sparse as sp
+    except ImportError:
+        return None
+    return x if sp.issparse(x) else None
+
+
+def _canonical_csc(A):
+    """A in CSC with sorted, distinct coordinates in every column (Julia's
+    SparseMatrixCSC invariant); a canonical CSC A is returned as it is."""
+    C = A.tocsc()
+    if not C.has_canonical_format:
+        C = C.copy()
+        C.sum_duplicates()
+    return C
+
+
+def _map_scipy(A):
+    """Finch's Tensor(::SparseMatrixCSC) (ext/SparseArraysExt.jl:17-22) for
+    scipy.sparse: Dense(SparseList(Element(zero(T)))) over A's own indptr,
+    indices and data (0-based, `base` 0), stored zeros kept.  A matrix that
+    is not canonical CSC is converted first."""
+    if A.ndim != 2:
+        raise ValueError("Tensor from scipy.sparse: 2-D matrices only")
+    C = _canonical_csc(A)
+    fmt = Dense(SparseList(Element(C.data.dtype.type(0)), index_type=C.indices.dtype.type))
+    return fmt, SparseBuffers(int(C.shape[0]), int(C.shape[1]), C.indptr, C.indices, C.data, "csc", base=0)
+
+
+def sparse(t):
+    """The scipy.sparse matrix of a 2-D tensor or swizzle, Finch's
+    sparse(::Tensor) (ext/SparseArraysExt.jl:61-76).  Only a zero fill value
+    can be represented.  A Dense(SparseList) tensor's host buffers are
+    reused where their layout allows (0-based ones are); a swizzled CSC comes
+    back as the CSR view of its transpose."""
+    import scipy.sparse as sp
+
+    body = t.body if isinstance(t, SwizzleArray) else t
+    if t.ndim != 2:
+        raise ValueError(f"sparse: scipy.sparse holds matrices, got a {t.ndim}-d tensor")
+    if np.any(np.asarray(t.fill_value)):
+        raise ValueError(f"sparse: scipy.sparse only supports zero fill values, was given {t.fill_value!r}")
+    if body.kind == "csc":
+        b = body.host_buffers()
+        ptr, idx = b.ptr, b.idx
+        if b.base:
+            ptr, idx = np.asarray(ptr) - b.base, np.asarray(idx) - b.base
+        val = np.ones(b.nnz, dtype=np.bool_) if b.val is None else b.val
+        M = sp.csc_matrix((val, idx, ptr), shape=(b.nrows, b.ncols)) if b.orient == "csc" else \
+            sp.csr_matrix((val, idx, ptr), shape=(b.nrows, b.ncols))
+    else:
+        M = sp.csc_matrix(body.todense())
+    if isinstance(t, SwizzleArray):
+        if t.dims != (2, 1):
+            raise ValueError(f"sparse: swizzle {t.dims}")
+        M = M.T
+    return M
 
 
 def _as_array(arr, dtype) -> np.ndarray:
@@ -506,7 +602,7 @@ def transfer(device, t):
     b = t.buf
     val = b.val
     t.dsparse = dev.DeviceSparse.from_host(b.nrows, b.ncols, b.ptr, b.idx, val, orient=b.orient,
-                                           base=1, device=idx)
+                                           base=b.base, device=idx)
     return t
 
 
@@ -523,7 +619,7 @@ def pattern(t):
     out.fill_value, out.dtype = False, np.dtype(np.bool_)
     if t.buf is not None:
         b = t.buf
-        out.buf = SparseBuffers(b.nrows, b.ncols, b.ptr, b.idx, None, b.orient)
+        out.buf = SparseBuffers(b.nrows, b.ncols, b.ptr, b.idx, None, b.orient, b.base)
     if t.dsparse is not None:
         d = t.dsparse
         out.dsparse = type(d)(d.nrows, d.ncols, d.ptr, d.idx, None, d.orient, d.base)

@@ -15,14 +15,19 @@ import numpy as np
 
 @dataclass
 class SparseBuffers:
-    """Host level buffers of a 2-D SparseList matrix (Finch layout)."""
+    """Host level buffers of a 2-D SparseList matrix (Finch layout).
+
+    Finch's own buffers are 1-based Int64 (`base` 1).  Buffers mapped from
+    scipy.sparse keep its 0-based int32/int64 arrays (`base` 0), as Finch
+    reads 0-based buffers through PlusOneVector (src/util/vectors.jl:3-37)."""
 
     nrows: int
     ncols: int
-    ptr: np.ndarray  # int64, 1-based, nfibers + 1
-    idx: np.ndarray  # int64, 1-based
+    ptr: np.ndarray  # nfibers + 1 offsets, ptr[0] == base
+    idx: np.ndarray  # coordinates counted from base
     val: np.ndarray | None
     orient: str  # "csc" (fibers = columns) or "csr" (fibers = rows)
+    base: int = 1
 
     @property
     def nnz(self) -> int:
@@ -36,7 +41,7 @@ class SparseBuffers:
         dt = np.float64 if self.val is None else self.val.dtype
         out = np.zeros((self.nrows, self.ncols), dtype=dt)
         f = np.repeat(np.arange(self.nfibers), np.diff(self.ptr))
-        c = self.idx - 1
+        c = np.asarray(self.idx, dtype=np.int64) - self.base
         v = 1 if self.val is None else self.val
         if self.orient == "csc":
             out[c, f] = v
