@@ -179,7 +179,15 @@ class Tensor:
                 arr[...] = tuple(self.fill_value)
             else:
                 arr = np.full(shape, self.fill_value, dtype=self.dtype)
-        if isinstance(arr, Tensor):
+        if isinstance(arr, (Tensor, SwizzleArray)):
+            # a sparse source with the same fill: its stored entries only
+            # (dropfills!, src/interface/copy.jl:77-113), no dense intermediate
+            if (self.kind in ("csc", "coo") and arr.kind == "csc" and not self.dtype.names
+                    and _same_fill(arr.fill_value, self.fill_value)):
+                M = _stored_scipy(arr)
+                if M is not None:
+                    self._from_scipy(M)
+                    return
             arr = arr.todense()
         if self.dtype.names:  # tuple elements: a record array
             arr = np.asarray(arr, dtype=self.dtype)
@@ -225,28 +233,34 @@ class Tensor:
             self.coo = (I[order] + 1, J[order] + 1, arr[I[order], J[order]])
 
     def _from_scipy(self, A):
-        """Tensor(fmt, A) for a scipy.sparse A and a zero fill: Finch's
-        dropfills! copy (src/interface/copy.jl:77-113) without a dense
-        intermediate.  Stored zeros are dropped, duplicates summed and
-        coordinates sorted; a canonical CSC A in the format's value type
-        keeps its own arrays (0-based, `base` 0)."""
+        """Tensor(fmt, A) for a scipy.sparse A whose implicit entries equal
+        the format's fill: Finch's dropfills! copy (src/interface/copy.jl:
+        77-113) without a dense intermediate.  Stored entries equal to the
+        fill are dropped, duplicates summed and coordinates sorted; a
+        canonical CSC A in the format's value type keeps its own arrays
+        (0-based, `base` 0)."""
         if A.ndim != 2:
             raise ValueError("Tensor from scipy.sparse: 2-D matrices only")
         self.shape = tuple(map(int, A.shape))
         if self.kind == "coo":
             C = A.tocoo(copy=True)
             C.sum_duplicates()
-            keep = C.data != 0
+            keep = ~_isfill(C.data, self.fill_value)
             I, J, V = C.row[keep].astype(np.int64), C.col[keep].astype(np.int64), C.data[keep]
             order = np.lexsort((I, J))  # Finch sorts by reverse coordinates (column-major)
             self.coo = (I[order] + 1, J[order] + 1, V[order].astype(self.dtype))
             return
         C = _canonical_csc(A)
-        if not np.all(C.data):
-            C = C.copy()
-            C.eliminate_zeros()
-        val = None if isinstance(self.fmt.lvl.lvl, Pattern) else C.data.astype(self.dtype, copy=False)
-        self.buf = SparseBuffers(self.shape[0], self.shape[1], C.indptr, C.indices, val, "csc", base=0)
+        ptr, idx, data = C.indptr, C.indices, C.data
+        drop = _isfill(data, self.fill_value)
+        if drop.any():
+            keep = ~drop
+            fib = np.repeat(np.arange(self.shape[1]), np.diff(ptr))
+            ptr = np.zeros(self.shape[1] + 1, dtype=ptr.dtype)
+            np.cumsum(np.bincount(fib[keep], minlength=self.shape[1]), out=ptr[1:])
+            idx, data = idx[keep], data[keep]
+        val = None if isinstance(self.fmt.lvl.lvl, Pattern) else data.astype(self.dtype, copy=False)
+        self.buf = SparseBuffers(self.shape[0], self.shape[1], ptr, idx, val, "csc", base=0)
 
     # -- constructors from level buffers (zero-copy on the host)
     @classmethod
@@ -365,6 +379,43 @@ def _scipy_sparse(x):
     return x if sp.issparse(x) else None
 
 
+def _isfill(data: np.ndarray, fill) -> np.ndarray:
+    """Entries equal to the fill value (NaN equals NaN, as in isequal)."""
+    f = np.asarray(fill)
+    if f.dtype.kind in "fc" and np.isnan(f):
+        return np.isnan(data)
+    return data == f
+
+
+def _same_fill(a, b) -> bool:
+    if isinstance(a, tuple) or isinstance(b, tuple):
+        return False
+    a, b = np.asarray(a), np.asarray(b)
+    return bool(a == b) or bool(a.dtype.kind in "fc" and b.dtype.kind in "fc" and np.isnan(a) and np.isnan(b))
+
+
+def _stored_scipy(t):
+    """The stored entries of a Dense(SparseList) tensor or swizzle as a
+    scipy.sparse matrix of its logical shape (a pattern's entries true);
+    the host buffers are shared where they are 0-based.  None without
+    scipy."""
+    try:
+        import scipy.sparse as sp
+    except ImportError:
+        return None
+    body = t.body if isinstance(t, SwizzleArray) else t
+    if isinstance(t, SwizzleArray) and t.dims != (2, 1):
+        raise ValueError(f"swizzle {t.dims}")
+    b = body.host_buffers()
+    ptr, idx = b.ptr, b.idx
+    if b.base:
+        ptr, idx = np.asarray(ptr) - b.base, np.asarray(idx) - b.base
+    val = np.ones(b.nnz, dtype=np.bool_) if b.val is None else b.val
+    make = sp.csc_matrix if b.orient == "csc" else sp.csr_matrix
+    M = make((val, idx, ptr), shape=(b.nrows, b.ncols))
+    return M.T if isinstance(t, SwizzleArray) else M
+
+
 def _canonical_csc(A):
     """A in CSC with sorted, distinct coordinates in every column (Julia's
     SparseMatrixCSC invariant); a canonical CSC A is returned as it is."""
@@ -395,26 +446,13 @@ def sparse(t):
     back as the CSR view of its transpose."""
     import scipy.sparse as sp
 
-    body = t.body if isinstance(t, SwizzleArray) else t
     if t.ndim != 2:
         raise ValueError(f"sparse: scipy.sparse holds matrices, got a {t.ndim}-d tensor")
     if np.any(np.asarray(t.fill_value)):
         raise ValueError(f"sparse: scipy.sparse only supports zero fill values, was given {t.fill_value!r}")
-    if body.kind == "csc":
-        b = body.host_buffers()
-        ptr, idx = b.ptr, b.idx
-        if b.base:
-            ptr, idx = np.asarray(ptr) - b.base, np.asarray(idx) - b.base
-        val = np.ones(b.nnz, dtype=np.bool_) if b.val is None else b.val
-        M = sp.csc_matrix((val, idx, ptr), shape=(b.nrows, b.ncols)) if b.orient == "csc" else \
-            sp.csr_matrix((val, idx, ptr), shape=(b.nrows, b.ncols))
-    else:
-        M = sp.csc_matrix(body.todense())
-    if isinstance(t, SwizzleArray):
-        if t.dims != (2, 1):
-            raise ValueError(f"sparse: swizzle {t.dims}")
-        M = M.T
-    return M
+    if t.kind == "csc":
+        return _stored_scipy(t)
+    return sp.csc_matrix(t.todense())
 
 
 def _as_array(arr, dtype) -> np.ndarray:
@@ -472,7 +510,8 @@ def swizzle(t, *dims) -> SwizzleArray:
 
 def csr(A, fill_value=0.0, dtype=None) -> SwizzleArray:
     """Finch's CSR of a matrix: swizzle(Tensor(Dense(SparseList(Element)), A^T), 2, 1)."""
-    A = np.asarray(A) if not hasattr(A, "toarray") else A.toarray()
+    if _scipy_sparse(A) is None:
+        A = np.asarray(A)
     el = Element(fill_value, dtype or A.dtype)
     return swizzle(Tensor(Dense(SparseList(el)), A.T), 2, 1)
 

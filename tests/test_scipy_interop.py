@@ -150,3 +150,60 @@ def test_galley_degrees_read_zero_based_buffers():
 def test_finch_buffers_keep_base_one():
     r = csr_from_dense(np.eye(4))
     assert r.base == 1 and r.ptr[0] == 1
+
+
+def huge_csc(fill=0.0):
+    """A 1M x 1M CSC with five stored entries: any dense intermediate (8 TB)
+    would fail, so these conversions must work on the stored entries."""
+    n = 1_000_000
+    cols = np.array([3, 3, 70_000, 999_999, 999_999])
+    rows = np.array([10, 500_000, 2, 0, 999_999])
+    vals = np.array([1.5, -2.0, 3.25, 4.0, 0.5])
+    ptr = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(cols, minlength=n), out=ptr[1:])
+    from finchgb.workloads import SparseBuffers
+
+    b = SparseBuffers(n, n, ptr + 1, rows.astype(np.int64) + 1, vals, "csc")
+    return F.Tensor.from_buffers(F.Dense(F.SparseList(F.Element(fill))), b), rows, cols, vals
+
+
+def test_sparse_to_sparse_conversions_skip_the_dense_form():
+    t, rows, cols, vals = huge_csc()
+    t32 = F.Tensor(F.Dense(F.SparseList(F.Element(np.float32(0)))), t)  # another value type
+    assert t32.dtype == np.float32 and t32.countstored() == 5
+    S = F.sparse(t32)
+    assert S.dtype == np.float32 and np.array_equal(S[rows, cols].A1, vals.astype(np.float32))
+    tp = F.Tensor(F.Dense(F.SparseList(F.Pattern())), t)  # pattern
+    assert tp.buf.val is None and tp.countstored() == 5
+    tc = F.Tensor(F.SparseCOO(2, F.Element(0.0)), t)  # COO, column-major
+    I, J, V = tc.coo
+    assert np.array_equal(J - 1, cols) and np.array_equal(I - 1, rows) and np.array_equal(V, vals)
+    tt = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), F.swizzle(t, 2, 1))  # CSC of the transpose
+    St = F.sparse(tt)
+    assert tt.countstored() == 5 and np.array_equal(St[cols, rows].A1, vals)
+    # csr() of a scipy matrix stays sparse too
+    R = sp.csr_matrix((vals, (rows, cols)), shape=(1_000_000, 1_000_000))
+    A = F.csr(R)
+    assert A.shape == (1_000_000, 1_000_000) and A.body.countstored() == 5
+
+
+def test_conversions_drop_stored_fills_of_any_value():
+    D = np.array([[np.inf, 2.0, np.inf], [1.0, np.inf, 5.0]])
+    src = F.Tensor(F.Dense(F.SparseList(F.Element(np.inf))), D)
+    assert src.countstored() == 3
+    # the same fill in another value type: stored entries only
+    t = F.Tensor(F.Dense(F.SparseList(F.Element(np.float32(np.inf)))), src)
+    assert t.countstored() == 3 and np.array_equal(t.todense(), D.astype(np.float32))
+    # a stored entry equal to the fill is dropped (dropfills!)
+    b = src.host_buffers()
+    b.val[0] = np.inf
+    t = F.Tensor(F.Dense(F.SparseList(F.Element(np.inf))), src)
+    assert t.countstored() == 2 and np.array_equal(t.todense(), src.todense())
+    # NaN fills compare equal, as isequal does
+    N = np.array([[np.nan, 1.0], [2.0, np.nan]])
+    tn = F.Tensor(F.Dense(F.SparseList(F.Element(np.nan))), N)
+    t = F.Tensor(F.Dense(F.SparseList(F.Element(np.float32(np.nan)))), tn)
+    assert t.countstored() == 2
+    # different fills: the implicit entries become stored
+    t = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), src)
+    assert t.countstored() == 6 and np.array_equal(t.todense(), src.todense())
