@@ -21,7 +21,8 @@ from .logic import LazyTensor, broadcast, lazy, maximum, minimum, permutedims, r
 from .scheduler import (FinchGBUnsupported, GB300Scheduler, Scalar, compute, default_scheduler,
                         einsum, finch, get_scheduler, set_scheduler, with_scheduler)
 from .tensors import (GPU, Dense, Element, Pattern, SparseByteMap, SparseCOO, SparseList, SwizzleArray,
-                      Tensor, csr, fsparse, fsprand, gpu, pattern, set_fill_value, sparse, swizzle, transfer)
+                      Tensor, csr, fsparse, fsprand, gpu, isequal, pattern, set_fill_value, sparse, swizzle,
+                      transfer)
 from .galley import GalleyScheduler, galley_scheduler
 
 __all__ = [
@@ -31,5 +32,5 @@ __all__ = [
     "reduce", "permutedims", "broadcast", "minimum", "maximum", "GB300Scheduler", "Scalar",
     "default_scheduler", "get_scheduler", "set_scheduler", "with_scheduler", "GPU", "Dense",
     "Element", "Pattern", "SparseCOO", "SparseList", "SwizzleArray", "Tensor", "csr", "fsparse", "fsprand", "fread", "fwrite", "FinchExtensionError",
-    "gpu", "sparse", "swizzle", "transfer", "_lib", "GalleyScheduler", "galley_scheduler",
+    "gpu", "isequal", "sparse", "swizzle", "transfer", "_lib", "GalleyScheduler", "galley_scheduler",
 ]

@@ -352,9 +352,7 @@ class Tensor:
         return f"Tensor({self.fmt}, shape={self.shape}, {where})"
 
     def __eq__(self, other):  # value-wise, like src/interface/compare.jl
-        a = self.todense()
-        b = other.todense() if isinstance(other, (Tensor, SwizzleArray)) else np.asarray(other)
-        return a.shape == b.shape and bool(np.all(a == b))
+        return _equal(self, other, nan_equal=False)
 
     __hash__ = None
 
@@ -414,6 +412,61 @@ def _stored_scipy(t):
     make = sp.csc_matrix if b.orient == "csc" else sp.csr_matrix
     M = make((val, idx, ptr), shape=(b.nrows, b.ncols))
     return M.T if isinstance(t, SwizzleArray) else M
+
+
+def _coord_values(t):
+    """Sorted linear coordinates (column-major) of a sparse matrix's stored
+    entries and their values; None when t is not a Dense(SparseList)."""
+    if not isinstance(t, (Tensor, SwizzleArray)) or t.kind != "csc" or t.ndim != 2:
+        return None
+    M = _stored_scipy(t)
+    if M is None:
+        return None
+    C = _canonical_csc(M)
+    cols = np.repeat(np.arange(C.shape[1], dtype=np.int64), np.diff(C.indptr))
+    return cols * C.shape[0] + C.indices.astype(np.int64), C.data
+
+
+def _equal(a, b, nan_equal: bool) -> bool:
+    """A == B (or isequal) over every coordinate, Finch's helper_equal
+    (src/interface/compare.jl:1-61).  Two sparse matrices are compared on the
+    union of their stored coordinates, and their fills once where neither
+    stores an entry, so no dense form is built."""
+    def eq(x, y):
+        r = np.asarray(x == y)
+        if nan_equal:
+            xn = np.isnan(x) if np.asarray(x).dtype.kind in "fc" else False
+            yn = np.isnan(y) if np.asarray(y).dtype.kind in "fc" else False
+            r = r | (np.asarray(xn) & np.asarray(yn))
+        return r
+
+    if tuple(getattr(a, "shape", np.shape(a))) != tuple(getattr(b, "shape", np.shape(b))):
+        return False
+    ca, cb = _coord_values(a), _coord_values(b)
+    if ca is None or cb is None:
+        x = a.todense() if hasattr(a, "todense") else np.asarray(a)
+        y = b.todense() if hasattr(b, "todense") else np.asarray(b)
+        return bool(np.all(eq(x, y)))
+    (ka, va), (kb, vb) = ca, cb
+    keys = np.union1d(ka, kb)
+    fa, fb = np.asarray(a.fill_value), np.asarray(b.fill_value)
+
+    def at(k, v, fill):
+        out = np.full(keys.size, fill, dtype=np.result_type(v.dtype, fill.dtype))
+        pos = np.searchsorted(keys, k)
+        out[pos] = v
+        return out
+
+    if not np.all(eq(at(ka, va, fa), at(kb, vb, fb))):
+        return False
+    total = int(np.prod(a.shape))
+    return keys.size == total or bool(eq(fa, fb))
+
+
+def isequal(a, b) -> bool:
+    """Finch's isequal on tensors: == with NaN equal to NaN
+    (src/interface/compare.jl:29-61)."""
+    return _equal(a, b, nan_equal=True)
 
 
 def _canonical_csc(A):
@@ -493,8 +546,7 @@ class SwizzleArray:
         return np.transpose(self.body.todense(), [d - 1 for d in self.dims])
 
     def __eq__(self, other):
-        b = other.todense() if hasattr(other, "todense") else np.asarray(other)
-        return bool(np.all(self.todense() == b))
+        return _equal(self, other, nan_equal=False)
 
     __hash__ = None
 

@@ -207,3 +207,30 @@ def test_conversions_drop_stored_fills_of_any_value():
     # different fills: the implicit entries become stored
     t = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), src)
     assert t.countstored() == 6 and np.array_equal(t.todense(), src.todense())
+
+
+def test_equality_walks_stored_entries_only():
+    """== and isequal as src/interface/compare.jl: every coordinate compared,
+    two sparse matrices over the union of their stored entries and their
+    fills, which holds for 1M x 1M operands."""
+    t, rows, cols, vals = huge_csc()
+    same = F.Tensor(sp.csc_matrix((vals, (rows, cols)), shape=t.shape))  # 0-based buffers
+    assert t == same and F.isequal(t, same)
+    other = sp.csc_matrix((vals * 2, (rows, cols)), shape=t.shape)
+    assert not (t == F.Tensor(other))
+    # an explicitly stored fill equals an implicit one
+    extra = sp.csc_matrix((np.r_[vals, 0.0], (np.r_[rows, 7], np.r_[cols, 8])), shape=t.shape)
+    assert t == F.Tensor(extra)
+    # fills differ where neither stores an entry
+    t1, *_ = huge_csc(fill=1.0)
+    assert not (t == t1)
+    # the CSR view of the transpose
+    tt = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), F.swizzle(t, 2, 1))
+    assert F.swizzle(tt, 2, 1) == t
+    # NaN: == is false, isequal true
+    N = np.array([[np.nan, 1.0], [0.0, 2.0]])
+    a, b = F.Tensor(CSC_F64, N), F.Tensor(sp.csc_matrix(N))
+    assert not (a == b) and F.isequal(a, b)
+    # against a dense array
+    assert a.__eq__(np.array([[1.0, 1.0], [0.0, 2.0]])) is False
+    assert F.isequal(a, N) and not F.isequal(a, N[:1])
