@@ -302,13 +302,15 @@ class Tensor:
                 uk = k[heads]
                 out[uk % self.shape[0], uk // self.shape[0]] = folded
             return out
-        buf = self.host_buffers()
-        D = buf.todense()
-        if buf.val is None:
-            D = D != 0
-        out = np.full(buf.todense().shape, self.fill_value, dtype=self.dtype)
-        mask = _stored_mask(buf)
-        out[mask] = D[mask]
+        buf = self.host_buffers()  # stored entries over the fill, one dense array
+        out = np.full((buf.nrows, buf.ncols), self.fill_value, dtype=self.dtype)
+        f = np.repeat(np.arange(buf.nfibers), np.diff(buf.ptr))
+        c = np.asarray(buf.idx, dtype=np.int64) - buf.base
+        v = True if buf.val is None else buf.val
+        if buf.orient == "csc":
+            out[c, f] = v
+        else:
+            out[f, c] = v
         return out.reshape(self.shape)
 
     def pair_device(self):
@@ -355,17 +357,6 @@ class Tensor:
         return _equal(self, other, nan_equal=False)
 
     __hash__ = None
-
-
-def _stored_mask(buf: SparseBuffers) -> np.ndarray:
-    mask = np.zeros((buf.nrows, buf.ncols), dtype=bool)
-    f = np.repeat(np.arange(buf.nfibers), np.diff(buf.ptr))
-    c = np.asarray(buf.idx, dtype=np.int64) - buf.base
-    if buf.orient == "csc":
-        mask[c, f] = True
-    else:
-        mask[f, c] = True
-    return mask
 
 
 def _scipy_sparse(x):
