@@ -53,6 +53,19 @@ __global__ void __launch_bounds__(DOT_THREADS) dot_fold(const T* __restrict__ pa
   if (threadIdx.x == 0) out[0] = acc;
 }
 
+// out = alpha*x + beta with alpha/beta device scalars (NULL: 1 and 0), or
+// out = beta with x NULL; fused (one rounding), like the Finch-order SpMV
+// and axpby around it.
+template <class T>
+__global__ void affine_k(int64_t n, const T* __restrict__ alpha, const T* __restrict__ x,
+                         const T* __restrict__ beta, T* __restrict__ out) {
+  const T a = alpha ? alpha[0] : T(1);
+  const T b = beta ? beta[0] : T(0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = x ? fused(a, x[i], b) : b;
+}
+
 // out = alpha*x + beta*y with alpha/beta device scalars (NULL means 1),
 // optional negation of each term (sign bits: 1 = -alpha, 2 = -beta).
 template <class T>
@@ -168,6 +181,24 @@ int fgb_dense_axpby(fgb_ctx* ctx, int dtype, int64_t n, const void* alpha, const
   else
     return set_error(FGB_EUNSUPPORTED, "fgb_dense_axpby: dtype %d", dtype);
   return check_launch("fgb_dense_axpby");
+}
+
+int fgb_dense_affine(fgb_ctx* ctx, int dtype, int64_t n, const void* alpha, const void* x,
+                     const void* beta, void* out, void* stream) {
+  if (!ctx) return set_error(FGB_EINVAL, "fgb_dense_affine: null ctx");
+  if (n < 0 || (n > 0 && !out)) return set_error(FGB_EINVAL, "fgb_dense_affine: bad argument");
+  if (n == 0) return FGB_OK;
+  cudaStream_t s = pick_stream(ctx, stream);
+  const int grid = grid_for(n, 256, ctx->num_sms, 8);
+  if (dtype == FGB_F64)
+    affine_k<double><<<grid, 256, 0, s>>>(n, (const double*)alpha, (const double*)x, (const double*)beta,
+                                          (double*)out);
+  else if (dtype == FGB_F32)
+    affine_k<float><<<grid, 256, 0, s>>>(n, (const float*)alpha, (const float*)x, (const float*)beta,
+                                         (float*)out);
+  else
+    return set_error(FGB_EUNSUPPORTED, "fgb_dense_affine: dtype %d", dtype);
+  return check_launch("fgb_dense_affine");
 }
 
 int fgb_dense_map(fgb_ctx* ctx, int op, int dtype, int64_t n, const void* x, const void* y,

@@ -189,6 +189,30 @@ __global__ void zero_vec(T* y, int64_t n) {
     y[i] = T(0);
 }
 
+// Counts for reduce(+, A; dims) of a Pattern (every stored entry is true)
+// or Bool matrix: Julia sums Bools into Int64.  v NULL for a Pattern.
+template <class P>
+__global__ void count_fiber_k(int64_t nf, Fiber<P> a, const unsigned char* __restrict__ v,
+                              long long* __restrict__ out) {
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = a.lo(f), hi = a.hi(f);
+    long long c = 0;
+    if (!v) c = hi - lo;
+    else
+      for (int64_t p = lo; p < hi; ++p) c += v[p] ? 1 : 0;
+    out[f] = c;
+  }
+}
+
+template <class P>
+__global__ void count_scatter_k(int64_t nnz, Fiber<P> a, const unsigned char* __restrict__ v,
+                                unsigned long long* __restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz;
+       p += (int64_t)gridDim.x * blockDim.x)
+    if (!v || v[p]) atomicAdd(out + a.at(p), 1ull);
+}
+
 template <class P>
 static Fiber<P> fiber_of(const fgb_sparse* A) {
   return Fiber<P>{(const P*)A->ptr, (const int*)A->idx, A->index_base};
@@ -301,6 +325,36 @@ int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_spar
   int rc = B ? check_pair(A, B, "fgb_ewise_reduce") : check_sparse(A, "fgb_ewise_reduce: A", true);
   if (rc) return rc;
   if (!B && B_dense && ldb < A->ncols) return set_error(FGB_EINVAL, "fgb_ewise_reduce: ldb < ncols");
+  if (!B && !B_dense && (A->val_t == FGB_NONE || A->val_t == FGB_BOOL) && dtype == FGB_I64) {
+    // reduce(+, A; dims) of a Pattern or Bool matrix: Int64 counts
+    if (!y) return set_error(FGB_EINVAL, "fgb_ewise_reduce: null y");
+    cudaStream_t s = pick_stream(ctx, stream);
+    const int64_t nf = n_fibers(A);
+    const bool per_fiber = dims == 0 || (A->orient == FGB_CSR ? dims == 2 : dims == 1);
+    const int64_t out_len = dims == 0 ? 1 : (dims == 2 ? A->nrows : A->ncols);
+    const unsigned char* v = A->val_t == FGB_BOOL ? (const unsigned char*)A->val : nullptr;
+    if (!per_fiber || nf == 0)
+      FGB_CUDA_TRY(cudaMemsetAsync(y, 0, sizeof(long long) * out_len, s));
+    if (!per_fiber)
+      return with_fibers(A, nullptr, [&](auto fa, auto) {
+        count_scatter_k<<<grid_for(A->nnz, 256, ctx->num_sms, 8), 256, 0, s>>>(A->nnz, fa, v,
+                                                                                 (unsigned long long*)y);
+        return check_launch("count_scatter");
+      });
+    if (nf == 0) return FGB_OK;
+    long long* target = (long long*)y;
+    if (dims == 0) FGB_CUDA_TRY(cudaMallocAsync((void**)&target, sizeof(long long) * nf, s));
+    rc = with_fibers(A, nullptr, [&](auto fa, auto) {
+      count_fiber_k<<<grid_for(nf, 256, ctx->num_sms, 8), 256, 0, s>>>(nf, fa, v, target);
+      return check_launch("count_fiber");
+    });
+    if (rc == FGB_OK && dims == 0) {
+      fold_partials<long long><<<1, 1024, 0, s>>>(target, nf, (long long*)y);
+      rc = check_launch("fold_partials");
+    }
+    if (target != (long long*)y) cudaFreeAsync(target, s);
+    return rc;
+  }
   if (A->val_t != dtype) return set_error(FGB_EUNSUPPORTED, "fgb_ewise_reduce: A dtype != dtype");
   if (dtype != FGB_F32 && dtype != FGB_F64)
     return set_error(FGB_EUNSUPPORTED, "fgb_ewise_reduce: dtype %d", dtype);

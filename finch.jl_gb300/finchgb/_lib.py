@@ -160,6 +160,11 @@ SIGNATURES: dict[str, tuple] = {
                                 c_void_p, c_int, c_void_p]),
     "fgb_dense_map": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
                               c_void_p]),
+    "fgb_dense_affine": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p]),
+    "fgb_sparse_scale": (c_int, [c_void_p, POINTER(FgbSparse), c_int, c_int, c_int, c_void_p, c_int, c_int,
+                                 c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(c_int64),
+                                 POINTER(c_int64), c_void_p]),
     "fgb_scalar_op": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fgb_spgemm_dense": (c_int, [c_void_p, POINTER(FgbSparse), POINTER(FgbSparse), c_int, c_uint, c_void_p,
                                  c_int64, c_void_p]),
@@ -205,6 +210,7 @@ SERVE_BATCHED, SERVE_PER_CALL = 0, 1
 
 # fgb_map_op
 MAP_ADD, MAP_SUB, MAP_MUL, MAP_DIV, MAP_MIN, MAP_MAX = range(6)
+AXIS_ROW, AXIS_COL = 0, 1
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

@@ -385,6 +385,39 @@ def axpby(alpha: torch.Tensor | None, x: torch.Tensor, beta: torch.Tensor | None
     return out
 
 
+def dense_affine(alpha: torch.Tensor | None, x: torch.Tensor | None, beta: torch.Tensor | None,
+                 out: torch.Tensor) -> torch.Tensor:
+    """out = alpha*x + beta (fused), or out = beta with x None
+    (fgb_dense_affine): device-scalar alpha/beta (None: 1 and 0)."""
+    L.call("fgb_dense_affine", _ctx_for(out), dtype_code(out), out.numel(),
+           None if alpha is None else alpha.data_ptr(), _dptr(x),
+           None if beta is None else beta.data_ptr(), _dptr(out), stream_ptr())
+    return out
+
+
+def sparse_scale(A: DeviceSparse, by: torch.Tensor, by_axis: int, keep: torch.Tensor | None = None,
+                 keep_axis: int = L.AXIS_ROW, op: int = L.MAP_DIV,
+                 out_dtype: torch.dtype = torch.float64) -> tuple[DeviceSparse, int]:
+    """The stored entries of A combined with `by` over one index and kept
+    where `keep` over an index is non-zero (fgb_sparse_scale).  Returns the
+    0-based result in A's orientation and how many elements of `by` turn
+    the fill 0 into something else (0 means skipping unstored entries was
+    exact)."""
+    nf = A.ncols if A.orient == "csc" else A.nrows
+    d = A.idx.device
+    out_ptr = torch.empty(nf + 1, dtype=torch.int64, device=d)
+    out_idx = torch.empty(A.nnz, dtype=torch.int32, device=d)
+    out_val = torch.empty(A.nnz, dtype=out_dtype, device=d)
+    kept, changed = ctypes.c_int64(), ctypes.c_int64()
+    desc = A.desc()
+    L.call("fgb_sparse_scale", _ctx_for(A.idx), ctypes.byref(desc), op, by_axis, dtype_code(by), _dptr(by),
+           keep_axis, 0 if keep is None else dtype_code(keep), _dptr(keep), dtype_code(out_val),
+           out_ptr.data_ptr(), _dptr(out_idx), _dptr(out_val), ctypes.byref(kept), ctypes.byref(changed),
+           stream_ptr())
+    n = kept.value
+    return DeviceSparse(A.nrows, A.ncols, out_ptr, out_idx[:n], out_val[:n], A.orient, 0), changed.value
+
+
 def dense_map(op: int, x: torch.Tensor, y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """out = op.(x, y) for op in MAP_ADD/SUB/MUL/MIN/MAX."""
     if out is None:
@@ -407,12 +440,13 @@ def ewise_reduce(dims: int, A: DeviceSparse, B: DeviceSparse | None = None,
                  B_dense: torch.Tensor | None = None, y: torch.Tensor | None = None) -> torch.Tensor:
     """sum(A .* B; dims) (dims 0 = all, 1 = over rows, 2 = over columns)."""
     length = 1 if dims == 0 else (A.nrows if dims == 2 else A.ncols)
-    if y is None:
-        y = torch.empty(length, dtype=A.val.dtype, device=A.idx.device)
+    counts = B is None and B_dense is None and (A.val is None or A.val.dtype == torch.uint8)
+    if y is None:  # a Pattern or Bool matrix sums into Int64 counts, as Julia sums Bools
+        y = torch.empty(length, dtype=torch.int64 if counts else A.val.dtype, device=A.idx.device)
     da = A.desc()
     db = None if B is None else ctypes.byref(B.desc())
     L.call("fgb_ewise_reduce", _ctx_for(A.idx), dims, ctypes.byref(da), db, _dptr(B_dense),
-           0 if B_dense is None else B_dense.stride(0), _dptr(y), dtype_code(A.val), 0,
+           0 if B_dense is None else B_dense.stride(0), _dptr(y), L.I64 if counts else dtype_code(A.val), 0,
            stream_ptr())
     return y
 

@@ -3,6 +3,7 @@ their @finch programs run through the matcher onto the GPU kernels:
 
   bfs(edges, source)          docs/examples/bfs.jl
   bellmanford(edges, source)  docs/examples/shortest_paths.jl
+  pagerank(edges, nsteps, damp)  docs/examples/pagerank.jl
 
 The programs are the reference's, statement for statement; vertex numbers
 are 1-based as in Finch.  Each round's tensors stay in HBM between the
@@ -55,6 +56,64 @@ RELAX = """
         end
     end
 """
+
+
+OUT_DEGREE = """
+    out_degree .= 0
+    for j=_, i=_
+        out_degree[j] += edges[i, j]
+    end
+"""
+
+SCALE_EDGES = """
+    scaled_edges .= 0
+    for j=_, i=_
+        if out_degree[i] != 0
+            scaled_edges[i, j] = edges[i, j] / out_degree[j]
+        end
+    end
+"""
+
+RANK_INIT = """
+    r .= 0.0
+    for j=_
+        r[j] = 1.0 / n
+    end
+"""
+
+RANK_STEP = """
+    rank .= 0
+    for j=_, i=_
+        rank[i] += scaled_edges[i, j] * r[j]
+    end
+"""
+
+RANK_DAMP = """
+    r .= 0.0
+    for i=_
+        r[i] = beta_score + damp * rank[i]
+    end
+"""
+
+
+def pagerank(edges, nsteps: int = 20, damp: float = 0.85) -> Tensor:
+    """`nsteps` steps of PageRank on the adjacency matrix `edges` (edges[i, j]
+    an edge j -> i), as pagerank.jl computes it: out-degrees, the masked
+    transition matrix, then rank = scaled_edges * r and r = beta + damp * rank
+    per step.  The rank sums run in Finch's serial order.  A vertex without
+    out-edges makes pagerank.jl divide 0 by 0 where `edges` stores nothing;
+    that program is refused (FinchGBUnsupported)."""
+    n, m = edges.shape
+    assert n == m
+    out_degree = finch(OUT_DEGREE, edges=edges)["out_degree"]
+    scaled_edges = finch(SCALE_EDGES, edges=edges, out_degree=out_degree)["scaled_edges"]
+    r = finch(RANK_INIT, r=Tensor(Dense(Element(0.0)), shape=(n,)), n=n)["r"]
+    rank = Tensor(Dense(Element(0.0)), shape=(n,))
+    beta_score = (1 - damp) / n
+    for _ in range(nsteps):
+        rank = finch(RANK_STEP, rank=rank, scaled_edges=scaled_edges, r=r)["rank"]
+        r = finch(RANK_DAMP, r=r, beta_score=beta_score, damp=damp, rank=rank)["r"]
+    return r
 
 
 def bfs(edges, source: int = 5) -> Tensor:

@@ -29,12 +29,23 @@ graph kernels of libfinchgb.
       end; end; end; end
   -> fgb_minby_relax over the CSR of `edges` (row i lists its j)
 
+  Transition matrix of PageRank (docs/examples/pagerank.jl:18-25)
+      scaled_edges .= 0
+      for j=_, i=_
+        if out_degree[i] != 0
+          scaled_edges[i, j] = edges[i, j] / out_degree[j]
+        end
+      end
+  -> fgb_sparse_scale over the stored entries of `edges` (the condition may
+     test either index, the divisor run over either, and `*` stands for `/`)
+
 The matchers bind the program's own tensor and index names, so any names
 work; the shapes of the statements must be these.  Vertex numbers are
 Finch's, 1-based.
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import device as dev
@@ -195,6 +206,42 @@ def match_minby_relax(prog) -> dict | None:
     return {"active": act, "active_prev": aprev, "dist_prev": dprev, "edges": edges, "dist": upd.lhs.tns}
 
 
+def match_masked_scale(prog) -> dict | None:
+    s = stmts(prog)
+    if len(s) != 2 or not isinstance(s[0], Init) or not isinstance(s[1], Loop):
+        return None
+    out = s[0].name
+    if not (isinstance(s[0].value, Lit) and s[0].value.value == 0 and not isinstance(s[0].value.value, bool)):
+        return None
+    nest = _nested(s[1], 2)
+    if nest is None:
+        return None
+    (j, i), body = nest
+    keep = None
+    sv = single(body)
+    if isinstance(sv, Sieve):
+        c = sv.cond
+        if not (isinstance(c, Call) and c.fn == "!=" and len(c.args) == 2 and isinstance(c.args[1], Lit)
+                and c.args[1].value == 0 and isinstance(c.args[0], Index) and len(c.args[0].idxs) == 1
+                and isinstance(c.args[0].idxs[0], Var) and c.args[0].idxs[0].name in (i, j)):
+            return None
+        keep = (c.args[0].tns, "row" if c.args[0].idxs[0].name == i else "col")
+        sv = single(sv.body)
+    if not (isinstance(sv, Assign) and sv.op is None and _is_idx(sv.lhs, out, i, j)):
+        return None
+    rhs = sv.rhs
+    if not (isinstance(rhs, Call) and rhs.fn in ("/", "*") and len(rhs.args) == 2):
+        return None
+    pairs = [rhs.args] if rhs.fn == "/" else [rhs.args, rhs.args[::-1]]
+    for a, b in pairs:
+        if (_is_idx(a, None, i, j) and isinstance(b, Index) and len(b.idxs) == 1 and isinstance(b.idxs[0], Var)
+                and b.idxs[0].name in (i, j) and b.tns != a.tns):
+            return {"out": out, "init": s[0].value.value, "edges": a.tns, "by": b.tns,
+                    "by_axis": "row" if b.idxs[0].name == i else "col", "op": rhs.fn,
+                    "keep": None if keep is None else keep[0], "keep_axis": None if keep is None else keep[1]}
+    return None
+
+
 # ---------------------------------------------------------------- execution
 
 
@@ -232,6 +279,9 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
         dst = tensors[m["dst"]].pair_device()
         dev.minby_map(mask, src, dst)
         return {m["dst"]: tensors[m["dst"]]}
+    m = match_masked_scale(prog)
+    if m is not None:
+        return _run_masked_scale(m, tensors)
     m = match_minby_relax(prog)
     if m is not None:
         A = adjacency_rows(tensors[m["edges"]])
@@ -243,3 +293,35 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
         act = dev.minby_relax(A, dprev[0], aprev, dst, index_offset=1)
         return {m["active"]: dense_from_device(act, False), m["dist"]: tensors[m["dist"]]}
     return None
+
+
+def _run_masked_scale(m: dict, tensors: dict) -> dict:
+    """fgb_sparse_scale for a matched masked scale.  The kernel visits the
+    stored entries of the sparse operand; Finch's nest also writes
+    `0 op by[l]` where it stores nothing, since `/` has no annihilator
+    (src/symbolic/symbolic.jl:145-153).  Those values equal the fill 0
+    unless an element of `by` is 0 or NaN (Inf or NaN for `*`), which the
+    library counts: such a program is refused rather than answered
+    differently."""
+    from . import _lib as L
+    from .scheduler import FinchGBUnsupported, _device_vector, sparse_operand
+    from .tensors import sparse_from_device
+
+    e = tensors[m["edges"]]
+    fill = (e.body if hasattr(e, "body") else e).fill_value
+    if np.any(np.asarray(fill)):
+        raise FinchGBUnsupported(f"{m['edges']}: a scale of stored entries needs a zero fill, not {fill!r}")
+    A = sparse_operand(e, ("i", "j"), ("i", "j"))
+    by = _device_vector(tensors[m["by"]], None)
+    keep = None if m["keep"] is None else _device_vector(tensors[m["keep"]], None)
+    prev = tensors.get(m["out"])
+    out_dtype = torch.float32 if prev is not None and np.dtype(prev.dtype) == np.float32 else torch.float64
+    axis = {"row": L.AXIS_ROW, "col": L.AXIS_COL}
+    res, changed = dev.sparse_scale(A, by, axis[m["by_axis"]], keep, axis.get(m["keep_axis"], L.AXIS_ROW),
+                                    L.MAP_DIV if m["op"] == "/" else L.MAP_MUL, out_dtype)
+    if changed:
+        raise FinchGBUnsupported(
+            f"{changed} element(s) of {m['by']} make `0 {m['op']} {m['by']}` non-zero (0/0 is NaN): Finch's "
+            f"nest writes that value wherever {m['edges']} stores nothing, so visiting its stored entries "
+            f"alone would give another result")
+    return {m["out"]: sparse_from_device(res, fill_value=float(m["init"]))}

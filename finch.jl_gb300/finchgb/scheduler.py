@@ -123,6 +123,26 @@ def dense_operand(t, idxs: tuple, want: tuple) -> torch.Tensor:
     raise FinchGBUnsupported(f"dense access {idxs} vs {want}")
 
 
+_CONST_OPS = {"+": lambda a, b: a + b, "-": lambda a, b: a - b, "*": lambda a, b: a * b,
+              "/": lambda a, b: a / b}
+
+
+def _constant(n):
+    """The value of an expression of literals (Julia's arithmetic on Float64
+    and Int values, evaluated on the host), else None."""
+    if isinstance(n, Literal):
+        v = n.value
+        return v if isinstance(v, (int, float, np.integer, np.floating)) and not isinstance(v, bool) else None
+    if isinstance(n, MapJoin) and n.op in _CONST_OPS and len(n.args) == 2:
+        a, b = _constant(n.args[0]), _constant(n.args[1])
+        if a is None or b is None:
+            return None
+        if n.op == "/":  # Julia's / always gives a float
+            return float(a) / float(b) if b != 0 else (float("nan") if a == 0 else float(np.sign(a)) * float("inf"))
+        return _CONST_OPS[n.op](a, b)
+    return None
+
+
 def _scalar_tensor(x, like_dtype) -> torch.Tensor:
     if isinstance(x, Scalar):
         return x.t
@@ -213,7 +233,7 @@ class GB300Scheduler:
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
         for rule in (self._spmv, self._spmm, self._spmm_semiring, self._spgemm, self._sddmm, self._ewise,
-                     self._ewise_reduce, self._dot, self._dense_map, self._scalar):
+                     self._ewise_reduce, self._dot, self._dense_map, self._dense_fill, self._scalar):
             r = rule(m, out, accumulate)
             if r is not None:
                 if self.verbose:
@@ -507,7 +527,29 @@ class GB300Scheduler:
             if s is not None:
                 self.last_kernel = "fgb_dense_axpby"
                 return dense_from_device(dev.axpby(s[0], s[1], None, None, o))
+        if core.op == "+" and len(core.args) == 2:  # c + s*x or s*x + c, c a constant
+            for c, t in (core.args, core.args[::-1]):
+                cv = _constant(c)
+                sx = scaled(t)
+                if cv is not None and sx is not None:
+                    x = sx[1]
+                    self.last_kernel = "fgb_dense_affine"
+                    r = dev.dense_affine(sx[0], x, _scalar_tensor(cv, x.dtype),
+                                         torch.empty_like(x) if o is None else o)
+                    return dense_from_device(r)
         return None
+
+    # -- z[i] = c: an assignment of a constant, the extent taken from the output
+    def _dense_fill(self, m: Match, out, accumulate):
+        if m.agg is not None or len(m.outs) != 1 or out is None:
+            return None
+        cv = _constant(m.core)
+        if cv is None:
+            return None
+        (i,) = m.outs
+        o = dense_operand(out, (i,), (i,))
+        self.last_kernel = "fgb_dense_affine"
+        return dense_from_device(dev.dense_affine(None, None, _scalar_tensor(cv, o.dtype), o))
 
     # -- s[] = a[] op b[]
     def _scalar(self, m: Match, out, accumulate):
@@ -667,7 +709,11 @@ def finch(program: str, ctx: GB300Scheduler | None = None, algebra: AbstractAlge
         init = prog.init[name]
         if plan.op is not None and init != _identity_value(plan.op, init):
             raise FinchGBUnsupported(f"@finch: {name} .= {init} is not the identity of {plan.op}")
-        res = sched(plan.logic())
+        if name in tensors and set(plan.out_idxs) - set(indices_of(flatten(plan.rhs))):
+            # `r[j] = c`: no operand gives j its extent, the output does (and is overwritten)
+            res = sched(plan.logic(), out=tensors[name], accumulate=False)
+        else:
+            res = sched(plan.logic())
     else:
         if name not in tensors:
             raise KeyError(f"@finch: output {name} must be passed when it is not initialised")

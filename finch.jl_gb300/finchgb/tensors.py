@@ -174,6 +174,16 @@ class Tensor:
         if arr is None:
             if shape is None:
                 raise ValueError("Tensor needs an array or a shape")
+            if self.kind in ("csc", "coo") and len(shape) == 2:  # an empty sparse matrix, no dense form
+                self.shape = tuple(map(int, shape))
+                m, n = self.shape
+                if self.kind == "coo":
+                    e = np.zeros(0, np.int64)
+                    self.coo = (e, e, np.zeros(0, self.dtype))
+                else:
+                    val = None if isinstance(self.fmt.lvl.lvl, Pattern) else np.zeros(0, self.dtype)
+                    self.buf = SparseBuffers(m, n, np.ones(n + 1, np.int64), np.zeros(0, np.int64), val, "csc")
+                return
             if self.dtype.names:
                 arr = np.empty(shape, dtype=self.dtype)
                 arr[...] = tuple(self.fill_value)

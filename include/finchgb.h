@@ -178,6 +178,38 @@ FGB_API int fgb_transpose(fgb_ctx* ctx, const fgb_sparse* A, int64_t* out_ptr, i
 FGB_API int fgb_sparse_to_dense(fgb_ctx* ctx, const fgb_sparse* A, const void* fill, void* out, int64_t ld,
                                 void* stream);
 
+/* The index a dense vector runs over in fgb_sparse_scale: A[i, j]'s row i
+ * or column j. */
+typedef enum fgb_axis {
+  FGB_AXIS_ROW = 0,
+  FGB_AXIS_COL = 1
+} fgb_axis;
+
+/* Stored entries of A combined with a dense vector and filtered by another
+ * one -- the masked broadcast that builds PageRank's transition matrix
+ * (docs/examples/pagerank.jl:17-25):
+ *     for j=_, i=_; if keep[k] != 0; out[i, j] = A[i, j] op by[l]; end; end
+ * with k and l the row i or column j as keep_axis and by_axis name them
+ * (keep NULL keeps every entry).  op is FGB_MAP_MUL or FGB_MAP_DIV.  A's
+ * values (F64, F32, I32, I64, BOOL, or NONE: a Pattern's true = 1) and `by`
+ * (F64, F32, I32, I64, BOOL) are combined in F32 when one of them is F32
+ * and neither is F64 (Julia's promotion for / and *), otherwise in F64
+ * (integer products too), and converted to out_t (F64 or F32).  keep: F64,
+ * F32, I32, I64 or BOOL (NaN counts as non-zero, as NaN != 0 is true).
+ * The result keeps A's orientation and entry order without the dropped
+ * entries: out_ptr (int64, n_fibers + 1, 0-based), out_idx (int32) and
+ * out_val (out_t) with room for A->nnz entries; *out_nnz (host) receives
+ * the kept count.  *n_fill_changed (host, may be NULL) receives how many
+ * elements of `by` turn A's fill 0 into something else (0/0 and 0/NaN for
+ * DIV, 0*Inf and 0*NaN for MUL): when it is 0, the entries A does not store
+ * would all come out 0, so visiting stored entries only is exact -- Finch's
+ * nest writes `0 / by[l]` there too, as `/` has no annihilator
+ * (src/symbolic/symbolic.jl:145-153).  Synchronous. */
+FGB_API int fgb_sparse_scale(fgb_ctx* ctx, const fgb_sparse* A, int op, int by_axis, int by_t,
+                             const void* by, int keep_axis, int keep_t, const void* keep, int out_t,
+                             int64_t* out_ptr, int32_t* out_idx, void* out_val, int64_t* out_nnz,
+                             int64_t* n_fill_changed, void* stream);
+
 /* Duplicate handling of fgb_coo_assemble: Julia's `combine` for fsparse. */
 typedef enum fgb_combine {
   FGB_COMBINE_ADD = 0, /* +  (the default; | for Bool values) */
@@ -375,7 +407,9 @@ FGB_API int fgb_ewise_fill(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_
  * B is a sparse matrix of the same shape/orientation (B_dense == NULL), a
  * dense row-major m x n matrix (B == NULL, ld = ldb), or absent (both NULL:
  * B = 1, i.e. reduce(+, A; dims), test/reference64/interface/
- * reduce_default.txt).  F32 or F64.
+ * reduce_default.txt).  F32 or F64; reduce(+, A; dims) of a Pattern or Bool
+ * A (val_t FGB_NONE or FGB_BOOL) counts its true entries into I64, as
+ * Julia sums Bools into Int64 (dtype FGB_I64).
  * Replaces compute(sum(lazy(A) .* lazy(B); dims)) (src/interface/lazy.jl). */
 FGB_API int fgb_ewise_reduce(fgb_ctx* ctx, int dims, const fgb_sparse* A, const fgb_sparse* B,
                      const void* B_dense, int64_t ldb, void* y, int dtype, unsigned flags,
@@ -450,6 +484,14 @@ FGB_API int fgb_dense_dot(fgb_ctx* ctx, int dtype, int64_t n, const void* x, con
  * signs bit 0 negates a, bit 1 negates b; y NULL = 0).  F32 or F64. */
 FGB_API int fgb_dense_axpby(fgb_ctx* ctx, int dtype, int64_t n, const void* alpha, const void* x,
                             const void* beta, const void* y, void* out, int signs, void* stream);
+
+/* out[i] = alpha*x[i] + beta, or out[i] = beta with x NULL; alpha
+ * and beta are device scalars (alpha NULL = 1, beta NULL = 0).  The
+ * `r[i] = b + a*x[i]` and `r[j] = c` assignments of Finch programs
+ * (docs/examples/pagerank.jl:27-32,43-48); fused (one rounding), as the
+ * Finch-order SpMV and fgb_dense_axpby are by default.  F32 or F64. */
+FGB_API int fgb_dense_affine(fgb_ctx* ctx, int dtype, int64_t n, const void* alpha, const void* x,
+                             const void* beta, void* out, void* stream);
 
 /* out[i] = op(x[i], y[i]) for op in ADD/SUB/MUL/MIN/MAX, the pointwise
  * `x = op.(x, y)` maps of Finch programs.  F64, F32, I32 (wrapping), I64. */

@@ -88,6 +88,8 @@ def lib(fast: bool = False) -> ctypes.CDLL:
             L.orc_bfs_round.restype = i64
             L.orc_minby_round.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
             L.orc_minby_round.restype = None
+            L.orc_pagerank.argtypes = [i64, vp, vp, vp, i64, ctypes.c_double, i32, vp]
+            L.orc_pagerank.restype = i32
             if fast:
                 _fast_lib = L
             else:
@@ -245,6 +247,20 @@ def bfs_round(n, ptr, idx, F, V, P, fill=0):
     c = lib().orc_bfs_round(n, _p(_i64(ptr)), _p(_i64(idx)), _p(np.ascontiguousarray(F, dtype=np.uint8)),
                             _p(V), _p(P), int(fill), _p(nF))
     return nF, int(c)
+
+
+def pagerank(n, ptr, idx, w=None, nsteps=20, damp=0.85, fma=False):
+    """Finch's PageRank example (docs/examples/pagerank.jl:7-51) over the
+    CSC adjacency (column j lists the i with edges[i, j]); w None for a
+    Pattern.  Returns r (float64).  The transition matrix is built over
+    every (i, j) as Finch's nest builds it, so this needs n * n doubles."""
+    r = np.zeros(n, dtype=np.float64)
+    wp = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    rc = lib().orc_pagerank(n, _p(_i64(ptr)), _p(_i64(idx)), None if wp is None else _p(wp), int(nsteps),
+                            float(damp), int(bool(fma)), _p(r))
+    if rc != 0:
+        raise MemoryError(f"oracle pagerank: {n} x {n} scratch")
+    return r
 
 
 def minby_round(n, ptr, idx, w, dprev, pprev, aprev, dist, par):

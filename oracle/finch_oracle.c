@@ -637,6 +637,52 @@ void orc_minby_round(int64_t n, const int64_t* ptr, const int64_t* idx, const do
   }
 }
 
+/* PageRank, docs/examples/pagerank.jl:7-51, as written, over the CSC of
+ * `edges` (column j lists the i with edges[i, j]; w NULL for a Pattern,
+ * whose stored entries are true = 1).  out_degree[j] += edges[i, j] visits
+ * the stored entries (the fill 0 is the identity of +).  The transition
+ * matrix is the loop over every (i, j), the fill region included, as `/`
+ * has no annihilator (src/symbolic/symbolic.jl:145-153): where
+ * out_degree[i] != 0 it stores edges[i, j] / out_degree[j], which is
+ * 0 / out_degree[j] where edges stores nothing (NaN for a zero
+ * out-degree).  r[j] = 1.0 / n.  Each step: rank .= 0; for j, then the
+ * stored i ascending, rank[i] += scaled[i, j] * r[j]; then r[i] = beta +
+ * damp * rank[i], beta = (1 - damp) / n; both fused when fma != 0.  Needs
+ * n * n doubles of scratch: returns -1 when they cannot be allocated. */
+int orc_pagerank(int64_t n, const int64_t* ptr, const int64_t* idx, const double* w, int64_t nsteps, double damp,
+                 int fma_on, double* r) {
+  double* deg = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+  double* col = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+  double* rank = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+  double* S = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n * n : 1));
+  uint8_t* st = (uint8_t*)malloc((size_t)(n > 0 ? n * n : 1));
+  if (!deg || !col || !rank || !S || !st) {
+    free(deg); free(col); free(rank); free(S); free(st);
+    return -1;
+  }
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t q = ptr[j] - 1; q < ptr[j + 1] - 1; ++q) deg[j] += w ? w[q] : 1.0;
+  for (int64_t j = 0; j < n; ++j) {
+    for (int64_t i = 0; i < n; ++i) col[i] = 0.0;
+    for (int64_t q = ptr[j] - 1; q < ptr[j + 1] - 1; ++q) col[idx[q] - 1] = w ? w[q] : 1.0;
+    for (int64_t i = 0; i < n; ++i) {
+      st[i + j * n] = deg[i] != 0.0;
+      S[i + j * n] = st[i + j * n] ? col[i] / deg[j] : 0.0;
+    }
+  }
+  for (int64_t j = 0; j < n; ++j) r[j] = 1.0 / (double)n;
+  const double beta = (1.0 - damp) / (double)n;
+  for (int64_t step = 0; step < nsteps; ++step) {
+    for (int64_t i = 0; i < n; ++i) rank[i] = 0.0;
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = 0; i < n; ++i)
+        if (st[i + j * n]) rank[i] = fma_on ? fma(S[i + j * n], r[j], rank[i]) : rank[i] + S[i + j * n] * r[j];
+    for (int64_t i = 0; i < n; ++i) r[i] = fma_on ? fma(damp, rank[i], beta) : beta + damp * rank[i];
+  }
+  free(deg); free(col); free(rank); free(S); free(st);
+  return 0;
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
