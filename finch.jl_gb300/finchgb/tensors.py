@@ -370,11 +370,12 @@ class Tensor:
 
 
 def _scipy_sparse(x):
-    """x when it is a scipy.sparse matrix or array, else None."""
-    try:
-        import scipy.sparse as sp
-    except ImportError:
+    """x when it is a scipy.sparse matrix or array, else None (scipy is
+    imported only for objects of its own)."""
+    if not type(x).__module__.startswith("scipy.sparse"):
         return None
+    import scipy.sparse as sp
+
     return x if sp.issparse(x) else None
 
 
