@@ -1023,6 +1023,60 @@ def suite_cg_probe() -> list[dict]:
     return out
 
 
+def suite_pagerank() -> list[dict]:
+    """PageRank (docs/examples/pagerank.jl) through finch() on a 4M-vertex
+    Pattern graph with out-degree 1 + Poisson(7) (every vertex has an
+    out-edge, which the example needs): the time per step (Finch-order SpMV
+    + fused affine map) from the difference of 21- and 1-step runs, the
+    setup (out-degree counts, the masked transition matrix, its CSR copy),
+    and the 21-step result against an independent power iteration in
+    scipy."""
+    import torch
+
+    import finchgb as F
+    from finchgb import examples
+    from finchgb.workloads import SparseBuffers, _fibers_from_lengths, _ptr
+
+    rng = np.random.default_rng(SEED + 6)
+    n = 4_000_000
+    lengths = (1 + rng.poisson(7.0, n)).astype(np.int64)
+    rows = _fibers_from_lengths(rng, lengths, n)
+    g = SparseBuffers(n, n, _ptr(lengths), rows + 1, None, "csc")
+    edges = F.Tensor.from_buffers(F.Dense(F.SparseList(F.Pattern())), g)
+    F.transfer(F.gpu(), edges)
+    examples.pagerank(edges, nsteps=2)  # warm-up: contexts, pools
+    torch.cuda.synchronize()
+
+    def wall(k):
+        t0 = time.perf_counter()
+        r = examples.pagerank(edges, nsteps=k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    import scipy.sparse as sp
+
+    t1 = min(wall(1)[0] for _ in range(2))
+    runs = [wall(21) for _ in range(2)]
+    t21, r = min(runs, key=lambda x: x[0])
+    per_step = (t21 - t1) / 20
+    setup = t1 - per_step  # out-degrees, transition matrix and its CSR copy
+    got = r.todense()
+    P = sp.csc_matrix((np.repeat(1.0 / lengths, lengths), rows, g.ptr - 1), shape=(n, n))
+    ref = np.full(n, 1.0 / n)
+    for _ in range(21):
+        ref = (1 - 0.85) / n + 0.85 * (P @ ref)
+    nnz = int(lengths.sum())
+    step_bytes = 4 * (n + 1) + 12 * nnz + 8 * n * 4  # CSR copy, r read, rank written/read, r written
+    return [{"suite": "pagerank", "metric": "pagerank_ms_per_step", "value": round(per_step * 1e3, 3),
+             "unit": "ms", "higher_is_better": False,
+             "config": {"workload": "Pattern graph, 4M vertices, out-degree 1 + Poisson(7)", "nnz": nnz,
+                        "steps": 21, "damp": 0.85},
+             "setup_ms": round(setup * 1e3, 2), "total_ms_21_steps": round(t21 * 1e3, 2),
+             "roofline_per_step": _roof(step_bytes, per_step * 1e3),
+             "max_rel_err_vs_power_iteration": float(np.max(np.abs(got - ref)) / np.max(ref)),
+             "timing": "host wall clock around finch() calls, synchronised"}]
+
+
 def serve_library(n_mats: int = 4096, n_partners: int = 512):
     """4,096 resident CSR matrices, rows log-uniform in [64, 8192], square,
     density U[0.5%, 5%], FP32 N(0,1), generated on the device; the first
@@ -1414,7 +1468,8 @@ def run_suite(args):
     from finchgb import build
 
     build.build()
-    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm, suite_cg_probe):
+    for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm, suite_cg_probe,
+               suite_pagerank):
         if args.suite_only and fn.__name__ not in args.suite_only.split(","):
             continue
         try:

@@ -19,6 +19,7 @@ Matched plans (A sparse, x/B/X/Y dense, s a 0-d Scalar):
 from __future__ import annotations
 
 import contextlib
+import functools
 from dataclasses import dataclass
 
 import numpy as np
@@ -681,6 +682,24 @@ def _rows_of(t) -> dev.DeviceSparse:
     return A if A.orient == "csr" else _csr_copy(t, A)
 
 
+@functools.lru_cache(maxsize=256)
+def _program_tree(program: str):
+    """The FinchNotation tree of a program's text, parsed once per text (as
+    Finch compiles a program once per type signature, src/util/staging.jl:
+    22-79); None when it does not parse."""
+    from . import notation
+
+    try:
+        return notation.parse(program)
+    except SyntaxError:
+        return None
+
+
+@functools.lru_cache(maxsize=256)
+def _finch_program(program: str):
+    return parse_finch(program)
+
+
 def finch(program: str, ctx: GB300Scheduler | None = None, algebra: AbstractAlgebra | None = None,
           **tensors) -> dict:
     """@finch over a loop program; returns {output name: tensor}.
@@ -691,17 +710,14 @@ def finch(program: str, ctx: GB300Scheduler | None = None, algebra: AbstractAlge
     programs with several statements (the choose/minby rounds of Finch's BFS
     and Bellman-Ford examples) are matched as whole programs and update
     their tensors in place."""
-    from . import notation, programs
+    from . import programs
 
-    try:
-        tree = notation.parse(program)
-    except SyntaxError:
-        tree = None
+    tree = _program_tree(program)
     if tree is not None:
         res = programs.run(tree, tensors, _rows_of)
         if res is not None:
             return res
-    prog = parse_finch(program)
+    prog = _finch_program(program)
     plan = parse_einsum(prog.stmt, tensors)
     name = plan.out_name
     sched = _with_algebra(ctx or GB300Scheduler(finch_order=True), algebra)
