@@ -144,7 +144,70 @@ def _kind(fmt) -> str:
 # ---------------------------------------------------------------- tensors
 
 
-class Tensor:
+def _eager(op: str, a, b):
+    """compute() of a lazy `a op b` (src/interface/eager.jl:82-143): numbers
+    stay scalars, arrays and scipy.sparse matrices become tensors."""
+    from .logic import lazy
+    from .scheduler import compute
+
+    def lz(x):
+        if isinstance(x, (int, float, np.integer, np.floating)) and not isinstance(x, (bool, np.bool_)):
+            return x
+        if not isinstance(x, (Tensor, SwizzleArray)):
+            sp_x = _scipy_sparse(x)
+            if sp_x is not None:
+                x = Tensor(sp_x)
+            else:
+                x = np.asarray(x)
+                el = Element(x.dtype.type(0))
+                x = Tensor(Dense(el) if x.ndim == 1 else Dense(Dense(el)), x)
+        return lazy(x)
+
+    la, lb = lz(a), lz(b)
+    if op == "@":
+        return compute(la @ lb)
+    if op == "-" and not hasattr(la, "node"):  # c - x = c + (-1) * x, exactly
+        return compute(lb * -1 + la)
+    if op == "-" and not hasattr(lb, "node"):  # x - c = x + (-c), exactly
+        return compute(la + (-lb))
+    return compute({"+": lambda: la + lb if hasattr(la, "node") else lb + la,
+                    "-": lambda: la - lb,
+                    "*": lambda: la * lb if hasattr(la, "node") else lb * la}[op]())
+
+
+class _EagerOps:
+    """Finch's eager operations on tensors (src/interface/eager.jl:82-143),
+    each the compute() of its lazy form.  `a @ b` is Julia's `a * b` between
+    tensors, tensordot over a's last and b's first index (SpMV, SpMM or
+    SpGEMM); `a * b` is Julia's `a .* b` (with a number, a scale); `+` and
+    `-` are elementwise."""
+
+    def __matmul__(self, other):
+        return _eager("@", self, other)
+
+    def __rmatmul__(self, other):
+        return _eager("@", other, self)
+
+    def __add__(self, other):
+        return _eager("+", self, other)
+
+    def __radd__(self, other):
+        return _eager("+", other, self)
+
+    def __sub__(self, other):
+        return _eager("-", self, other)
+
+    def __rsub__(self, other):
+        return _eager("-", other, self)
+
+    def __mul__(self, other):
+        return _eager("*", self, other)
+
+    def __rmul__(self, other):
+        return _eager("*", other, self)
+
+
+class Tensor(_EagerOps):
     """A Finch tensor: a level format plus its buffers (host or device).
 
     Storage by kind:
@@ -521,7 +584,7 @@ def _as_array(arr, dtype) -> np.ndarray:
     return np.asarray(arr).astype(dtype, copy=False)
 
 
-class SwizzleArray:
+class SwizzleArray(_EagerOps):
     """A permuted view of a tensor (src/tensors/combinators/swizzle.jl).
 
     swizzle(Tensor(Dense(SparseList(...)), A^T), 2, 1) is Finch's CSR of A."""

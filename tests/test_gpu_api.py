@@ -248,3 +248,26 @@ def test_einsum_max_plus_needs_the_annihilating_fill(gpu_lib):
     P = F.Tensor(F.Dense(F.SparseList(F.Element(0.0))), D)  # fill 0 is not max-plus's annihilator
     with pytest.raises(F.FinchGBUnsupported):
         F.einsum("R[i,j] <<max>>= P[i,k] + Q[k,j]", init=-np.inf, P=P, Q=dense2(D))
+
+
+def test_eager_operations(gpu_lib):
+    """The eager forms of test/suites/interface_tests.jl (A * B == C * D,
+    A * x == C * x; src/interface/eager.jl:82-143), with Julia's `*`
+    between tensors written `@` and Python's `*` as Julia's `.*`."""
+    rng = np.random.default_rng(12)
+    A = np.where(rng.random((5, 5)) < 0.5, rng.random((5, 5)), 0.0)
+    B = np.where(rng.random((5, 5)) < 0.5, rng.random((5, 5)), 0.0)
+    x = rng.random(5)
+    C, D = csc(A), csc(B)
+    np.testing.assert_allclose((C @ D).todense(), A @ B, rtol=1e-12, atol=1e-300)  # SpGEMM
+    np.testing.assert_allclose((C @ x).todense(), A @ x, rtol=1e-12, atol=1e-300)  # SpMV, numpy operand
+    np.testing.assert_allclose((C @ vec(x)).todense(), A @ x, rtol=1e-12, atol=1e-300)
+    W = rng.random((5, 3))
+    np.testing.assert_allclose((C @ W).todense(), A @ W, rtol=1e-12, atol=1e-300)  # SpMM
+    np.testing.assert_allclose((F.csr(A) @ W).todense(), A @ W, rtol=1e-12, atol=1e-300)
+    assert (C + D) == A + B and (C * D) == A * B
+    y = vec(x)
+    assert np.array_equal((y * 2.0).todense(), x * 2.0) and np.array_equal((2.0 * y).todense(), 2.0 * x)
+    assert np.array_equal((y + 1.5).todense(), x + 1.5) and np.array_equal((y - 1.5).todense(), x - 1.5)
+    assert np.array_equal((1.5 - y).todense(), 1.5 - x)
+    assert np.array_equal((y + y).todense(), x + x)
