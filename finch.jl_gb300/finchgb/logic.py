@@ -17,6 +17,7 @@ nodes from broadcast, tensordot and sum (src/interface/lazy.jl:207-404);
 from __future__ import annotations
 
 import ast
+import functools
 import itertools
 import re
 from dataclasses import dataclass, field
@@ -128,9 +129,16 @@ _REDUCERS = {"+": "+", "*": "*", "|": "|", "&": "&", "min": "min", "max": "max",
              "and": "&"}
 
 
-def _parse_rhs(src: str, tensors: dict) -> Node:
+@functools.lru_cache(maxsize=512)
+def _rhs_tree(src: str):
+    """The Python syntax tree of a right-hand side, parsed once per text (the
+    names are bound to tensors per call)."""
     src = re.sub(r"(\w+)\[\s*\]", r"\1[()]", src)  # s[] -> s[()]
-    tree = ast.parse(src.strip(), mode="eval").body
+    return ast.parse(src.strip(), mode="eval").body
+
+
+def _parse_rhs(src: str, tensors: dict) -> Node:
+    tree = _rhs_tree(src)
 
     def conv(e):
         if isinstance(e, ast.BinOp) and type(e.op) in _OPS:

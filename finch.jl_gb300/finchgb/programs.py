@@ -245,15 +245,34 @@ def match_masked_scale(prog) -> dict | None:
 # ---------------------------------------------------------------- execution
 
 
+MATCHERS = (("bfs_round", match_bfs_round), ("or_count", match_or_count), ("minby_map", match_minby_map),
+            ("masked_scale", match_masked_scale), ("minby_relax", match_minby_relax))
+
+
+def match(prog) -> tuple | None:
+    """(kind, bindings) of the first whole-program matcher that binds prog,
+    or None.  Depends on the program alone, so callers may keep it."""
+    for kind, fn in MATCHERS:
+        m = fn(prog)
+        if m is not None:
+            return kind, m
+    return None
+
+
 def run(prog, tensors: dict, adjacency_rows) -> dict | None:
     """Runs a matched program on the device; returns {name: tensor} of the
     outputs, or None if no graph program matches.  adjacency_rows(t) gives
     the CSR of a matrix tensor whose row i lists the j with t[i, j] stored."""
+    found = match(prog)
+    return None if found is None else run_matched(found[0], found[1], tensors, adjacency_rows)
+
+
+def run_matched(kind: str, m: dict, tensors: dict, adjacency_rows) -> dict:
+    """Runs a program that match() bound, on the given tensors."""
     from .tensors import dense_from_device
     from .scheduler import FinchGBUnsupported, Scalar, _device_vector
 
-    m = match_bfs_round(prog)
-    if m is not None:
+    if kind == "bfs_round":
         A = adjacency_rows(tensors[m["edges"]])
         F = _device_vector(tensors[m["frontier"]], torch.uint8)
         V = _device_vector(tensors[m["visited"]], torch.uint8)
@@ -262,8 +281,7 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
             raise FinchGBUnsupported("choose: the parent vector must hold Int32 or Int64")
         nxt = dev.bfs_pull(A, F, V, P, choose_fill=int(m["fill"]), index_offset=1)
         return {m["next"]: dense_from_device(nxt, False), m["parent"]: tensors[m["parent"]]}
-    m = match_or_count(prog)
-    if m is not None:
+    if kind == "or_count":
         nxt = _device_vector(tensors[m["next"]], torch.uint8)
         V = _device_vector(tensors[m["visited"]], torch.uint8)
         c = tensors[m["count"]]
@@ -272,18 +290,15 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
         cnt = c.device_value(torch.int64)
         dev.or_count(V, nxt, cnt)
         return {m["visited"]: tensors[m["visited"]], m["count"]: c}
-    m = match_minby_map(prog)
-    if m is not None:
+    if kind == "minby_map":
         mask = None if m["mask"] is None else _device_vector(tensors[m["mask"]], torch.uint8)
         src = tensors[m["src"]].pair_device()
         dst = tensors[m["dst"]].pair_device()
         dev.minby_map(mask, src, dst)
         return {m["dst"]: tensors[m["dst"]]}
-    m = match_masked_scale(prog)
-    if m is not None:
+    if kind == "masked_scale":
         return _run_masked_scale(m, tensors)
-    m = match_minby_relax(prog)
-    if m is not None:
+    if kind == "minby_relax":
         A = adjacency_rows(tensors[m["edges"]])
         dprev = tensors[m["dist_prev"]].pair_device()
         aprev = _device_vector(tensors[m["active_prev"]], torch.uint8)
@@ -292,7 +307,7 @@ def run(prog, tensors: dict, adjacency_rows) -> dict | None:
             raise FinchGBUnsupported("minby: the edge weights and distances must share one type")
         act = dev.minby_relax(A, dprev[0], aprev, dst, index_offset=1)
         return {m["active"]: dense_from_device(act, False), m["dist"]: tensors[m["dist"]]}
-    return None
+    raise ValueError(f"unknown program kind {kind!r}")
 
 
 def _run_masked_scale(m: dict, tensors: dict) -> dict:

@@ -144,10 +144,23 @@ def _constant(n):
     return None
 
 
+_LITERALS: dict = {}
+
+
 def _scalar_tensor(x, like_dtype) -> torch.Tensor:
+    """The device scalar of a Scalar, or of a literal.  A literal's device
+    copy is made once per (value, type, device) and reused: kernels only
+    read these, and a fresh copy costs a synchronous host-to-device
+    transfer per call."""
     if isinstance(x, Scalar):
         return x.t
-    return torch.tensor(x, dtype=like_dtype, device="cuda")
+    key = (type(x), x, like_dtype, torch.cuda.current_device())
+    t = _LITERALS.get(key)
+    if t is None:
+        if len(_LITERALS) >= 1024:
+            _LITERALS.clear()
+        t = _LITERALS[key] = torch.tensor(x, dtype=like_dtype, device="cuda")
+    return t
 
 
 # ---------------------------------------------------------------- matching
@@ -696,6 +709,16 @@ def _program_tree(program: str):
 
 
 @functools.lru_cache(maxsize=256)
+def _program_match(program: str):
+    """The whole-program match of a program's text (programs.match), found
+    once per text."""
+    from . import programs
+
+    tree = _program_tree(program)
+    return None if tree is None else programs.match(tree)
+
+
+@functools.lru_cache(maxsize=256)
 def _finch_program(program: str):
     return parse_finch(program)
 
@@ -712,11 +735,9 @@ def finch(program: str, ctx: GB300Scheduler | None = None, algebra: AbstractAlge
     their tensors in place."""
     from . import programs
 
-    tree = _program_tree(program)
-    if tree is not None:
-        res = programs.run(tree, tensors, _rows_of)
-        if res is not None:
-            return res
+    found = _program_match(program)
+    if found is not None:
+        return programs.run_matched(found[0], found[1], tensors, _rows_of)
     prog = _finch_program(program)
     plan = parse_einsum(prog.stmt, tensors)
     name = plan.out_name
