@@ -157,9 +157,9 @@ def _scalar_tensor(x, like_dtype) -> torch.Tensor:
     key = (type(x), x, like_dtype, torch.cuda.current_device())
     t = _LITERALS.get(key)
     if t is None:
-        if len(_LITERALS) >= 1024:
-            _LITERALS.clear()
-        t = _LITERALS[key] = torch.tensor(x, dtype=like_dtype, device="cuda")
+        t = torch.tensor(x, dtype=like_dtype, device="cuda")
+        if len(_LITERALS) < 1024:  # entries are never dropped: a kernel on any stream may still read one
+            _LITERALS[key] = t
     return t
 
 
