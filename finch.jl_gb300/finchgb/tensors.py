@@ -206,6 +206,14 @@ class _EagerOps:
     def __rmul__(self, other):
         return _eager("*", other, self)
 
+    def sum(self, dims=None):
+        """sum(A; dims) (src/interface/eager.jl:149): dims 1 sums over rows,
+        2 over columns, None everything (a Scalar)."""
+        from .logic import lazy
+        from .scheduler import compute
+
+        return compute(lazy(self).sum(dims=dims))
+
 
 class Tensor(_EagerOps):
     """A Finch tensor: a level format plus its buffers (host or device).

@@ -271,3 +271,6 @@ def test_eager_operations(gpu_lib):
     assert np.array_equal((y + 1.5).todense(), x + 1.5) and np.array_equal((y - 1.5).todense(), x - 1.5)
     assert np.array_equal((1.5 - y).todense(), 1.5 - x)
     assert np.array_equal((y + y).todense(), x + x)
+    np.testing.assert_allclose(C.sum(dims=1).todense(), A.sum(axis=0), rtol=1e-12, atol=0)
+    np.testing.assert_allclose(F.csr(A).sum(dims=2).todense(), A.sum(axis=1), rtol=1e-12, atol=0)
+    np.testing.assert_allclose(float(C.sum().value), A.sum(), rtol=1e-12)
