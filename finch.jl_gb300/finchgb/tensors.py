@@ -147,7 +147,7 @@ def _kind(fmt) -> str:
 def _eager(op: str, a, b):
     """compute() of a lazy `a op b` (src/interface/eager.jl:82-143): numbers
     stay scalars, arrays and scipy.sparse matrices become tensors."""
-    from .logic import lazy
+    from .logic import LazyTensor, lazy
     from .scheduler import compute
 
     def lz(x):
@@ -166,13 +166,17 @@ def _eager(op: str, a, b):
     la, lb = lz(a), lz(b)
     if op == "@":
         return compute(la @ lb)
-    if op == "-" and not hasattr(la, "node"):  # c - x = c + (-1) * x, exactly
-        return compute(lb * -1 + la)
-    if op == "-" and not hasattr(lb, "node"):  # x - c = x + (-c), exactly
-        return compute(la + (-lb))
-    return compute({"+": lambda: la + lb if hasattr(la, "node") else lb + la,
-                    "-": lambda: la - lb,
-                    "*": lambda: la * lb if hasattr(la, "node") else lb * la}[op]())
+    if not isinstance(la, LazyTensor):  # a number on the left: put the tensor first
+        if op == "-":
+            return compute(lb * -1 + la)  # c - x = c + (-1) * x, exactly
+        la, lb = lb, la
+    elif op == "-" and not isinstance(lb, LazyTensor):
+        return compute(la + (-lb))  # x - c = x + (-c), exactly
+    if op == "+":
+        return compute(la + lb)
+    if op == "-":
+        return compute(la - lb)
+    return compute(la * lb)
 
 
 class _EagerOps:
