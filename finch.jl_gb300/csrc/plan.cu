@@ -191,6 +191,8 @@ std::vector<Choice> candidates(const fgb_plan* p) {
   if (d.op == FGB_PLAN_SPMV) {
     if (d.flags & FGB_FINCH_ORDER) return {Choice{1, 0}};
     for (int g : {1, 4, 8, 32}) out.push_back(Choice{g, 0});
+    if (d.semiring != FGB_OR_AND && p->A.orient == FGB_CSR)
+      out.push_back(Choice{2, 0});  // the adaptive pull: one lane per short row, a warp per long one
     if (d.semiring == FGB_OR_AND && p->A.orient == FGB_CSC)
       out.push_back(Choice{0, 0});  // the warp-cooperative push over the true columns
   } else if (d.op == FGB_PLAN_SPMM) {

@@ -55,6 +55,63 @@ __global__ void __launch_bounds__(256) spmv_csr_pull(int64_t nrows, const PtrT* 
   }
 }
 
+// CSR pull with lanes per row chosen row by row: a warp owns 32 consecutive
+// rows; a row of at most SPMV_LONG entries is folded by its own lane (j
+// ascending, one running value, as G = 1), and the warp's longer rows are
+// then folded one after another by all 32 lanes (lane-strided, xor-shuffle
+// combine, as G = 32).  Uniform short rows run at one lane per row, the long
+// rows of a skewed matrix still spread over a warp, and the host needs no
+// row-length statistics.  Not for OR-AND (its pull stops at the first true
+// product).
+constexpr int SPMV_LONG = 32;
+
+template <int SR, class VT, class A, class PtrT, bool PATTERN>
+__global__ void __launch_bounds__(256) spmv_csr_adaptive(int64_t nrows, const PtrT* __restrict__ ptr,
+                                                         const int* __restrict__ idx,
+                                                         const VT* __restrict__ val,
+                                                         const A* __restrict__ x, A* __restrict__ y,
+                                                         int base, int accumulate, int fm) {
+  using S = Semi<SR, A>;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r0 = warp * 32; r0 < nrows; r0 += nwarps * 32) {  // warp-uniform
+    const int64_t row = r0 + lane;
+    int64_t p0 = 0, p1 = 0;
+    if (row < nrows) {
+      p0 = ld_ptr(ptr, row) - base;
+      p1 = ld_ptr(ptr, row + 1) - base;
+    }
+    const bool is_long = p1 - p0 > SPMV_LONG;
+    if (row < nrows && !is_long) {
+      A acc = accumulate ? y[row] : S::identity();
+#pragma unroll 4
+      for (int64_t p = p0; p < p1; ++p) {
+        const int j = __ldg(idx + p) - base;
+        const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
+        acc = S::step(acc, a, __ldg(x + j), fm);
+      }
+      y[row] = acc;
+    }
+    unsigned longs = __ballot_sync(FULL, is_long);
+    while (longs) {
+      const int l = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const int64_t q0 = __shfl_sync(FULL, p0, l), q1 = __shfl_sync(FULL, p1, l);
+      A acc = S::identity();
+      for (int64_t p = q0 + lane; p < q1; p += 32) {
+        const int j = __ldg(idx + p) - base;
+        const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
+        acc = S::step(acc, a, __ldg(x + j), fm);
+      }
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) acc = S::add(acc, shfl_xor(FULL, acc, m, 32));
+      if (lane == 0) y[r0 + l] = accumulate ? S::add(y[r0 + l], acc) : acc;
+    }
+  }
+}
+
 template <int SR, class VT, class A, class PtrT, int G, bool PATTERN>
 __global__ void __launch_bounds__(256) spmv_csc_push(int64_t ncols, const PtrT* __restrict__ ptr,
                                                      const int* __restrict__ idx,
@@ -149,8 +206,10 @@ __global__ void fill_identity(A* __restrict__ y, int64_t n) {
 }
 
 // Lanes per fiber chosen by the plan autotuner for the calls it times and
-// captures (0 = the heuristic below); set only around those calls.
+// captures (0 = the heuristic below, 2 = the adaptive pull); set only around
+// those calls.
 static thread_local int t_group_override = 0;
+constexpr int SPMV_ADAPTIVE = 2;
 
 static int pick_group(double avg) {
   if (avg <= 2.0) return 1;
@@ -175,8 +234,23 @@ static int launch_typed(fgb_ctx* ctx, const fgb_sparse* A_, const void* x, void*
     if (flags & FGB_NO_FMA) fm = FM_NOFMA;
     if (flags & FGB_FMA) fm = FM_FMA;
     int G = (flags & FGB_FINCH_ORDER) ? 1 : (t_group_override > 0 ? t_group_override : pick_group(avg));
-    int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
+    // Without a plan, a matrix with rows enough to fill the device at one
+    // lane per row takes the adaptive pull: on millions of uniform rows of
+    // 2 to 24 entries one lane per row beat 4 or 8 lanes by 30-50 %
+    // (GB300, FP64), and its long rows still get a warp each.
+    if (!(flags & FGB_FINCH_ORDER) && t_group_override <= 0 && SR != SR_OA &&
+        nf >= (int64_t)ctx->num_sms * 2048)
+      G = SPMV_ADAPTIVE;
     if (nf == 0) return FGB_OK;
+    if constexpr (SR != SR_OA) {
+      if (G == SPMV_ADAPTIVE) {
+        const int grid = grid_for((nf + 31) / 32 * 32, threads, ctx->num_sms, 8);
+        spmv_csr_adaptive<SR, VT, A, PtrT, PATTERN><<<grid, threads, 0, s>>>(nf, ptr, idx, val, (const A*)x,
+                                                                             (A*)y, base, accumulate, fm);
+        return check_launch("spmv_csr_adaptive");
+      }
+    }
+    int grid = grid_for(nf * G, threads, ctx->num_sms, 8);
 #define FGB_PULL(GG)                                                                    \
   spmv_csr_pull<SR, VT, A, PtrT, GG, PATTERN><<<grid, threads, 0, s>>>(                 \
       nf, ptr, idx, val, (const A*)x, (A*)y, base, accumulate, fm)

@@ -248,7 +248,10 @@ FGB_API int fgb_coo_assemble(fgb_ctx* ctx, int64_t nrows, int64_t ncols, int64_t
  * CSR runs as a pull (one running value per row); CSC runs as a push with
  * atomic updates of y (order-independent for exact semirings).  With
  * FGB_FINCH_ORDER on a CSR matrix every y[i] is one sequential sum over j
- * ascending, which equals Finch's serial CSC nest bit for bit. */
+ * ascending, which equals Finch's serial CSC nest bit for bit.  Otherwise a
+ * CSR matrix with at least 2048 rows per SM takes the adaptive pull (one
+ * lane per row of at most 32 entries, a warp per longer row), and a smaller
+ * one a fixed number of lanes per row chosen by its mean row length. */
 FGB_API int fgb_spmv(fgb_ctx* ctx, int semiring, const fgb_sparse* A, const void* x, int x_t, void* y,
              int y_t, unsigned flags, void* stream);
 
@@ -548,7 +551,9 @@ typedef struct fgb_plan_desc {
 } fgb_plan_desc;
 
 typedef struct fgb_plan_info {
-  int32_t lanes;             /* chosen lanes per fiber / row group / entry */
+  int32_t lanes;             /* chosen lanes per fiber / row group / entry; for a
+                                CSR SpMV, 2 is the adaptive pull (one lane per row
+                                of at most 32 entries, a warp per longer row) */
   int32_t bands;             /* SpMM/SDDMM virtual rows: column bands (1 = none) */
   int64_t path;              /* chosen merge-path item (SpMM) or entry chunk (SDDMM) */
   double tuned_ms;           /* time of the chosen schedule (-1 if not tuned) */

@@ -223,6 +223,57 @@ def test_short_row_blocks(gpu_lib, sr, dtype):
         assert_close(y, want, abs_terms(b, x), np.float32)
 
 
+@pytest.mark.parametrize("sr,dtype", [(L.PLUS_TIMES, np.float64), (L.PLUS_TIMES, np.float32),
+                                      (L.MIN_PLUS, np.int32), (L.MAX_PLUS, np.int64),
+                                      (L.PLUS_TIMES, np.int64)])
+def test_adaptive_pull_on_many_rows(gpu_lib, sr, dtype):
+    """A CSR with more rows than 2048 per SM takes the adaptive pull without a
+    plan: short rows one lane each, rows over 32 entries a warp each.  Rows of
+    0 to ~15 entries, 64 rows of 33 to 3000 entries, a partial last warp;
+    exact semirings bit for bit (accumulating too), float sums within the
+    bound.  A plan over the same matrix picks one of its candidates, the
+    adaptive pull among them, and gives the same result."""
+    from finchgb.plan import Plan
+    from finchgb.workloads import _fibers_from_lengths, _ptr
+
+    rng = np.random.default_rng(90 + sr)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    m, n = sms * 2048 + 1013, 60_000
+    lengths = rng.poisson(4.0, m).astype(np.int64)
+    lengths[rng.choice(m, 64, replace=False)] = rng.integers(33, 3001, 64)
+    lengths[5 * 32:6 * 32] = 0  # a warp of empty rows
+    cols = _fibers_from_lengths(rng, lengths, n)
+    b = SparseBuffers(m, n, _ptr(lengths), cols + 1, None, "csr")
+    if np.dtype(dtype).kind == "i":
+        info = np.iinfo(dtype)
+        b.val = rng.integers(info.min // 2, info.max // 2, size=b.nnz, dtype=dtype)
+        x = rng.integers(info.min // 2, info.max // 2, size=n, dtype=dtype)
+    else:
+        b.val = rng.standard_normal(b.nnz).astype(dtype)
+        x = rng.standard_normal(n).astype(dtype)
+    A = upload(b)
+    y = to_host(dev.spmv(A, to_dev(x), semiring=sr))
+    want = oracle_spmv(sr, b, x)
+    if np.dtype(dtype).kind == "i":
+        assert np.array_equal(y, want)
+        y0 = rng.integers(-1000, 1000, size=m).astype(dtype)
+        yd = to_dev(y0)
+        dev.spmv(A, to_dev(x), yd, semiring=sr, flags=L.ACCUMULATE)
+        add = {L.MIN_PLUS: np.minimum, L.MAX_PLUS: np.maximum}.get(sr)
+        exp = (y0.astype(np.int64) + want.astype(np.int64)).astype(dtype) if add is None else add(y0, want)
+        assert np.array_equal(to_host(yd), exp)
+    else:
+        assert_close(y, want, abs_terms(b, x), dtype)
+    xd, yp = to_dev(x), torch.empty(m, dtype=to_dev(x).dtype, device="cuda")
+    plan = Plan.spmv(A, xd, yp, semiring=sr, tune_reps=2)
+    assert plan.info()["lanes"] in (1, 2, 4, 8, 32)
+    plan.execute()
+    if np.dtype(dtype).kind == "i":
+        assert np.array_equal(to_host(yp), want)
+    else:
+        assert_close(to_host(yp), want, abs_terms(b, x), dtype)
+
+
 @pytest.mark.parametrize("ptr_i64", [False, True])
 def test_edge_cases(gpu_lib, ptr_i64):
     # empty matrix, empty fibers, a long fiber, 1x1
