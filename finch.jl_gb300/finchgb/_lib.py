@@ -162,6 +162,8 @@ SIGNATURES: dict[str, tuple] = {
                               c_void_p]),
     "fgb_dense_affine": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
+    "fgb_reduce_minmax": (c_int, [c_void_p, c_int, c_int, POINTER(FgbSparse), c_void_p, c_void_p, c_void_p,
+                                  c_void_p]),
     "fgb_sparse_scale": (c_int, [c_void_p, POINTER(FgbSparse), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                  c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(c_int64),
                                  POINTER(c_int64), c_void_p]),

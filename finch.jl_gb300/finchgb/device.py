@@ -395,6 +395,24 @@ def dense_affine(alpha: torch.Tensor | None, x: torch.Tensor | None, beta: torch
     return out
 
 
+_NP_OF = {torch.float64: np.float64, torch.float32: np.float32, torch.int64: np.int64, torch.int32: np.int32}
+
+
+def reduce_minmax(op: int, dims: int, A: DeviceSparse, fill, init=None) -> torch.Tensor:
+    """reduce(max | min, A; dims) with A's fill folded where it stores
+    nothing (fgb_reduce_minmax); dims 1 needs A stored CSC, 2 CSR, 0 either.
+    init None: Finch's initial value (-Inf / typemin for max)."""
+    length = 1 if dims == 0 else (A.ncols if dims == 1 else A.nrows)
+    y = torch.empty(length, dtype=A.val.dtype, device=A.idx.device)
+    npt = _NP_OF[A.val.dtype]
+    f = np.array([fill], dtype=npt)
+    i0 = None if init is None else np.array([init], dtype=npt)
+    desc = A.desc()
+    L.call("fgb_reduce_minmax", _ctx_for(A.idx), op, dims, ctypes.byref(desc), f.ctypes.data,
+           None if i0 is None else i0.ctypes.data, _dptr(y), stream_ptr())
+    return y
+
+
 def sparse_scale(A: DeviceSparse, by: torch.Tensor, by_axis: int, keep: torch.Tensor | None = None,
                  keep_axis: int = L.AXIS_ROW, op: int = L.MAP_DIV,
                  out_dtype: torch.dtype = torch.float64) -> tuple[DeviceSparse, int]:

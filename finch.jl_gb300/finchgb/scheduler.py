@@ -247,7 +247,8 @@ class GB300Scheduler:
     def __call__(self, plan: Node, out=None, accumulate=False):
         m = _decompose(plan)
         for rule in (self._spmv, self._spmm, self._spmm_semiring, self._spgemm, self._sddmm, self._ewise,
-                     self._ewise_reduce, self._dot, self._dense_map, self._dense_fill, self._scalar):
+                     self._ewise_reduce, self._reduce_minmax, self._dot, self._dense_map, self._dense_fill,
+                     self._scalar):
             r = rule(m, out, accumulate)
             if r is not None:
                 if self.verbose:
@@ -481,6 +482,34 @@ class GB300Scheduler:
         dims = 0 if not m.outs else (2 if m.outs == (i,) else 1)
         self.last_kernel = "fgb_ewise_reduce"
         y = dev.ewise_reduce(dims, Ad, B=Bs, B_dense=Bdn)
+        if dims == 0:
+            return Scalar(y.reshape(()))
+        return dense_from_device(y)
+
+    # -- y[j] <<max|min>>= A[i,j] (or over both indices): reduce(max|min, A; dims),
+    #    the fill folded where A stores nothing, so any fill is exact
+    def _reduce_minmax(self, m: Match, out, accumulate):
+        if m.agg not in ("max", "min") or (out is not None and accumulate):
+            return None
+        a = m.core
+        if not (isinstance(a, Access) and _is_sparse(a.tns) and len(a.idxs) == 2) or len(m.outs) > 1:
+            return None
+        i, j = a.idxs
+        if set(m.outs) | set(m.red) != {i, j}:
+            return None
+        Ad = sparse_operand(a.tns, a.idxs, (i, j))
+        if Ad.val is None or Ad.val.dtype not in (torch.float64, torch.float32, torch.int64, torch.int32):
+            return None
+        dims = 0 if not m.outs else (1 if m.outs == (j,) else 2)
+        want = {1: "csc", 2: "csr"}.get(dims, Ad.orient)
+        if Ad.orient != want:
+            Ad = _other_orientation(a.tns, Ad)
+        fill = (a.tns.body if isinstance(a.tns, SwizzleArray) else a.tns).fill_value
+        init = m.init
+        if init is not None and not Ad.val.dtype.is_floating_point and isinstance(init, float) and np.isinf(init):
+            init = None  # -Inf / +Inf: typemin / typemax for integers
+        self.last_kernel = "fgb_reduce_minmax"
+        y = dev.reduce_minmax(L.MAP_MAX if m.agg == "max" else L.MAP_MIN, dims, Ad, fill, init)
         if dims == 0:
             return Scalar(y.reshape(()))
         return dense_from_device(y)

@@ -218,6 +218,21 @@ class _EagerOps:
 
         return compute(lazy(self).sum(dims=dims))
 
+    def maximum(self, dims=None):
+        """maximum(A; dims) (src/interface/eager.jl:156-158): reduce(max, A; dims),
+        the fill counted where nothing is stored."""
+        from .logic import lazy, reduce
+        from .scheduler import compute
+
+        return compute(reduce("max", lazy(self), dims))
+
+    def minimum(self, dims=None):
+        """minimum(A; dims) (src/interface/eager.jl:153-155): reduce(min, A; dims)."""
+        from .logic import lazy, reduce
+        from .scheduler import compute
+
+        return compute(reduce("min", lazy(self), dims))
+
 
 class Tensor(_EagerOps):
     """A Finch tensor: a level format plus its buffers (host or device).

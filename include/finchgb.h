@@ -403,6 +403,21 @@ FGB_API int fgb_ewise_count(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb
 FGB_API int fgb_ewise_fill(fgb_ctx* ctx, int op, const fgb_sparse* A, const fgb_sparse* B,
                    const int64_t* out_ptr, int32_t* out_idx, void* out_val, void* stream);
 
+/* reduce(op, A; dims) for op FGB_MAP_MIN or FGB_MAP_MAX -- maximum(A; dims)
+ * and minimum(A; dims) (src/interface/eager.jl:153-158) -- of a sparse A
+ * whatever its fill: every output folds its stored entries in coordinate
+ * order and the fill `*fill` (one host element of val_t) once where a gap
+ * or the end of the fiber leaves coordinates unstored, which is Finch's
+ * fold with its fill runs folded once (min and max are idempotent), so the
+ * results are Finch's bit for bit, @fastmath's first-operand rule for NaN
+ * and signed zeros included.  The fold starts from `*init` (NULL: -Inf or
+ * typemin for max, +Inf or typemax for min).  dims 1 reduces over rows
+ * (y has ncols elements; A stored CSC), dims 2 over columns (nrows; A
+ * stored CSR), dims 0 everything (one element; fibers in storage order).
+ * y has A's value type: F64, F32, I64 or I32. */
+FGB_API int fgb_reduce_minmax(fgb_ctx* ctx, int op, int dims, const fgb_sparse* A, const void* fill,
+                              const void* init, void* y, void* stream);
+
 /* Fused elementwise multiply + reduction:
  *   dims = 2:  y[i] = sum_j A[i,j] * B[i,j]      (length m)
  *   dims = 1:  y[j] = sum_i A[i,j] * B[i,j]      (length n)

@@ -90,6 +90,8 @@ def lib(fast: bool = False) -> ctypes.CDLL:
             L.orc_minby_round.restype = None
             L.orc_pagerank.argtypes = [i64, vp, vp, vp, i64, ctypes.c_double, i32, vp]
             L.orc_pagerank.restype = i32
+            L.orc_reduce_minmax.argtypes = [i32, i32, i64, i64, vp, vp, vp, ctypes.c_double, ctypes.c_double, vp]
+            L.orc_reduce_minmax.restype = None
             if fast:
                 _fast_lib = L
             else:
@@ -261,6 +263,17 @@ def pagerank(n, ptr, idx, w=None, nsteps=20, damp=0.85, fma=False):
     if rc != 0:
         raise MemoryError(f"oracle pagerank: {n} x {n} scratch")
     return r
+
+
+def reduce_minmax(is_max, dims, m, n, ptr, idx, val, fill, init=None):
+    """reduce(max | min, A; dims) of the CSC (ptr, idx, val) with fill `fill`,
+    every coordinate folded in Finch's order (orc_reduce_minmax); float64."""
+    if init is None:
+        init = -np.inf if is_max else np.inf
+    y = np.zeros(n if dims == 1 else (m if dims == 2 else 1), dtype=np.float64)
+    lib().orc_reduce_minmax(int(bool(is_max)), int(dims), m, n, _p(_i64(ptr)), _p(_i64(idx)),
+                            _p(np.ascontiguousarray(val, dtype=np.float64)), float(fill), float(init), _p(y))
+    return y
 
 
 def minby_round(n, ptr, idx, w, dprev, pprev, aprev, dist, par):

@@ -683,6 +683,30 @@ int orc_pagerank(int64_t n, const int64_t* ptr, const int64_t* idx, const double
   return 0;
 }
 
+/* reduce(max | min, A; dims) as Finch's loop runs it (src/interface/eager.jl:
+ * 153-158 lowered like the sum of test/reference64/interface/
+ * reduce_default.txt): over the CSC of A, j outer and i inner, every
+ * (i, j) folds -- the stored value, or the fill -- with @fastmath's
+ * first-operand max/min (the second operand wins only when strictly larger
+ * / smaller), from init.  dims 1: y[j] over i; dims 2: y[i] over j; dims 0:
+ * y[0] over everything in that order.  Values as doubles. */
+void orc_reduce_minmax(int is_max, int dims, int64_t m, int64_t n, const int64_t* ptr, const int64_t* idx,
+                       const double* val, double fill, double init, double* y) {
+  double* col = (double*)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+  const int64_t ny = dims == 1 ? n : (dims == 2 ? m : 1);
+  for (int64_t k = 0; k < ny; ++k) y[k] = init;
+  for (int64_t j = 0; j < n; ++j) {
+    for (int64_t i = 0; i < m; ++i) col[i] = fill;
+    for (int64_t q = ptr[j] - 1; q < ptr[j + 1] - 1; ++q) col[idx[q] - 1] = val[q];
+    for (int64_t i = 0; i < m; ++i) {
+      double* acc = dims == 1 ? &y[j] : (dims == 2 ? &y[i] : &y[0]);
+      const double v = col[i];
+      if (is_max ? (v > *acc) : (v < *acc)) *acc = v;
+    }
+  }
+  free(col);
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
