@@ -1023,6 +1023,42 @@ def suite_cg_probe() -> list[dict]:
     return out
 
 
+def suite_spmv_adaptive() -> list[dict]:
+    """The per-call CSR SpMV (no plan), FP64, on the 1M x 1M Zipf matrix
+    (16M entries) and on 4M rows of Poisson(8) entries: at these row counts
+    the library's default is the adaptive pull (one lane per row of at most
+    32 entries, a warp per longer row).  Device time per call from CUDA-graph
+    replays, and the plan autotuner's choice over 1, 4, 8 or 32 lanes per
+    row and the adaptive pull (lanes 2) with its time."""
+    import torch
+
+    from finchgb import _lib as L
+    from finchgb import device as dev
+    from finchgb.plan import Plan
+    from finchgb.workloads import _fibers_from_lengths, _ptr, zipf_csr
+
+    rng = np.random.default_rng(SEED + 7)
+    z = zipf_csr(rng, 1_000_000, 1_000_000, mean=16, a=1.5, cap=50_000, dtype=np.float64)
+    lengths = rng.poisson(8.0, 4_000_000).astype(np.int64)
+    cols = _fibers_from_lengths(rng, lengths, 4_000_000)
+    out = []
+    for name, (m, n, ptr, idx, val) in (
+            ("zipf1.5_1Mx1M_nnz16M", (z.nrows, z.ncols, z.ptr, z.idx, z.val)),
+            ("poisson8_4Mx4M", (4_000_000, 4_000_000, _ptr(lengths), cols + 1, rng.random(int(lengths.sum()))))):
+        A = dev.DeviceSparse.from_host(m, n, ptr, idx, val, orient="csr")
+        x = torch.rand(n, dtype=torch.float64, device="cuda")
+        y = torch.empty(m, dtype=torch.float64, device="cuda")
+        ms = _graph_ms(lambda: dev.spmv(A, x, y), reps=20)
+        nbytes = 4 * (m + 1) + 12 * A.nnz + 8 * n + 8 * m
+        plan = Plan.spmv(A, x, y, tune_reps=5)
+        out.append({"suite": "spmv_adaptive", "workload": name, "nnz": int(A.nnz), "dtype": "f64",
+                    "us_per_call": round(ms * 1e3, 1), "roofline": _roof(nbytes, ms),
+                    "plan_lanes": plan.info()["lanes"], "plan_us": round(plan.info()["tuned_ms"] * 1e3, 1)})
+        del A, plan
+        torch.cuda.empty_cache()
+    return out
+
+
 def suite_pagerank() -> list[dict]:
     """PageRank (docs/examples/pagerank.jl) through finch() on a 4M-vertex
     Pattern graph with out-degree 1 + Poisson(7) (every vertex has an
@@ -1469,7 +1505,7 @@ def run_suite(args):
 
     build.build()
     for fn in (suite_spmv_fp64, suite_semiring, suite_cg, suite_sddmm, suite_coo, suite_spgemm, suite_cg_probe,
-               suite_pagerank):
+               suite_pagerank, suite_spmv_adaptive):
         if args.suite_only and fn.__name__ not in args.suite_only.split(","):
             continue
         try:

@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(256) spmv_csr_adaptive(int64_t nrows, const Pt
       longs &= longs - 1;
       const int64_t q0 = __shfl_sync(FULL, p0, l), q1 = __shfl_sync(FULL, p1, l);
       A acc = S::identity();
+#pragma unroll 4
       for (int64_t p = q0 + lane; p < q1; p += 32) {
         const int j = __ldg(idx + p) - base;
         const A a = PATTERN ? S::one() : to_acc<A>(val[p]);
